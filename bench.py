@@ -1,0 +1,381 @@
+"""Benchmark of the contraction hot path on one GB300 (replicas on N GPUs).
+
+Workload (default): the single large pairwise contraction. A has rank 27 and
+B rank 25, all index dimensions 2, with 13 shared labels: a complex GEMM of
+M = 2^14, N = 2^12, K = 2^13. Both operands' labels are seeded-randomly
+permuted, so both need a transpose. Entries are complex64 with real and
+imaginary parts i.i.d. N(0, 1/2), scaled by 2^-10 (synthetic, seeded).
+
+One step = Tensor::ContractTensors on the device in the TF32x3 tensor-core
+form: permute+split A, permute+split B, tcgen05 GEMM. Metric: effective
+TFLOP/s = 4 x PathInfo flops / step time = 8 M N K / t. Inputs (1.34 GB) are
+larger than L2 (129 MB), so no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+`--impl reference` times the reference's CPU algorithm (the oracle port:
+DefaultPermuter restated in C with OpenMP plus OpenBLAS cgemm through numpy)
+on a bounded sample of the same contraction (s common labels fixed, so the
+transposes and the GEMM shrink by the same factor).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_LEFT, N_COMMON, N_RIGHT = 14, 13, 12
+SEED = 20240601
+METRIC = "slices/s & eff. TFLOP/s: TC-split vs plain FP32 on GB300 at ≤1e-5 rel err"
+
+
+def _perm(seed, r):
+    return [int(i) for i in np.random.default_rng(seed).permutation(r)]
+
+
+def workload(n_left=N_LEFT, n_common=N_COMMON, n_right=N_RIGHT):
+    """Labels, shapes and the axis orders ContractTensors derives from them."""
+    left = ["l%d" % i for i in range(n_left)]
+    common = ["c%d" % i for i in range(n_common)]
+    right = ["r%d" % i for i in range(n_right)]
+    a_lab = [(left + common)[i] for i in _perm(SEED, n_left + n_common)]
+    b_lab = [(common + right)[i] for i in _perm(SEED + 1, n_common + n_right)]
+    # Tensor::ContractTensors label algebra: left = A\B, common = A∩B (A order).
+    lft = [x for x in a_lab if x not in b_lab]
+    rgt = [x for x in b_lab if x not in a_lab]
+    com = [x for x in a_lab if x in b_lab]
+    a_perm = [a_lab.index(x) for x in lft + com]            # A -> (left, common)
+    b_perm_kn = [b_lab.index(x) for x in com + rgt]         # B -> (common, right)
+    b_perm_nk = [b_lab.index(x) for x in rgt + com]         # B -> (right, common)
+    return dict(a_lab=a_lab, b_lab=b_lab, a_shape=[2] * len(a_lab), b_shape=[2] * len(b_lab),
+                a_perm=a_perm, b_perm_kn=b_perm_kn, b_perm_nk=b_perm_nk,
+                m=2 ** n_left, n=2 ** n_right, k=2 ** n_common)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = []
+        for i, nm in enumerate(names):
+            if any(r[5 + i].lower().startswith("active") for r in rows):
+                reasons.append(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_sample(nthreads=0, s_common=1, reps=3):
+    """The oracle port on the config with s_common shared labels fixed."""
+    import numpy as np
+
+    from oracle import port
+
+    w = workload(N_LEFT, N_COMMON - s_common, N_RIGHT)
+    rng = np.random.default_rng(SEED)
+    na, nb = 2 ** len(w["a_lab"]), 2 ** len(w["b_lab"])
+    a = ((rng.standard_normal(na) + 1j * rng.standard_normal(na)) * np.sqrt(0.5) * 2**-10).astype(np.complex64)
+    b = ((rng.standard_normal(nb) + 1j * rng.standard_normal(nb)) * np.sqrt(0.5) * 2**-10).astype(np.complex64)
+    port.contract(a, w["a_shape"], w["a_perm"], b, w["b_shape"], w["b_perm_kn"], w["m"], w["n"],
+                  w["k"], nthreads)  # warm-up
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        port.contract(a, w["a_shape"], w["a_perm"], b, w["b_shape"], w["b_perm_kn"], w["m"],
+                      w["n"], w["k"], nthreads)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    flops = 8.0 * w["m"] * w["n"] * w["k"]
+    return {"value": flops / t / 1e12, "unit": "TFLOP/s", "cores": port.max_threads(),
+            "kind": "port",
+            "sample": "config-1 contraction with %d of 13 shared labels fixed (M=2^14, N=2^12, "
+                      "K=2^%d), median of %d runs, %.2f s each" % (s_common, N_COMMON - s_common,
+                                                                  reps, t)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    steps = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_sample(s_common=2, reps=1)
+        if i >= args.warmup:
+            steps.append(info["value"])
+    value = statistics.median(steps)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
+            "config": {"workload": "config 1: rank-27 x rank-25 contraction, 13 shared labels "
+                                   "(M=2^14, N=2^12, K=2^13), complex64",
+                       "sample": info["sample"]},
+            "cpu_baseline": dict(info, value=value),
+            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import jet_gb300.capi as capi
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    w = workload()
+    m, n, k = w["m"], w["n"], w["k"]
+    kp = k
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + rank)
+    # torch.randn on complex draws re, im i.i.d. N(0, 1/2).
+    A = torch.randn(2 ** 27, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
+    B = torch.randn(2 ** 25, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
+    pa = torch.empty(4 * m * kp, dtype=torch.float32, device=dev)
+    pb = torch.empty(4 * n * kp, dtype=torch.float32, device=dev)
+    C = torch.empty(m * n, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(events=None):
+        if events:
+            events[0].record(stream)
+        capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
+        if events:
+            events[1].record(stream)
+        capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, stream=stream)
+        if events:
+            events[2].record(stream)
+        capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
+        if events:
+            events[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if capi.take_device_status() != 0:
+        raise RuntimeError("device status reports a timeout in the warm-up")
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with Clocks(local_rank) as clk:
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            step(evs[s])
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.summary()
+    split_a = [e[0].elapsed_time(e[1]) for e in evs]
+    split_b = [e[1].elapsed_time(e[2]) for e in evs]
+    gemm = [e[2].elapsed_time(e[3]) for e in evs]
+    total = evs[0][0].elapsed_time(evs[-1][3])
+    ms_step = total / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    flops = 8.0 * m * n * k  # = 4 x PathInfo flops (size(C) * 2 * K)
+    value = world * flops / (ms_step * 1e-3) / 1e12
+
+    # Accuracy of this step's C against complex128 on 32 rows.
+    rows = 32
+    At = capi.permute(A, w["a_shape"], w["a_perm"]).view(m, k)[:rows].cpu().numpy()
+    Bt = capi.permute(B, w["b_shape"], w["b_perm_kn"]).view(k, n).cpu().numpy()
+    ref_rows = At.astype(np.complex128) @ Bt.astype(np.complex128)
+    got_rows = C.view(m, n)[:rows].cpu().numpy()
+    rel_err = float(np.linalg.norm(got_rows - ref_rows) / np.linalg.norm(ref_rows))
+
+    # Plain FP32 form of the same step (permute + SIMT complex GEMM), 2 runs.
+    ws_need = capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
+                                           w["b_perm_kn"], m, n, k, capi.C64, capi.PREC_FP32)
+    ws = torch.empty(ws_need, dtype=torch.uint8, device=dev)
+    C2 = torch.empty_like(C)
+    capi.contract(A, w["a_shape"], w["a_perm"], B, w["b_shape"], w["b_perm_kn"], m, n, k,
+                  precision=capi.PREC_FP32, out=C2, workspace=ws, stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(2):
+        capi.contract(A, w["a_shape"], w["a_perm"], B, w["b_shape"], w["b_perm_kn"], m, n, k,
+                      precision=capi.PREC_FP32, out=C2, workspace=ws, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = e0.elapsed_time(e1) / 2
+    plain_err = float(np.linalg.norm(C2.view(m, n)[:rows].cpu().numpy() - ref_rows)
+                      / np.linalg.norm(ref_rows))
+    del ws, C2
+
+    # End to end through the public API with host buffers: pinned A, B in,
+    # C out, every step.
+    hA = A.cpu().pin_memory()
+    hB = B.cpu().pin_memory()
+    hC = torch.empty(C.shape, dtype=C.dtype).pin_memory()
+    dA, dB = torch.empty_like(A), torch.empty_like(B)
+    ws_tc = torch.empty(capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
+                                                     w["b_perm_kn"], m, n, k, capi.C64,
+                                                     capi.PREC_TF32X3),
+                        dtype=torch.uint8, device=dev)
+    del pa, pb
+
+    def e2e_step():
+        dA.copy_(hA, non_blocking=True)
+        dB.copy_(hB, non_blocking=True)
+        capi.contract(dA, w["a_shape"], w["a_perm"], dB, w["b_shape"], w["b_perm_kn"], m, n, k,
+                      precision=capi.PREC_TF32X3, out=C, workspace=ws_tc, stream=stream)
+        hC.copy_(C, non_blocking=True)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    e2e_steps = max(2, min(args.steps, 5))
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_value = world * flops / (e2e_ms * 1e-3) / 1e12
+
+    hbm_peak, bf16_peak, peak_src = measured_peaks()
+    tf32_peak = bf16_peak / 2.0
+    gemm_ms = statistics.mean(gemm)
+    split_ms = statistics.mean(split_a)
+    split_bytes = 24.0 * m * k  # read 8 B, write 4 planes x 4 B per element
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 (fp32 data, TF32x3 tensor-core products, fp32 accumulate)",
+        "data": "synthetic (seeded N(0,1/2) * 2^-10 complex64)",
+        "config": {"workload": "config 1: rank-27 x rank-25 contraction, 13 shared labels, "
+                               "seeded label permutations (M=2^14, N=2^12, K=2^13)",
+                   "form": "TF32x3 4M", "l2": "inputs 1.34 GB > L2, no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "rel_err_vs_fp64": rel_err,
+        "stages_ms": {"split_a": split_ms, "split_b": statistics.mean(split_b),
+                      "gemm_tf32x3": gemm_ms},
+        "plain_fp32": {"ms_per_step": plain_ms,
+                       "value": world * flops / (plain_ms * 1e-3) / 1e12,
+                       "rel_err_vs_fp64": plain_err},
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_tf32x3_kernel",
+                     "achieved": flops / (gemm_ms * 1e-3) / 1e12,
+                     "peak": tf32_peak, "unit": "TFLOP/s",
+                     "frac": flops / (gemm_ms * 1e-3) / 1e12 / tf32_peak,
+                     "tensor_pipe_frac": 3 * flops / (gemm_ms * 1e-3) / 1e12 / tf32_peak,
+                     "peak_source": "TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak),
+                     "traffic": None},
+        "roofline_split": {"bound": "hbm", "kernel": "bitperm_kernel (split store)",
+                           "achieved": split_bytes / (split_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                           "unit": "GB/s",
+                           "frac": split_bytes / (split_ms * 1e-3) / 1e9 / hbm_peak,
+                           "peak_source": peak_src},
+        "e2e": {"value": e2e_value, "unit": "TFLOP/s",
+                "h2d_bytes_per_step": int(A.numel() * 8 + B.numel() * 8),
+                "d2h_bytes_per_step": int(C.numel() * 8), "ms_per_step": e2e_ms},
+        "gpu_launches": 3 * args.steps,
+        "wall_s_timed": wall,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_sample()
+        except Exception as e:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

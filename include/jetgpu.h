@@ -1,0 +1,205 @@
+/*
+ * jetgpu.h -- C-ABI of the GB300 (sm_103a) tensor-network contraction library.
+ *
+ * This is the drop-in boundary for Jet's contraction hot path. Every entry
+ * point takes plain device pointers, sizes and a cudaStream_t passed as
+ * `void *` (NULL = legacy default stream), returns an int status
+ * (JETGPU_OK = 0) and records a message readable through jetgpu_last_error()
+ * on failure. No entry point allocates device memory unless its comment says
+ * so; scratch space is caller-owned ("workspace") and sized by the matching
+ * *_workspace_size query. Tensors are row-major complex arrays: complex64 =
+ * interleaved float (re, im), complex128 = interleaved double.
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the reference project root).
+ */
+#ifndef JETGPU_H
+#define JETGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JETGPU_ABI_VERSION 1
+
+/* Status codes. */
+#define JETGPU_OK 0
+#define JETGPU_ERR_INVALID 1     /* bad argument (shape, permutation, size) */
+#define JETGPU_ERR_CUDA 2        /* a CUDA runtime/driver call failed */
+#define JETGPU_ERR_UNSUPPORTED 3 /* valid request this build cannot serve */
+#define JETGPU_ERR_WORKSPACE 4   /* workspace missing or too small */
+#define JETGPU_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+
+/* Element types. */
+#define JETGPU_C64 0  /* std::complex<float>  */
+#define JETGPU_C128 1 /* std::complex<double> */
+
+/* Arithmetic forms of a contraction. */
+#define JETGPU_PREC_FP32 0   /* plain: complex FMA in the element type (FP32 or FP64) */
+#define JETGPU_PREC_TF32X3 1 /* tcgen05 kind::tf32, hi/lo split, 3 products, FP32 accumulate */
+#define JETGPU_PREC_AUTO 2   /* TF32x3 where the shape suits the tensor cores, else plain */
+
+/* Complex product algorithms for the tensor-core form. */
+#define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
+
+/* Message of the last failing call made by this host thread ("" if none). */
+const char *jetgpu_last_error(void);
+
+/* ABI version (JETGPU_ABI_VERSION) of the loaded library. */
+int jetgpu_version(void);
+
+/* Streaming multiprocessor count and compute capability of the current
+ * device. */
+int jetgpu_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/*
+ * Index permutation, out-of-place.
+ *   out[new multi-index] = in[old multi-index], new axis j = old axis perm[j].
+ * shape: `rank` old dimensions (any sizes >= 1); perm: a permutation of
+ * 0..rank-1. Bit-exact (a pure copy). Power-of-two tensors take a tiled
+ * bit-permutation kernel; other shapes a mixed-radix gather kernel.
+ * Replaces Permuter<QFlexPermuter|DefaultPermuter>::Transpose
+ * (include/jet/permute/Permuter.hpp:49-119, QFlex.hpp:158-538,
+ * Default.hpp:20-133) as used by Tensor::Transpose (Tensor.hpp:578-642).
+ * `in` and `out` must not overlap.
+ */
+int jetgpu_permute(const void *in, void *out, int rank, const uint64_t *shape,
+                   const int32_t *perm, int dtype, void *stream);
+
+/*
+ * Same permutation applied to `batch` tensors stored back to back
+ * (in + b * size, out + b * size, size = prod(shape)).
+ */
+int jetgpu_permute_batched(const void *in, void *out, uint64_t batch, int rank,
+                           const uint64_t *shape, const int32_t *perm,
+                           int dtype, void *stream);
+
+/*
+ * Dense product of already-ordered operands, plain arithmetic:
+ *   C[m x n] = A[m x k] * B[k x n], row-major, alpha = 1, beta = 0.
+ * Covers all four cases of TensorHelpers::MultiplyTensorData
+ * (include/jet/TensorHelpers.hpp:128-168: GEMM, GEMV, GEMV^T, DOTU; m or n
+ * equal to 1 selects the vector kernels). Complex64 computes with FP32 FMA,
+ * complex128 with FP64 FMA. k = 0 writes zeros.
+ */
+int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
+                    uint64_t n, uint64_t k, int dtype, void *stream);
+
+/*
+ * Pairwise contraction with both transposes fused in:
+ *   C[left ++ right] = sum_common A * B
+ * a_perm orders A's axes as (left ++ common); b_perm orders B's axes as
+ * (common ++ right); m, n, k are the products of the left, right and common
+ * dimensions. Replaces Tensor::ContractTensors (include/jet/Tensor.hpp:708-752)
+ * after its label algebra; the label algebra stays on the host.
+ *
+ * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3 (complex64 only) or
+ * JETGPU_PREC_AUTO. algo: JETGPU_ALGO_4M.
+ * scale_a, scale_b: power-of-two exponents applied exactly to A and B before
+ * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
+ * workspace: caller-owned device scratch of at least
+ * jetgpu_contract_workspace_size(...) bytes (may be NULL when that is 0).
+ */
+size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
+                                      const int32_t *a_perm, int b_rank,
+                                      const uint64_t *b_shape,
+                                      const int32_t *b_perm, uint64_t m,
+                                      uint64_t n, uint64_t k, int dtype,
+                                      int precision);
+
+int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
+                    const int32_t *a_perm, const void *B, int b_rank,
+                    const uint64_t *b_shape, const int32_t *b_perm, void *C,
+                    uint64_t m, uint64_t n, uint64_t k, int dtype,
+                    int precision, int algo, int scale_a, int scale_b,
+                    void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * The two stages of the TF32x3 form of jetgpu_contract, for callers that
+ * schedule them separately (batched executors, profilers).
+ *
+ * jetgpu_split_tf32: permutes a complex64 tensor (as jetgpu_permute) and
+ * writes it, multiplied by 2^scale_exp, as four fp32 planes holding TF32
+ * values: plane p at planes + p * plane_stride floats, p = 0 re_hi,
+ * 1 re_lo, 2 im_hi, 3 im_lo (x = hi + lo + O(2^-22 |x|)); the permuted
+ * tensor is viewed as a rows x cols row-major matrix stored with a row pitch
+ * of `pitch` floats (pitch >= cols, pitch % 4 == 0).
+ *
+ * jetgpu_gemm_tf32x3: C[m x n] (complex64, row-major) = A * B^T from the
+ * planes of A (m x k) and B (n x k, i.e. B in (right ++ common) order), with
+ * row pitch kpitch; tcgen05 kind::tf32 tensor cores, three products per real
+ * product, FP32 accumulation, output multiplied by `out_scale`.
+ * Replaces the cblas_cgemm call of TensorHelpers.hpp:47-61.
+ */
+int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape,
+                      const int32_t *perm, uint64_t rows, uint64_t cols,
+                      uint64_t pitch, uint64_t plane_stride, int scale_exp,
+                      float *planes, void *stream);
+
+int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
+                       uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
+                       float out_scale, void *stream);
+
+/*
+ * Element-wise sum C = A + B of equal-size tensors whose data are already in
+ * the same index order (the transpose of B into A's order is a separate
+ * jetgpu_permute). Replaces the data loop of Tensor::AddTensors
+ * (include/jet/Tensor.hpp:446-451).
+ */
+int jetgpu_add(const void *A, const void *B, void *C, uint64_t size, int dtype,
+               void *stream);
+
+/* Element-wise complex conjugate (Tensor::Conj, Tensor.hpp:668-675). */
+int jetgpu_conj(const void *in, void *out, uint64_t size, int dtype,
+                void *stream);
+
+/*
+ * Cross-slice reduction in FP64: out[i] = sum_s results[s * size + i] for
+ * s = 0..n_slices-1, summed in a fixed order in double precision; `out` is
+ * complex128. Replaces the result reduction of
+ * TaskBasedContractor::AddReductionTask (TaskBasedContractor.hpp:258-280),
+ * which adds slice results with Tensor::AddTensors.
+ * accumulate != 0 adds into the existing contents of `out`.
+ */
+int jetgpu_slice_sum_f64(const void *results, uint64_t n_slices, uint64_t size,
+                         int dtype, void *out, int accumulate, void *stream);
+
+/*
+ * Device Tensor::SliceIndex for a run of slice values
+ * (include/jet/Tensor.hpp:493-526 as driven by TensorNetwork::SliceIndices,
+ * TensorNetwork.hpp:210-284). For s < n_values, with v = first_value + s,
+ * axis axes[j] is fixed to (v / value_strides[j]) % shape[axes[j]] -- the
+ * row-major unravel of the network-wide slice value v that SliceIndices
+ * performs (Utilities.hpp:463-475) -- and out + s * out_size receives the
+ * sub-tensor over the remaining axes in their original order
+ * (out_size = product of the remaining dimensions).
+ */
+int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
+                        int n_axes, const int32_t *axes,
+                        const uint64_t *value_strides, uint64_t first_value,
+                        uint64_t n_values, void *out, int dtype, void *stream);
+
+/*
+ * Reads and clears the device status word that bounded waits inside the
+ * tensor-core kernels set on timeout (JETGPU_ERR_TIMEOUT), so that a hung
+ * pipeline surfaces as an error on the host instead of a hang. Synchronous.
+ */
+int jetgpu_take_device_status(int *status);
+
+/*
+ * Largest binary exponent e with 2^e <= max |x_i| over the real and imaginary
+ * parts of `size` complex elements, written to the device int *exp_dev
+ * (stream-ordered, no host synchronisation). -1000 when every element is
+ * zero. Used to choose the power-of-two scales of jetgpu_contract.
+ */
+int jetgpu_max_exponent(const void *x, uint64_t size, int dtype, int *exp_dev,
+                        void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JETGPU_H */

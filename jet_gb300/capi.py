@@ -1,0 +1,259 @@
+"""ctypes binding of the C-ABI library libjetgpu.so (include/jetgpu.h).
+
+This is the Python-side FFI a maintainer of the reference would add next to
+its pybind bindings: plain pointers, sizes and a stream, int status codes.
+Device memory and streams come from PyTorch (torch.cuda tensors); PyTorch is
+plumbing here, every computation runs in libjetgpu.so.
+
+Importing this module fails loudly (ImportError) when the library has not
+been built; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libjetgpu.so")
+HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "jetgpu.h")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        "libjetgpu.so is not built; run `python -c \"import __graft_entry__ as g; g.build()\"` "
+        "or `python -m jet_gb300.build`")
+
+lib = ctypes.CDLL(LIB_PATH)
+
+OK = 0
+ERR_INVALID = 1
+ERR_CUDA = 2
+ERR_UNSUPPORTED = 3
+ERR_WORKSPACE = 4
+ERR_TIMEOUT = 5
+
+C64 = 0
+C128 = 1
+
+PREC_FP32 = 0
+PREC_TF32X3 = 1
+PREC_AUTO = 2
+
+ALGO_4M = 0
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+lib.jetgpu_last_error.restype = ctypes.c_char_p
+lib.jetgpu_contract_workspace_size.restype = ctypes.c_size_t
+lib.jetgpu_contract_workspace_size.argtypes = [ctypes.c_int, _u64p, _i32p, ctypes.c_int, _u64p,
+                                               _i32p, ctypes.c_uint64, ctypes.c_uint64,
+                                               ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+lib.jetgpu_permute.argtypes = [_vp, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp]
+lib.jetgpu_permute_batched.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _u64p, _i32p,
+                                       ctypes.c_int, _vp]
+lib.jetgpu_multiply.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
+                                ctypes.c_uint64, ctypes.c_int, _vp]
+lib.jetgpu_contract.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, _vp, ctypes.c_int, _u64p, _i32p,
+                                _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, _vp, ctypes.c_size_t, _vp]
+lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                  _vp, _vp]
+lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
+lib.jetgpu_add.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
+lib.jetgpu_conj.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
+lib.jetgpu_slice_sum_f64.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _vp,
+                                     ctypes.c_int, _vp]
+lib.jetgpu_slice_gather.argtypes = [_vp, ctypes.c_int, _u64p, ctypes.c_int, _i32p, _u64p,
+                                    ctypes.c_uint64, ctypes.c_uint64, _vp, ctypes.c_int, _vp]
+lib.jetgpu_max_exponent.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, _vp]
+lib.jetgpu_take_device_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
+lib.jetgpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+
+
+class JetGpuError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"jetgpu error {code}: {msg}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise JetGpuError(rc, lib.jetgpu_last_error().decode())
+
+
+def declared_symbols() -> List[str]:
+    """Entry points declared in include/jetgpu.h."""
+    text = open(HEADER_PATH).read()
+    return sorted(set(re.findall(r"\b(jetgpu_\w+)\s*\(", text)))
+
+
+def u64(vals: Sequence[int]):
+    return (ctypes.c_uint64 * max(1, len(vals)))(*[int(v) for v in vals])
+
+
+def i32(vals: Sequence[int]):
+    return (ctypes.c_int32 * max(1, len(vals)))(*[int(v) for v in vals])
+
+
+def dtype_code(dtype) -> int:
+    import torch
+
+    if dtype in (torch.complex64, np.complex64) or str(dtype) in ("complex64", "torch.complex64"):
+        return C64
+    if dtype in (torch.complex128, np.complex128) or str(dtype) in ("complex128", "torch.complex128"):
+        return C128
+    raise TypeError(f"unsupported dtype {dtype}")
+
+
+def _stream(stream) -> Optional[int]:
+    import torch
+
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _ptr(t) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def permute(x, shape: Sequence[int], perm: Sequence[int], out=None, batch: int = 1, stream=None):
+    """out[new] = x[old], new axis j = old axis perm[j] (batch tensors back to back)."""
+    import torch
+
+    if out is None:
+        out = torch.empty_like(x)
+    if batch == 1:
+        rc = lib.jetgpu_permute(_ptr(x), _ptr(out), len(shape), u64(shape), i32(perm),
+                                dtype_code(x.dtype), _stream(stream))
+    else:
+        rc = lib.jetgpu_permute_batched(_ptr(x), _ptr(out), batch, len(shape), u64(shape),
+                                        i32(perm), dtype_code(x.dtype), _stream(stream))
+    check(rc)
+    return out
+
+
+def multiply(a, b, m: int, n: int, k: int, out=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty(m * n, dtype=a.dtype, device=a.device)
+    check(lib.jetgpu_multiply(_ptr(a), _ptr(b), _ptr(out), m, n, k, dtype_code(a.dtype),
+                              _stream(stream)))
+    return out
+
+
+def contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dtype_c, precision) -> int:
+    return int(lib.jetgpu_contract_workspace_size(len(a_shape), u64(a_shape), i32(a_perm),
+                                                  len(b_shape), u64(b_shape), i32(b_perm),
+                                                  m, n, k, dtype_c, precision))
+
+
+def contract(a, a_shape, a_perm, b, b_shape, b_perm, m, n, k, precision=PREC_FP32,
+             out=None, workspace=None, scale_a=0, scale_b=0, stream=None):
+    """C[m x n] = permute(A)[m x k] permute(B)[k x n] through jetgpu_contract."""
+    import torch
+
+    dc = dtype_code(a.dtype)
+    if out is None:
+        out = torch.empty(max(m * n, 1), dtype=a.dtype, device=a.device)
+    need = contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dc, precision)
+    if workspace is None and need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=a.device)
+    ws_bytes = 0 if workspace is None else workspace.numel() * workspace.element_size()
+    check(lib.jetgpu_contract(_ptr(a), len(a_shape), u64(a_shape), i32(a_perm), _ptr(b),
+                              len(b_shape), u64(b_shape), i32(b_perm), _ptr(out), m, n, k, dc,
+                              precision, ALGO_4M, scale_a, scale_b, _ptr(workspace), ws_bytes,
+                              _stream(stream)))
+    return out
+
+
+def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, stream=None):
+    """Permute + TF32 hi/lo split into 4 planes of rows x pitch floats."""
+    check(lib.jetgpu_split_tf32(_ptr(x), len(shape), u64(shape), i32(perm), rows, cols, pitch,
+                                rows * pitch, scale_exp, _ptr(planes), _stream(stream)))
+    return planes
+
+
+def gemm_tf32x3(a_planes, b_planes, m, n, k, kpitch, out, out_scale=1.0, stream=None):
+    check(lib.jetgpu_gemm_tf32x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
+                                 out_scale, _stream(stream)))
+    return out
+
+
+def add(a, b, out=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty_like(a)
+    check(lib.jetgpu_add(_ptr(a), _ptr(b), _ptr(out), a.numel(), dtype_code(a.dtype),
+                         _stream(stream)))
+    return out
+
+
+def conj(a, out=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty_like(a)
+    check(lib.jetgpu_conj(_ptr(a), _ptr(out), a.numel(), dtype_code(a.dtype), _stream(stream)))
+    return out
+
+
+def slice_sum_f64(results, n_slices: int, size: int, out=None, accumulate=False, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.zeros(size, dtype=torch.complex128, device=results.device)
+    check(lib.jetgpu_slice_sum_f64(_ptr(results), n_slices, size, dtype_code(results.dtype),
+                                   _ptr(out), int(bool(accumulate)), _stream(stream)))
+    return out
+
+
+def slice_gather(x, shape, axes, value_strides, first_value, n_values, out=None, stream=None):
+    import torch
+
+    fixed = set(axes)
+    out_size = 1
+    for i, d in enumerate(shape):
+        if i not in fixed:
+            out_size *= int(d)
+    if out is None:
+        out = torch.empty(max(out_size * n_values, 1), dtype=x.dtype, device=x.device)
+    check(lib.jetgpu_slice_gather(_ptr(x), len(shape), u64(shape), len(axes), i32(axes),
+                                  u64(value_strides), first_value, n_values, _ptr(out),
+                                  dtype_code(x.dtype), _stream(stream)))
+    return out
+
+
+def max_exponent(x, stream=None) -> int:
+    import torch
+
+    e = torch.empty(1, dtype=torch.int32, device=x.device)
+    check(lib.jetgpu_max_exponent(_ptr(x), x.numel(), dtype_code(x.dtype), _ptr(e),
+                                  _stream(stream)))
+    return int(e.item())
+
+
+def take_device_status() -> int:
+    v = ctypes.c_int(0)
+    check(lib.jetgpu_take_device_status(ctypes.byref(v)))
+    return v.value
+
+
+def device_info():
+    sm, ma, mi = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    check(lib.jetgpu_device_info(ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)))
+    return sm.value, ma.value, mi.value

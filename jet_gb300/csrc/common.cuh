@@ -1,0 +1,93 @@
+// Shared helpers of the jetgpu C-ABI library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/jetgpu.h"
+
+namespace jetgpu {
+
+// Records `msg` as this thread's last error and returns `code`.
+int SetError(int code, const std::string &msg);
+// Clears this thread's last error.
+void ClearError();
+
+inline cudaStream_t AsStream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Checks the launch that was just enqueued.
+int CheckLaunch(const char *what);
+
+#define JETGPU_CUDA_TRY(expr)                                                  \
+    do {                                                                       \
+        cudaError_t err__ = (expr);                                            \
+        if (err__ != cudaSuccess)                                              \
+            return ::jetgpu::SetError(JETGPU_ERR_CUDA,                         \
+                                      std::string(#expr) + ": " +              \
+                                          cudaGetErrorString(err__));          \
+    } while (0)
+
+#define JETGPU_REQUIRE(cond, msg)                                              \
+    do {                                                                       \
+        if (!(cond))                                                           \
+            return ::jetgpu::SetError(JETGPU_ERR_INVALID, (msg));              \
+    } while (0)
+
+inline size_t ElemBytes(int dtype) { return dtype == JETGPU_C128 ? 16 : 8; }
+
+inline bool IsPow2(uint64_t v) { return v && !(v & (v - 1)); }
+
+inline int Log2(uint64_t v)
+{
+    int r = 0;
+    while (v > 1) {
+        v >>= 1;
+        ++r;
+    }
+    return r;
+}
+
+// Number of SMs of the current device (cached per device).
+int SmCount();
+
+// Grid size for a persistent / grid-stride kernel: `per_sm` CTAs per SM,
+// never more than `work_items`.
+inline unsigned GridFor(uint64_t work_items, int per_sm)
+{
+    uint64_t g = (uint64_t)SmCount() * (uint64_t)per_sm;
+    if (work_items < g)
+        g = work_items;
+    return (unsigned)(g ? g : 1);
+}
+
+// Internal entry points shared between translation units.
+int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
+                const uint64_t *shape, const int32_t *perm, int dtype,
+                cudaStream_t stream);
+
+// Permutes a complex64 tensor and writes it as TF32 hi/lo planes for the
+// tensor-core product: plane p (0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo) holds a
+// rows x cols fp32 matrix with row pitch `pitch` floats, where the permuted
+// tensor is viewed as rows x cols (row-major). Values are multiplied by
+// 2^scale_exp first.
+int PermuteSplitTf32(const void *in, float *planes, int rank,
+                     const uint64_t *shape, const int32_t *perm, uint64_t rows,
+                     uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                     int scale_exp, cudaStream_t stream);
+
+int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
+                  uint64_t n, uint64_t k, int dtype, int scale_exp,
+                  void *workspace, size_t ws_bytes, cudaStream_t stream);
+
+size_t MultiplyPlainWorkspace(uint64_t m, uint64_t n, uint64_t k, int dtype);
+
+// Tensor-core 3xTF32 complex product of planar operands (see gemm_tc.cu).
+int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
+                     uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
+                     float out_scale, cudaStream_t stream);
+
+bool TcAvailable();
+
+} // namespace jetgpu

@@ -1,0 +1,206 @@
+// Pairwise contraction orchestration (Tensor::ContractTensors, device side).
+//
+// Reference: include/jet/Tensor.hpp:708-752 transposes A to (left ++ common)
+// and B to (common ++ right) with the Permuter backends, then calls
+// TensorHelpers::MultiplyTensorData. The label algebra stays on the host;
+// this file receives the two orderings as axis permutations.
+//
+// Plain form:  At = permute(A), Bt = permute(B) into the workspace (skipped
+//              when already ordered), then the SIMT complex product.
+// TF32x3 form: A is permuted straight into TF32 hi/lo planes (M x K), B into
+//              planes of its (right ++ common) order (N x K, K-major), then the
+//              tcgen05 product writes C.
+#include <vector>
+
+#include "common.cuh"
+
+namespace jetgpu {
+namespace {
+
+constexpr size_t kAlign = 256;
+
+inline size_t AlignUp(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+bool IsIdentity(int rank, const int32_t *perm)
+{
+    for (int i = 0; i < rank; ++i)
+        if (perm[i] != i)
+            return false;
+    return true;
+}
+
+// Number of leading axes of `perm` whose dimensions multiply to `lead`
+// (-1 if no prefix does).
+int SplitPoint(int rank, const uint64_t *shape, const int32_t *perm, uint64_t lead)
+{
+    uint64_t p = 1;
+    if (lead == 1)
+        return 0;
+    for (int j = 0; j < rank; ++j) {
+        p *= shape[perm[j]];
+        if (p == lead)
+            return j + 1;
+        if (p > lead)
+            return -1;
+    }
+    return -1;
+}
+
+bool UseTensorCores(uint64_t m, uint64_t n, uint64_t k, int dtype, int precision)
+{
+    if (dtype != JETGPU_C64 || precision == JETGPU_PREC_FP32)
+        return false;
+    if (m < 2 || n < 2)
+        return false; // vector-shaped steps are bandwidth bound
+    if (precision == JETGPU_PREC_AUTO && (m < 128 || n < 64 || k < 32))
+        return false;
+    return TcAvailable();
+}
+
+int Validate(int rank, const uint64_t *shape, const int32_t *perm, uint64_t lead,
+             uint64_t tail, const char *which)
+{
+    JETGPU_REQUIRE(rank >= 0 && rank <= 64, std::string(which) + ": rank out of range");
+    uint64_t size = 1;
+    for (int i = 0; i < rank; ++i)
+        size *= shape[i];
+    JETGPU_REQUIRE(size == lead * tail, std::string(which) + ": size does not match the product dimensions");
+    JETGPU_REQUIRE(SplitPoint(rank, shape, perm, lead) >= 0,
+                   std::string(which) + ": permutation does not split into the product dimensions");
+    return JETGPU_OK;
+}
+
+} // namespace
+} // namespace jetgpu
+
+using namespace jetgpu;
+
+extern "C" {
+
+int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m, uint64_t n,
+                    uint64_t k, int dtype, void *stream)
+{
+    ClearError();
+    return MultiplyPlain(A, B, C, m, n, k, dtype, 0, nullptr, 0, AsStream(stream));
+}
+
+size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
+                                      const int32_t *a_perm, int b_rank,
+                                      const uint64_t *b_shape, const int32_t *b_perm,
+                                      uint64_t m, uint64_t n, uint64_t k, int dtype,
+                                      int precision)
+{
+    if (UseTensorCores(m, n, k, dtype, precision)) {
+        const uint64_t kp = (k + 3) / 4 * 4;
+        return AlignUp(4 * m * kp * sizeof(float)) + AlignUp(4 * n * kp * sizeof(float));
+    }
+    const size_t eb = ElemBytes(dtype);
+    size_t ws = 0;
+    if (!IsIdentity(a_rank, a_perm))
+        ws += AlignUp(m * k * eb);
+    if (!IsIdentity(b_rank, b_perm))
+        ws += AlignUp(k * n * eb);
+    ws += AlignUp(MultiplyPlainWorkspace(m, n, k, dtype));
+    return ws;
+}
+
+int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
+                    const int32_t *a_perm, const void *B, int b_rank,
+                    const uint64_t *b_shape, const int32_t *b_perm, void *C,
+                    uint64_t m, uint64_t n, uint64_t k, int dtype, int precision,
+                    int algo, int scale_a, int scale_b, void *workspace,
+                    size_t workspace_bytes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(precision == JETGPU_PREC_FP32 || precision == JETGPU_PREC_TF32X3 ||
+                       precision == JETGPU_PREC_AUTO,
+                   "bad precision");
+    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
+    if (precision == JETGPU_PREC_TF32X3 && dtype != JETGPU_C64)
+        return SetError(JETGPU_ERR_UNSUPPORTED, "TF32x3 needs complex64 operands");
+    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
+    if (rc)
+        return rc;
+    rc = Validate(b_rank, b_shape, b_perm, k, n, "B");
+    if (rc)
+        return rc;
+    if (m * n == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(C != nullptr, "null output");
+    JETGPU_REQUIRE(k == 0 || (A != nullptr && B != nullptr), "null operand");
+    const size_t need = jetgpu_contract_workspace_size(a_rank, a_shape, a_perm, b_rank,
+                                                       b_shape, b_perm, m, n, k, dtype,
+                                                       precision);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return SetError(JETGPU_ERR_WORKSPACE,
+                        "workspace too small: need " + std::to_string(need) + " bytes");
+    cudaStream_t st = AsStream(stream);
+    uint8_t *ws = static_cast<uint8_t *>(workspace);
+
+    if (k > 0 && UseTensorCores(m, n, k, dtype, precision)) {
+        const uint64_t kp = (k + 3) / 4 * 4;
+        float *pa = reinterpret_cast<float *>(ws);
+        float *pb = reinterpret_cast<float *>(ws + AlignUp(4 * m * kp * sizeof(float)));
+        // B is wanted as (right ++ common): rotate its (common ++ right) order.
+        const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
+        std::vector<int32_t> bt(b_rank);
+        for (int j = 0; j < b_rank; ++j)
+            bt[j] = b_perm[(j + nc) % b_rank];
+        rc = PermuteSplitTf32(A, pa, a_rank, a_shape, a_perm, m, k, kp, m * kp, scale_a, st);
+        if (rc)
+            return rc;
+        rc = PermuteSplitTf32(B, pb, b_rank, b_shape, bt.data(), n, k, kp, n * kp, scale_b, st);
+        if (rc)
+            return rc;
+        return GemmTf32x3Planar(pa, pb, C, m, n, k, kp, 1.0f, st);
+    }
+
+    const size_t eb = ElemBytes(dtype);
+    const void *at = A;
+    const void *btp = B;
+    if (k > 0 && !IsIdentity(a_rank, a_perm)) {
+        rc = PermuteImpl(A, ws, 1, a_rank, a_shape, a_perm, dtype, st);
+        if (rc)
+            return rc;
+        at = ws;
+        ws += AlignUp(m * k * eb);
+    }
+    if (k > 0 && !IsIdentity(b_rank, b_perm)) {
+        rc = PermuteImpl(B, ws, 1, b_rank, b_shape, b_perm, dtype, st);
+        if (rc)
+            return rc;
+        btp = ws;
+        ws += AlignUp(k * n * eb);
+    }
+    const size_t vec_ws = MultiplyPlainWorkspace(m, n, k, dtype);
+    return MultiplyPlain(at, btp, C, m, n, k, dtype, scale_a + scale_b, ws, vec_ws, st);
+}
+
+} // extern "C"
+
+extern "C" {
+
+int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
+                      uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                      int scale_exp, float *planes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(pitch >= cols && pitch % 4 == 0, "pitch must be >= cols and a multiple of 4");
+    JETGPU_REQUIRE(plane_stride >= rows * pitch, "plane stride too small");
+    if (rows * cols == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
+    return PermuteSplitTf32(in, planes, rank, shape, perm, rows, cols, pitch, plane_stride,
+                            scale_exp, AsStream(stream));
+}
+
+int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C, uint64_t m,
+                       uint64_t n, uint64_t k, uint64_t kpitch, float out_scale, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
+    return GemmTf32x3Planar(a_planes, b_planes, C, m, n, k, kpitch, out_scale, AsStream(stream));
+}
+
+} // extern "C"

@@ -1,0 +1,421 @@
+// Tensor-core complex product in split precision (3xTF32), sm_103a.
+//
+// Replaces the cgemm of TensorHelpers::MultiplyTensorData
+// (include/jet/TensorHelpers.hpp:47-61, 147-152) for large steps.
+//
+// Operands arrive as planar TF32 splits written by PermuteSplitTf32:
+//   A: planes {Ar_hi, Ar_lo, Ai_hi, Ai_lo}, each M x K (K contiguous)
+//   B: planes {Br_hi, Br_lo, Bi_hi, Bi_lo}, each N x K (K contiguous)
+// and the complex product uses four real products ("4M"), each as three
+// TF32 products (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM:
+//   Cr += Ar Br - Ai Bi,   Ci += Ar Bi + Ai Br.
+//
+// One CTA computes a 128 x 128 complex tile: Cr in TMEM columns [0,128),
+// Ci in [128,256). Warp 0 lane 0 feeds a 3-stage ring of shared-memory
+// stages with TMA (8 boxes of 128 rows x 16 floats, 64-byte swizzle); warp 1
+// lane 0 issues tcgen05.mma (M=128, N=128, K=8) and releases stages with
+// tcgen05.commit; all four warps drain TMEM with tcgen05.ld in the epilogue.
+// Every mbarrier wait is bounded: on timeout the kernel records
+// JETGPU_ERR_TIMEOUT in a device status word, skips the remaining work,
+// frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+
+namespace jetgpu {
+
+__device__ int g_tc_status = 0;
+
+namespace {
+
+constexpr int kBM = 128;
+constexpr int kBN = 128;
+constexpr int kBK = 16;                    // complex k per stage (64 bytes of fp32)
+constexpr int kStages = 3;
+constexpr int kTileBytes = kBM * kBK * 4;  // one plane box: 8 KB
+constexpr int kStageBytes = 8 * kTileBytes; // 4 A planes + 4 B planes: 64 KB
+constexpr int kTmemCols = 256;
+constexpr int kThreads = 128;
+constexpr unsigned long long kWaitNs = 4000000000ull; // 4 s bound per wait
+
+__device__ __forceinline__ uint32_t SmemAddr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t GlobalTimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void MbarInit(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void MbarArriveExpectTx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool MbarTryWait(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
+// Bounded wait for the phase of parity `parity`; false on timeout.
+__device__ __forceinline__ bool MbarWait(uint32_t bar, uint32_t parity)
+{
+    if (MbarTryWait(bar, parity))
+        return true;
+    const uint64_t t0 = GlobalTimer();
+    for (uint32_t i = 1;; ++i) {
+        if (MbarTryWait(bar, parity))
+            return true;
+        if ((i & 255u) == 0 && GlobalTimer() - t0 > kWaitNs) {
+            atomicExch(&g_tc_status, JETGPU_ERR_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void TmaLoad3d(uint32_t dst, const CUtensorMap *map,
+                                          int c0, int c1, int c2, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::"
+                 "complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2),
+                 "r"(bar)
+                 : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 64-byte swizzle, 8-row
+// groups 512 bytes apart.
+__device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                   // leading byte offset (unused)
+    d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)4 << 61;                   // 64-byte swizzle
+    return d;
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t InstrDesc(int m, int n, bool neg_a)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((neg_a ? 1u : 0u) << 13) |
+           ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void MmaTf32(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                        uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void MmaCommit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void FenceBeforeSync()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void FenceAfterSync()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void TmemLoad16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+                   "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+                   "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void TmemWaitLoad()
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
+                          const __grid_constant__ CUtensorMap tmB,
+                          float2 *__restrict__ C, int M, int N, int ktiles,
+                          float scale)
+{
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[kStages];
+    __shared__ __align__(8) uint64_t empty_bar[kStages];
+    __shared__ __align__(8) uint64_t acc_bar;
+    __shared__ uint32_t tmem_slot;
+
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kBM;
+    const int n0 = blockIdx.x * kBN;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            MbarInit(SmemAddr(&full_bar[s]), 1);
+            MbarInit(SmemAddr(&empty_bar[s]), 1);
+        }
+        MbarInit(SmemAddr(&acc_bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         SmemAddr(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    FenceBeforeSync();
+    __syncthreads();
+    FenceAfterSync();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // TMA producer.
+            for (int kt = 0; kt < ktiles; ++kt) {
+                const int s = kt % kStages;
+                const uint32_t phase = (uint32_t)(kt / kStages) & 1u;
+                if (!MbarWait(SmemAddr(&empty_bar[s]), phase ^ 1u))
+                    break;
+                const uint32_t fb = SmemAddr(&full_bar[s]);
+                MbarArriveExpectTx(fb, kStageBytes);
+                const uint32_t base = SmemAddr(smem + s * kStageBytes);
+                const int k0 = kt * kBK;
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    TmaLoad3d(base + p * kTileBytes, &tmA, k0, m0, p, fb);
+                    TmaLoad3d(base + (4 + p) * kTileBytes, &tmB, k0, n0, p, fb);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer.
+            constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false);
+            constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true);
+            const uint32_t d_re = tmem;
+            const uint32_t d_im = tmem + kBN;
+            bool ok = true;
+            for (int kt = 0; kt < ktiles && ok; ++kt) {
+                const int s = kt % kStages;
+                const uint32_t phase = (uint32_t)(kt / kStages) & 1u;
+                if (!MbarWait(SmemAddr(&full_bar[s]), phase)) {
+                    ok = false;
+                    break;
+                }
+                FenceAfterSync();
+                const uint32_t base = SmemAddr(smem + s * kStageBytes);
+#pragma unroll
+                for (int kk = 0; kk < kBK / 8; ++kk) {
+                    const uint32_t koff = kk * 32; // 8 fp32 per MMA step
+                    const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
+                    const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
+                    const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
+                    const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
+                    const uint64_t brh = SmemDesc(base + 4 * kTileBytes + koff);
+                    const uint64_t brl = SmemDesc(base + 5 * kTileBytes + koff);
+                    const uint64_t bih = SmemDesc(base + 6 * kTileBytes + koff);
+                    const uint64_t bil = SmemDesc(base + 7 * kTileBytes + koff);
+                    const uint32_t first = (kt == 0 && kk == 0) ? 0u : 1u;
+                    // Cr += Ar Br
+                    MmaTf32(d_re, arh, brh, kIdesc, first);
+                    MmaTf32(d_re, arh, brl, kIdesc, 1u);
+                    MmaTf32(d_re, arl, brh, kIdesc, 1u);
+                    // Cr -= Ai Bi
+                    MmaTf32(d_re, aih, bih, kIdescNeg, 1u);
+                    MmaTf32(d_re, aih, bil, kIdescNeg, 1u);
+                    MmaTf32(d_re, ail, bih, kIdescNeg, 1u);
+                    // Ci += Ar Bi
+                    MmaTf32(d_im, arh, bih, kIdesc, first);
+                    MmaTf32(d_im, arh, bil, kIdesc, 1u);
+                    MmaTf32(d_im, arl, bih, kIdesc, 1u);
+                    // Ci += Ai Br
+                    MmaTf32(d_im, aih, brh, kIdesc, 1u);
+                    MmaTf32(d_im, aih, brl, kIdesc, 1u);
+                    MmaTf32(d_im, ail, brh, kIdesc, 1u);
+                }
+                MmaCommit(SmemAddr(&empty_bar[s]));
+            }
+            // Signals the epilogue once every issued MMA has completed.
+            MmaCommit(SmemAddr(&acc_bar));
+        }
+        __syncwarp();
+    }
+
+    // Epilogue: warp w owns TMEM lanes / tile rows [32w, 32w + 32).
+    const bool ready = MbarWait(SmemAddr(&acc_bar), 0);
+    __syncwarp();
+    FenceAfterSync();
+    const int row = m0 + warp * 32 + lane;
+    if (ready && ktiles > 0) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll 1
+        for (int c = 0; c < kBN; c += 16) {
+            float re[16], im[16];
+            TmemLoad16(tmem + lane_base + c, re);
+            TmemLoad16(tmem + lane_base + kBN + c, im);
+            TmemWaitLoad();
+            if (row < M) {
+                float2 *dst = C + (size_t)row * N + n0 + c;
+                if (n0 + c + 16 <= N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) {
+                        float4 v = make_float4(re[j] * scale, im[j] * scale,
+                                               re[j + 1] * scale, im[j + 1] * scale);
+                        *reinterpret_cast<float4 *>(dst + j) = v;
+                    }
+                }
+                else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (n0 + c + j < N)
+                            dst[j] = make_float2(re[j] * scale, im[j] * scale);
+                }
+            }
+        }
+    }
+    FenceBeforeSync();
+    __syncthreads();
+    if (warp == 1) {
+        FenceAfterSync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+int GetEncoder()
+{
+    std::call_once(g_encode_once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    if (!g_encode)
+        return SetError(JETGPU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    return JETGPU_OK;
+}
+
+// 3-D map over planes: (k, row, plane), box 16 x 128 x 1, 64-byte swizzle.
+int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
+                 uint64_t kpitch)
+{
+    cuuint64_t dims[3] = {k, rows, 4};
+    cuuint64_t strides[2] = {kpitch * 4, rows * kpitch * 4};
+    cuuint32_t box[3] = {kBK, kBM, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                          const_cast<float *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return SetError(JETGPU_ERR_CUDA,
+                        "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return JETGPU_OK;
+}
+
+} // namespace
+
+int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
+                     uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
+                     float out_scale, cudaStream_t stream)
+{
+    JETGPU_REQUIRE(m > 0 && n > 0 && k > 0, "empty product");
+    JETGPU_REQUIRE(m < (1ull << 31) && n < (1ull << 31) && k < (1ull << 31),
+                   "dimension too large");
+    JETGPU_REQUIRE(kpitch >= k && kpitch % 4 == 0, "bad k pitch");
+    JETGPU_REQUIRE(((uintptr_t)a_planes % 16) == 0 && ((uintptr_t)b_planes % 16) == 0,
+                   "planes must be 16-byte aligned");
+    JETGPU_REQUIRE((n + kBN - 1) / kBN <= 0x7fffffffull && (m + kBM - 1) / kBM <= 65535ull,
+                   "grid too large");
+    if (!TcAvailable())
+        return SetError(JETGPU_ERR_UNSUPPORTED, "tensor-core path needs an sm_103 device");
+    int rc = GetEncoder();
+    if (rc)
+        return rc;
+    CUtensorMap ta, tb;
+    if ((rc = EncodePlanes(&ta, a_planes, m, k, kpitch)))
+        return rc;
+    if ((rc = EncodePlanes(&tb, b_planes, n, k, kpitch)))
+        return rc;
+    const size_t smem = (size_t)kStages * kStageBytes + 1024;
+    static thread_local int configured_dev = -1;
+    int dev = 0;
+    JETGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (configured_dev != dev) {
+        JETGPU_CUDA_TRY(cudaFuncSetAttribute(
+            tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured_dev = dev;
+    }
+    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM));
+    const int ktiles = (int)((k + kBK - 1) / kBK);
+    tc_gemm_tf32x3_kernel<<<grid, kThreads, smem, stream>>>(
+        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale);
+    return CheckLaunch("tc_gemm_tf32x3_kernel");
+}
+
+} // namespace jetgpu
+
+extern "C" int jetgpu_take_device_status(int *status)
+{
+    jetgpu::ClearError();
+    int v = 0;
+    JETGPU_CUDA_TRY(cudaMemcpyFromSymbol(&v, jetgpu::g_tc_status, sizeof(int)));
+    if (v != 0) {
+        int zero = 0;
+        JETGPU_CUDA_TRY(cudaMemcpyToSymbol(jetgpu::g_tc_status, &zero, sizeof(int)));
+    }
+    if (status)
+        *status = v;
+    return JETGPU_OK;
+}

@@ -1,0 +1,560 @@
+// Index permutation kernels (Tensor::Transpose / Permuter backends).
+//
+// Reference algorithm being replaced: QFlexPermuter (permute/QFlex.hpp) splits
+// every power-of-2 dimension into binary sub-indices and runs up to three
+// out-of-place passes over the whole tensor; DefaultPermuter
+// (permute/Default.hpp) walks the old index with an odometer. Both produce
+// out[new multi-index] = in[old multi-index].
+//
+// GB300 design:
+//  * Power-of-2 tensors: the permutation is a permutation of the bits of the
+//    linear index. One pass. Each CTA owns a tile of 2^u elements spanned by
+//    the t lowest input bits, the t lowest output bits and further input bits
+//    up to u; the remaining bits enumerate tiles. Loads read runs of 2^t
+//    consecutive input elements (512 B per warp, 16-byte vectors), stores
+//    write runs of 2^t consecutive output elements; the tile sits in shared
+//    memory with an XOR swizzle. All bit-scatter arithmetic is folded into
+//    small lookup tables built on the host and passed as __grid_constant__
+//    kernel parameters (warp-uniform reads).
+//  * Any other shape: a mixed-radix gather (one thread per output element,
+//    coalesced stores).
+//  * PermuteSplitTf32: the same two kernels with a store stage that writes the
+//    tensor-core operand planes (TF32 hi/lo of re/im) directly.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace jetgpu {
+namespace {
+
+constexpr int kMaxRank = 64;
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Host-side simplification: drop unit axes, merge input axes that stay
+// adjacent and in order in the output.
+// ---------------------------------------------------------------------------
+struct Simplified {
+    std::vector<uint64_t> dims; // input dims (row-major)
+    std::vector<int> perm;      // output axis j = input axis perm[j]
+    uint64_t size = 1;
+};
+
+int Simplify(int rank, const uint64_t *shape, const int32_t *perm,
+             Simplified &s)
+{
+    JETGPU_REQUIRE(rank >= 0 && rank <= kMaxRank, "rank out of range");
+    std::vector<int> seen(rank, 0);
+    for (int j = 0; j < rank; ++j) {
+        JETGPU_REQUIRE(perm[j] >= 0 && perm[j] < rank && !seen[perm[j]],
+                       "perm is not a permutation of 0..rank-1");
+        seen[perm[j]] = 1;
+    }
+    s.size = 1;
+    for (int i = 0; i < rank; ++i) {
+        JETGPU_REQUIRE(shape[i] >= 1, "zero-sized dimension");
+        s.size *= shape[i];
+    }
+    // Keep non-unit axes.
+    std::vector<int> keep_id(rank, -1);
+    std::vector<uint64_t> d;
+    for (int i = 0; i < rank; ++i)
+        if (shape[i] != 1) {
+            keep_id[i] = (int)d.size();
+            d.push_back(shape[i]);
+        }
+    std::vector<int> p;
+    for (int j = 0; j < rank; ++j)
+        if (keep_id[perm[j]] >= 0)
+            p.push_back(keep_id[perm[j]]);
+    // Merge runs: output-consecutive axes p[j], p[j+1] with p[j+1] == p[j]+1.
+    std::vector<int> group_of(d.size(), -1);
+    std::vector<std::vector<int>> groups; // in output order
+    for (size_t j = 0; j < p.size(); ++j) {
+        if (j > 0 && p[j] == p[j - 1] + 1)
+            groups.back().push_back(p[j]);
+        else
+            groups.push_back({p[j]});
+    }
+    // Input order of groups = sort by first input axis.
+    std::vector<int> order(groups.size());
+    for (size_t g = 0; g < groups.size(); ++g)
+        order[g] = (int)g;
+    std::sort(order.begin(), order.end(),
+              [&](int a, int b) { return groups[a][0] < groups[b][0]; });
+    std::vector<int> in_pos(groups.size());
+    s.dims.clear();
+    for (size_t r = 0; r < order.size(); ++r) {
+        in_pos[order[r]] = (int)r;
+        uint64_t m = 1;
+        for (int ax : groups[order[r]])
+            m *= d[ax];
+        s.dims.push_back(m);
+    }
+    s.perm.clear();
+    for (size_t g = 0; g < groups.size(); ++g)
+        s.perm.push_back(in_pos[g]);
+    return JETGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-radix gather kernel.
+// ---------------------------------------------------------------------------
+struct GatherParams {
+    int rank;
+    uint64_t out_dims[kMaxRank];   // output dims, [rank-1] fastest
+    uint64_t in_strides[kMaxRank]; // input element stride of output axis j
+    uint64_t size;                 // elements per tensor
+    uint64_t total;                // batch * size
+};
+
+template <typename E>
+__global__ void __launch_bounds__(kThreads)
+    gather_kernel(const __grid_constant__ GatherParams p,
+                  const E *__restrict__ in, E *__restrict__ out)
+{
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t b = idx / p.size;
+        uint64_t o = idx - b * p.size;
+        uint64_t src = b * p.size;
+        for (int j = p.rank - 1; j >= 0; --j) {
+            uint64_t d = p.out_dims[j];
+            uint64_t q = o / d;
+            src += (o - q * d) * p.in_strides[j];
+            o = q;
+        }
+        out[idx] = in[src];
+    }
+}
+
+// TF32 rounding to nearest (ties away from zero) by adding half a unit in the
+// last TF32 place and truncating the 13 low mantissa bits.
+__device__ __forceinline__ float RoundTf32(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7f800000u) == 0x7f800000u) // inf / nan: keep
+        return x;
+    return __uint_as_float((u + 0x1000u) & 0xffffe000u);
+}
+
+struct SplitOut {
+    float *planes;         // 4 planes
+    uint64_t plane_stride; // floats between planes
+    uint64_t cols;         // logical columns of the permuted view
+    uint64_t pitch;        // floats per row in a plane
+    float scale;           // exact power of two
+};
+
+__device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
+                                           float2 v)
+{
+    uint64_t row = o / so.cols;
+    uint64_t col = o - row * so.cols;
+    uint64_t off = row * so.pitch + col;
+    float re = v.x * so.scale, im = v.y * so.scale;
+    float rh = RoundTf32(re), ih = RoundTf32(im);
+    float rl = RoundTf32(re - rh), il = RoundTf32(im - ih);
+    so.planes[off] = rh;
+    so.planes[off + so.plane_stride] = rl;
+    so.planes[off + 2 * so.plane_stride] = ih;
+    so.planes[off + 3 * so.plane_stride] = il;
+}
+
+__global__ void __launch_bounds__(kThreads)
+    gather_split_kernel(const __grid_constant__ GatherParams p,
+                        const float2 *__restrict__ in, SplitOut so)
+{
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t o = idx;
+        uint64_t src = 0;
+        for (int j = p.rank - 1; j >= 0; --j) {
+            uint64_t d = p.out_dims[j];
+            uint64_t q = o / d;
+            src += (o - q * d) * p.in_strides[j];
+            o = q;
+        }
+        WriteSplit(so, idx, in[src]);
+    }
+}
+
+void BuildGather(const Simplified &s, uint64_t batch, GatherParams &p)
+{
+    int r = (int)s.dims.size();
+    std::vector<uint64_t> in_stride(r, 1);
+    for (int i = r - 2; i >= 0; --i)
+        in_stride[i] = in_stride[i + 1] * s.dims[i + 1];
+    std::memset(&p, 0, sizeof(p));
+    p.rank = r;
+    for (int j = 0; j < r; ++j) {
+        p.out_dims[j] = s.dims[s.perm[j]];
+        p.in_strides[j] = in_stride[s.perm[j]];
+    }
+    p.size = s.size;
+    p.total = s.size * batch;
+}
+
+// ---------------------------------------------------------------------------
+// Bit-permutation tiled kernel (power-of-2 tensors).
+// ---------------------------------------------------------------------------
+constexpr int kTileTables = 3; // 3 x 8 outer bits
+
+struct BitParams {
+    int n;       // bits of the linear index
+    int u;       // tile bits
+    int t;       // run bits (t lowest input / output bits)
+    int n_outer; // n - u
+    uint64_t total_tiles;
+    uint64_t in_hi[64];  // input offset of run h (h = L >> t)
+    uint64_t out_hi[64]; // output offset of run h (h = M >> t)
+    uint32_t l_lo[64];   // tile-local input index of M & (2^t - 1)
+    uint32_t l_hi[64];   // tile-local input index of (M >> t) << t
+    uint64_t tile_in[kTileTables][256];
+    uint64_t tile_out[kTileTables][256];
+};
+
+__device__ __forceinline__ uint32_t Swz(uint32_t h, int log_ve)
+{
+    return ((h ^ (h >> 5)) & 31u) << log_ve;
+}
+
+__device__ __forceinline__ uint64_t TileBase(const uint64_t (*tbl)[256],
+                                             uint64_t tt)
+{
+    return tbl[0][tt & 255] + tbl[1][(tt >> 8) & 255] +
+           tbl[2][(tt >> 16) & 255];
+}
+
+// Store stage functor: plain element copy.
+template <typename E> struct PlainStore {
+    E *out;
+    __device__ __forceinline__ void operator()(uint64_t off, const E *v,
+                                               int ve) const
+    {
+        if (sizeof(E) == 8) {
+            uint4 w;
+            const uint2 *a = reinterpret_cast<const uint2 *>(v);
+            w.x = a[0].x;
+            w.y = a[0].y;
+            w.z = a[1].x;
+            w.w = a[1].y;
+            *reinterpret_cast<uint4 *>(out + off) = w;
+        }
+        else {
+            *reinterpret_cast<uint4 *>(out + off) =
+                *reinterpret_cast<const uint4 *>(v);
+        }
+    }
+};
+
+// Store stage functor: TF32 hi/lo planes (complex64 only, 2 elements).
+struct SplitStore {
+    SplitOut so;
+    __device__ __forceinline__ void operator()(uint64_t off, const uint2 *v,
+                                               int) const
+    {
+        // off is even and cols >= 2 is a power of 2: both elements share a row.
+        uint64_t row = off / so.cols;
+        uint64_t col = off - row * so.cols;
+        uint64_t base = row * so.pitch + col;
+        float2 a = make_float2(__uint_as_float(v[0].x), __uint_as_float(v[0].y));
+        float2 b = make_float2(__uint_as_float(v[1].x), __uint_as_float(v[1].y));
+        float ar = a.x * so.scale, ai = a.y * so.scale;
+        float br = b.x * so.scale, bi = b.y * so.scale;
+        float arh = RoundTf32(ar), aih = RoundTf32(ai);
+        float brh = RoundTf32(br), bih = RoundTf32(bi);
+        float2 rh = make_float2(arh, brh);
+        float2 rl = make_float2(RoundTf32(ar - arh), RoundTf32(br - brh));
+        float2 ih = make_float2(aih, bih);
+        float2 il = make_float2(RoundTf32(ai - aih), RoundTf32(bi - bih));
+        *reinterpret_cast<float2 *>(so.planes + base) = rh;
+        *reinterpret_cast<float2 *>(so.planes + base + so.plane_stride) = rl;
+        *reinterpret_cast<float2 *>(so.planes + base + 2 * so.plane_stride) = ih;
+        *reinterpret_cast<float2 *>(so.planes + base + 3 * so.plane_stride) = il;
+    }
+};
+
+// E: element (uint2 = complex64, uint4 = complex128); LOG_VE: log2 of
+// elements per 16-byte vector.
+template <typename E, int LOG_VE, typename Store>
+__global__ void __launch_bounds__(kThreads)
+    bitperm_kernel(const __grid_constant__ BitParams p,
+                   const E *__restrict__ in, Store store)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    E *tile = reinterpret_cast<E *>(smem_raw);
+    constexpr int VE = 1 << LOG_VE;
+    const int t = p.t;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int runs = 1 << (p.u - t);
+    const uint64_t outer_mask = (1ull << p.n_outer) - 1;
+
+    uint32_t llo[VE];
+#pragma unroll
+    for (int e = 0; e < VE; ++e)
+        llo[e] = p.l_lo[lane * VE + e];
+
+    for (uint64_t g = blockIdx.x; g < p.total_tiles; g += gridDim.x) {
+        const uint64_t b = g >> p.n_outer;
+        const uint64_t tt = g & outer_mask;
+        const uint64_t in_base = (b << p.n) + TileBase(p.tile_in, tt);
+        const uint64_t out_base = (b << p.n) + TileBase(p.tile_out, tt);
+
+        // Load: run h covers tile-local input indices [h << t, (h+1) << t).
+        for (int h = warp; h < runs; h += nwarps) {
+            const uint64_t off = in_base + p.in_hi[h] + (uint64_t)(lane * VE);
+            uint4 v = __ldg(reinterpret_cast<const uint4 *>(in + off));
+            const uint32_t L = ((uint32_t)h << t) | (uint32_t)(lane * VE);
+            const uint32_t phys = L ^ Swz((uint32_t)h, LOG_VE);
+            *reinterpret_cast<uint4 *>(tile + phys) = v;
+        }
+        __syncthreads();
+        // Store: run h covers tile-local output indices [h << t, (h+1) << t).
+        for (int h = warp; h < runs; h += nwarps) {
+            const uint32_t lhi = p.l_hi[h];
+            E vals[VE];
+#pragma unroll
+            for (int e = 0; e < VE; ++e) {
+                const uint32_t L = llo[e] | lhi;
+                vals[e] = tile[L ^ Swz(L >> t, LOG_VE)];
+            }
+            store(out_base + p.out_hi[h] + (uint64_t)(lane * VE), vals, VE);
+        }
+        __syncthreads();
+    }
+}
+
+// Builds the bit-permutation tables. Returns false when the tensor does not
+// suit the tiled kernel (too small, or too many outer bits).
+bool BuildBitParams(const Simplified &s, uint64_t batch, int log_ve,
+                    BitParams &p)
+{
+    const int r = (int)s.dims.size();
+    int n = 0;
+    std::vector<int> logd(r);
+    for (int i = 0; i < r; ++i) {
+        if (!IsPow2(s.dims[i]))
+            return false;
+        logd[i] = Log2(s.dims[i]);
+        n += logd[i];
+    }
+    const int t = 5 + log_ve;
+    const int umax = log_ve == 1 ? 12 : 11; // 32 KB tile
+    if (n < umax || n - umax > 8 * kTileTables)
+        return false;
+    // Input bit offsets of each input axis (axis r-1 is fastest).
+    std::vector<int> in_off(r), out_off(r), out_axis_of_in(r);
+    for (int i = r - 1, o = 0; i >= 0; --i) {
+        in_off[i] = o;
+        o += logd[i];
+    }
+    for (int j = 0; j < r; ++j)
+        out_axis_of_in[s.perm[j]] = j;
+    for (int j = r - 1, o = 0; j >= 0; --j) {
+        out_off[j] = o;
+        o += logd[s.perm[j]];
+    }
+    std::vector<int> dst(n), src(n);
+    for (int i = 0; i < r; ++i)
+        for (int q = 0; q < logd[i]; ++q) {
+            int ib = in_off[i] + q;
+            int ob = out_off[out_axis_of_in[i]] + q;
+            dst[ib] = ob;
+            src[ob] = ib;
+        }
+    // Tile bit set U (input positions).
+    std::vector<char> inU(n, 0);
+    int u = 0;
+    for (int b = 0; b < t; ++b)
+        if (!inU[b]) {
+            inU[b] = 1;
+            ++u;
+        }
+    for (int j = 0; j < t; ++j)
+        if (!inU[src[j]]) {
+            inU[src[j]] = 1;
+            ++u;
+        }
+    for (int b = 0; b < n && u < umax; ++b)
+        if (!inU[b]) {
+            inU[b] = 1;
+            ++u;
+        }
+    std::vector<int> Us, Vs;
+    for (int b = 0; b < n; ++b)
+        (inU[b] ? Us : Vs).push_back(b);
+    // Output positions of U, sorted.
+    std::vector<int> Os;
+    for (int b : Us)
+        Os.push_back(dst[b]);
+    std::sort(Os.begin(), Os.end());
+    std::vector<int> pos_in_Us(n, -1);
+    for (size_t i = 0; i < Us.size(); ++i)
+        pos_in_Us[Us[i]] = (int)i;
+
+    std::memset(&p, 0, sizeof(p));
+    p.n = n;
+    p.u = u;
+    p.t = t;
+    p.n_outer = n - u;
+    p.total_tiles = batch << (n - u);
+    const int hb = u - t; // bits of a run index
+    for (int h = 0; h < (1 << hb); ++h) {
+        uint64_t vin = 0, vout = 0;
+        uint32_t lh = 0;
+        for (int j = 0; j < hb; ++j)
+            if ((h >> j) & 1) {
+                vin |= 1ull << Us[t + j];
+                vout |= 1ull << Os[t + j];
+                lh |= 1u << pos_in_Us[src[Os[t + j]]];
+            }
+        p.in_hi[h] = vin;
+        p.out_hi[h] = vout;
+        p.l_hi[h] = lh;
+    }
+    for (int m = 0; m < (1 << t); ++m) {
+        uint32_t l = 0;
+        for (int j = 0; j < t; ++j)
+            if ((m >> j) & 1)
+                l |= 1u << pos_in_Us[src[Os[j]]];
+        p.l_lo[m] = l;
+    }
+    const int nv = (int)Vs.size();
+    for (int k = 0; k < kTileTables; ++k)
+        for (int v = 0; v < 256; ++v) {
+            uint64_t ti = 0, to = 0;
+            for (int j = 0; j < 8; ++j) {
+                int bit = 8 * k + j;
+                if (bit < nv && ((v >> j) & 1)) {
+                    ti |= 1ull << Vs[bit];
+                    to |= 1ull << dst[Vs[bit]];
+                }
+            }
+            p.tile_in[k][v] = ti;
+            p.tile_out[k][v] = to;
+        }
+    return true;
+}
+
+template <typename E, int LOG_VE, typename Store>
+int LaunchBitperm(const BitParams &p, const void *in, Store store,
+                  cudaStream_t stream)
+{
+    const size_t smem = (sizeof(E) << p.u);
+    auto kern = bitperm_kernel<E, LOG_VE, Store>;
+    static thread_local bool configured = false;
+    if (!configured) {
+        JETGPU_CUDA_TRY(cudaFuncSetAttribute(
+            kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        configured = true;
+    }
+    unsigned grid = GridFor(p.total_tiles, 6);
+    kern<<<grid, kThreads, smem, stream>>>(p, reinterpret_cast<const E *>(in),
+                                           store);
+    return CheckLaunch("bitperm_kernel");
+}
+
+} // namespace
+
+int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
+                const uint64_t *shape, const int32_t *perm, int dtype,
+                cudaStream_t stream)
+{
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    Simplified s;
+    int rc = Simplify(rank, shape, perm, s);
+    if (rc)
+        return rc;
+    if (batch == 0 || s.size == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in != nullptr && out != nullptr, "null data pointer");
+    const size_t eb = ElemBytes(dtype);
+    bool identity = true;
+    for (size_t j = 0; j < s.perm.size(); ++j)
+        identity = identity && (s.perm[j] == (int)j);
+    if (identity) {
+        JETGPU_CUDA_TRY(cudaMemcpyAsync(out, in, s.size * batch * eb,
+                                        cudaMemcpyDeviceToDevice, stream));
+        return JETGPU_OK;
+    }
+    const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+    if (aligned) {
+        static thread_local BitParams bp; // ~14 KB: keep off the stack
+        if (dtype == JETGPU_C64 && BuildBitParams(s, batch, 1, bp))
+            return LaunchBitperm<uint2, 1>(bp, in,
+                                           PlainStore<uint2>{(uint2 *)out},
+                                           stream);
+        if (dtype == JETGPU_C128 && BuildBitParams(s, batch, 0, bp))
+            return LaunchBitperm<uint4, 0>(bp, in,
+                                           PlainStore<uint4>{(uint4 *)out},
+                                           stream);
+    }
+    GatherParams gp;
+    BuildGather(s, batch, gp);
+    unsigned grid = GridFor((gp.total + kThreads - 1) / kThreads, 8);
+    if (dtype == JETGPU_C64)
+        gather_kernel<uint2><<<grid, kThreads, 0, stream>>>(
+            gp, (const uint2 *)in, (uint2 *)out);
+    else
+        gather_kernel<uint4><<<grid, kThreads, 0, stream>>>(
+            gp, (const uint4 *)in, (uint4 *)out);
+    return CheckLaunch("gather_kernel");
+}
+
+int PermuteSplitTf32(const void *in, float *planes, int rank,
+                     const uint64_t *shape, const int32_t *perm, uint64_t rows,
+                     uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                     int scale_exp, cudaStream_t stream)
+{
+    Simplified s;
+    int rc = Simplify(rank, shape, perm, s);
+    if (rc)
+        return rc;
+    JETGPU_REQUIRE(rows * cols == s.size, "split view does not match size");
+    JETGPU_REQUIRE(scale_exp >= -126 && scale_exp <= 127, "scale out of range");
+    SplitOut so;
+    so.planes = planes;
+    so.plane_stride = plane_stride;
+    so.cols = cols;
+    so.pitch = pitch;
+    so.scale = ldexpf(1.0f, scale_exp);
+    const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
+                         (pitch % 2 == 0) && (plane_stride % 2 == 0);
+    static thread_local BitParams bp;
+    if (aligned && IsPow2(cols) && cols >= 2 && BuildBitParams(s, 1, 1, bp))
+        return LaunchBitperm<uint2, 1>(bp, in, SplitStore{so}, stream);
+    GatherParams gp;
+    BuildGather(s, 1, gp);
+    unsigned grid = GridFor((gp.total + kThreads - 1) / kThreads, 8);
+    gather_split_kernel<<<grid, kThreads, 0, stream>>>(gp, (const float2 *)in,
+                                                       so);
+    return CheckLaunch("gather_split_kernel");
+}
+
+} // namespace jetgpu
+
+extern "C" {
+
+int jetgpu_permute(const void *in, void *out, int rank, const uint64_t *shape,
+                   const int32_t *perm, int dtype, void *stream)
+{
+    jetgpu::ClearError();
+    return jetgpu::PermuteImpl(in, out, 1, rank, shape, perm, dtype,
+                               jetgpu::AsStream(stream));
+}
+
+int jetgpu_permute_batched(const void *in, void *out, uint64_t batch, int rank,
+                           const uint64_t *shape, const int32_t *perm,
+                           int dtype, void *stream)
+{
+    jetgpu::ClearError();
+    return jetgpu::PermuteImpl(in, out, batch, rank, shape, perm, dtype,
+                               jetgpu::AsStream(stream));
+}
+
+} // extern "C"

@@ -1,0 +1,310 @@
+// Element-wise and reduction kernels: AddTensors, Conj, the FP64 cross-slice
+// sum, device SliceIndex and the max-exponent query.
+#include <vector>
+
+#include "common.cuh"
+
+namespace jetgpu {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename V>
+__global__ void add_kernel(const V *__restrict__ a, const V *__restrict__ b,
+                           V *__restrict__ c, uint64_t n)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        V x = a[i], y = b[i];
+        c[i] = V{x.x + y.x, x.y + y.y};
+    }
+}
+
+template <typename V>
+__global__ void conj_kernel(const V *__restrict__ a, V *__restrict__ c, uint64_t n)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        V x = a[i];
+        c[i] = V{x.x, -x.y};
+    }
+}
+
+// size >= kThreads: one thread per element, slices summed in order.
+template <typename V>
+__global__ void slice_sum_wide(const V *__restrict__ r, double2 *__restrict__ out,
+                               uint64_t n_slices, uint64_t size, int accumulate)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < size;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        double re = 0, im = 0;
+        if (accumulate) {
+            re = out[i].x;
+            im = out[i].y;
+        }
+        for (uint64_t s = 0; s < n_slices; ++s) {
+            V v = r[s * size + i];
+            re += (double)v.x;
+            im += (double)v.y;
+        }
+        out[i] = make_double2(re, im);
+    }
+}
+
+// Small outputs (amplitudes): one CTA per element; threads stride over the
+// slices, then a fixed-shape tree reduction (deterministic).
+template <typename V>
+__global__ void slice_sum_narrow(const V *__restrict__ r, double2 *__restrict__ out,
+                                 uint64_t n_slices, uint64_t size, int accumulate)
+{
+    __shared__ double sre[kThreads], sim[kThreads];
+    for (uint64_t i = blockIdx.x; i < size; i += gridDim.x) {
+        double re = 0, im = 0;
+        for (uint64_t s = threadIdx.x; s < n_slices; s += blockDim.x) {
+            V v = r[s * size + i];
+            re += (double)v.x;
+            im += (double)v.y;
+        }
+        sre[threadIdx.x] = re;
+        sim[threadIdx.x] = im;
+        __syncthreads();
+        for (int w = kThreads / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) {
+                sre[threadIdx.x] += sre[threadIdx.x + w];
+                sim[threadIdx.x] += sim[threadIdx.x + w];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            double2 prev = accumulate ? out[i] : make_double2(0, 0);
+            out[i] = make_double2(prev.x + sre[0], prev.y + sim[0]);
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int kMaxRank = 64;
+
+struct SliceParams {
+    int free_rank;
+    uint64_t free_dims[kMaxRank];
+    uint64_t free_strides[kMaxRank];
+    int n_axes;
+    uint64_t fixed_stride[kMaxRank];  // input stride of each sliced axis
+    uint64_t fixed_dim[kMaxRank];     // its dimension
+    uint64_t value_stride[kMaxRank];  // divisor of the global slice value
+    uint64_t out_size;
+    uint64_t first_value;
+    uint64_t total;                   // n_values * out_size
+};
+
+template <typename E>
+__global__ void slice_gather_kernel(const __grid_constant__ SliceParams p,
+                                    const E *__restrict__ in, E *__restrict__ out)
+{
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = idx / p.out_size;
+        uint64_t o = idx - s * p.out_size;
+        const uint64_t v = p.first_value + s;
+        uint64_t src = 0;
+        for (int j = 0; j < p.n_axes; ++j)
+            src += ((v / p.value_stride[j]) % p.fixed_dim[j]) * p.fixed_stride[j];
+        for (int j = p.free_rank - 1; j >= 0; --j) {
+            const uint64_t d = p.free_dims[j];
+            const uint64_t q = o / d;
+            src += (o - q * d) * p.free_strides[j];
+            o = q;
+        }
+        out[idx] = in[src];
+    }
+}
+
+__global__ void init_exp_kernel(int *e) { *e = -1000; }
+
+template <typename V, typename U>
+__global__ void max_exp_kernel(const V *__restrict__ x, uint64_t n, int *e)
+{
+    U best = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        V v = x[i];
+        U a, b;
+        if constexpr (sizeof(U) == 4) {
+            a = (U)(__float_as_uint((float)v.x) & 0x7fffffffu);
+            b = (U)(__float_as_uint((float)v.y) & 0x7fffffffu);
+        }
+        else {
+            a = (U)((unsigned long long)__double_as_longlong((double)v.x) &
+                    0x7fffffffffffffffull);
+            b = (U)((unsigned long long)__double_as_longlong((double)v.y) &
+                    0x7fffffffffffffffull);
+        }
+        best = max(best, max(a, b));
+    }
+    // Exponent of the largest magnitude (finite values; bit patterns of
+    // non-negative floats order like the values).
+    int ex;
+    if (best == 0) {
+        ex = -1000;
+    }
+    else if constexpr (sizeof(U) == 4) {
+        const int biased = (int)((best >> 23) & 0xff);
+        ex = biased == 0 ? -127 : biased - 127;
+    }
+    else {
+        const int biased = (int)((best >> 52) & 0x7ff);
+        ex = biased == 0 ? -1023 : biased - 1023;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(e, ex);
+}
+
+} // namespace
+} // namespace jetgpu
+
+using namespace jetgpu;
+
+extern "C" {
+
+int jetgpu_add(const void *A, const void *B, void *C, uint64_t size, int dtype,
+               void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    if (size == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(A && B && C, "null pointer");
+    unsigned grid = GridFor((size + kThreads - 1) / kThreads, 8);
+    if (dtype == JETGPU_C64)
+        add_kernel<float2><<<grid, kThreads, 0, AsStream(stream)>>>(
+            (const float2 *)A, (const float2 *)B, (float2 *)C, size);
+    else
+        add_kernel<double2><<<grid, kThreads, 0, AsStream(stream)>>>(
+            (const double2 *)A, (const double2 *)B, (double2 *)C, size);
+    return CheckLaunch("add_kernel");
+}
+
+int jetgpu_conj(const void *in, void *out, uint64_t size, int dtype, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    if (size == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in && out, "null pointer");
+    unsigned grid = GridFor((size + kThreads - 1) / kThreads, 8);
+    if (dtype == JETGPU_C64)
+        conj_kernel<float2><<<grid, kThreads, 0, AsStream(stream)>>>(
+            (const float2 *)in, (float2 *)out, size);
+    else
+        conj_kernel<double2><<<grid, kThreads, 0, AsStream(stream)>>>(
+            (const double2 *)in, (double2 *)out, size);
+    return CheckLaunch("conj_kernel");
+}
+
+int jetgpu_slice_sum_f64(const void *results, uint64_t n_slices, uint64_t size,
+                         int dtype, void *out, int accumulate, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    if (size == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(out != nullptr, "null output");
+    if (n_slices == 0 && accumulate)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(n_slices == 0 || results != nullptr, "null results");
+    cudaStream_t st = AsStream(stream);
+    if (size >= kThreads) {
+        unsigned grid = GridFor((size + kThreads - 1) / kThreads, 8);
+        if (dtype == JETGPU_C64)
+            slice_sum_wide<float2><<<grid, kThreads, 0, st>>>(
+                (const float2 *)results, (double2 *)out, n_slices, size, accumulate);
+        else
+            slice_sum_wide<double2><<<grid, kThreads, 0, st>>>(
+                (const double2 *)results, (double2 *)out, n_slices, size, accumulate);
+    }
+    else {
+        unsigned grid = (unsigned)size;
+        if (dtype == JETGPU_C64)
+            slice_sum_narrow<float2><<<grid, kThreads, 0, st>>>(
+                (const float2 *)results, (double2 *)out, n_slices, size, accumulate);
+        else
+            slice_sum_narrow<double2><<<grid, kThreads, 0, st>>>(
+                (const double2 *)results, (double2 *)out, n_slices, size, accumulate);
+    }
+    return CheckLaunch("slice_sum");
+}
+
+int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
+                        int n_axes, const int32_t *axes,
+                        const uint64_t *value_strides, uint64_t first_value,
+                        uint64_t n_values, void *out, int dtype, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(rank >= 0 && rank <= kMaxRank, "rank out of range");
+    JETGPU_REQUIRE(n_axes >= 0 && n_axes <= rank, "bad number of sliced axes");
+    std::vector<uint64_t> stride(rank, 1);
+    for (int i = rank - 2; i >= 0; --i)
+        stride[i] = stride[i + 1] * shape[i + 1];
+    std::vector<char> fixed(rank, 0);
+    static thread_local SliceParams p;
+    p.n_axes = n_axes;
+    for (int j = 0; j < n_axes; ++j) {
+        JETGPU_REQUIRE(axes[j] >= 0 && axes[j] < rank && !fixed[axes[j]],
+                       "bad sliced axis");
+        JETGPU_REQUIRE(value_strides[j] >= 1, "bad value stride");
+        fixed[axes[j]] = 1;
+        p.fixed_stride[j] = stride[axes[j]];
+        p.fixed_dim[j] = shape[axes[j]];
+        p.value_stride[j] = value_strides[j];
+    }
+    p.free_rank = 0;
+    p.out_size = 1;
+    for (int i = 0; i < rank; ++i)
+        if (!fixed[i]) {
+            p.free_dims[p.free_rank] = shape[i];
+            p.free_strides[p.free_rank] = stride[i];
+            ++p.free_rank;
+            p.out_size *= shape[i];
+        }
+    p.first_value = first_value;
+    p.total = p.out_size * n_values;
+    if (p.total == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in && out, "null pointer");
+    unsigned grid = GridFor((p.total + kThreads - 1) / kThreads, 8);
+    if (dtype == JETGPU_C64)
+        slice_gather_kernel<uint2><<<grid, kThreads, 0, AsStream(stream)>>>(
+            p, (const uint2 *)in, (uint2 *)out);
+    else
+        slice_gather_kernel<uint4><<<grid, kThreads, 0, AsStream(stream)>>>(
+            p, (const uint4 *)in, (uint4 *)out);
+    return CheckLaunch("slice_gather_kernel");
+}
+
+int jetgpu_max_exponent(const void *x, uint64_t size, int dtype, int *exp_dev,
+                        void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(exp_dev != nullptr, "null exponent pointer");
+    cudaStream_t st = AsStream(stream);
+    init_exp_kernel<<<1, 1, 0, st>>>(exp_dev);
+    if (size == 0)
+        return CheckLaunch("init_exp_kernel");
+    JETGPU_REQUIRE(x != nullptr, "null input");
+    unsigned grid = GridFor((size + kThreads - 1) / kThreads, 8);
+    if (dtype == JETGPU_C64)
+        max_exp_kernel<float2, uint32_t><<<grid, kThreads, 0, st>>>(
+            (const float2 *)x, size, exp_dev);
+    else
+        max_exp_kernel<double2, unsigned long long><<<grid, kThreads, 0, st>>>(
+            (const double2 *)x, size, exp_dev);
+    return CheckLaunch("max_exp_kernel");
+}
+
+} // extern "C"
