@@ -79,7 +79,7 @@ class Clocks:
             self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.tmp, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -185,14 +185,14 @@ def run_ours(args, rank, world, local_rank):
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
-    w = workload()
+    w = workload(12, N_COMMON, 12) if args.small else workload()
     m, n, k = w["m"], w["n"], w["k"]
     kp = k
     g = torch.Generator(device=dev)
     g.manual_seed(SEED + rank)
     # torch.randn on complex draws re, im i.i.d. N(0, 1/2).
-    A = torch.randn(2 ** 27, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
-    B = torch.randn(2 ** 25, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
+    A = torch.randn(m * k, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
+    B = torch.randn(k * n, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
     pa = torch.empty(4 * m * kp, dtype=torch.float32, device=dev)
     pb = torch.empty(4 * n * kp, dtype=torch.float32, device=dev)
     C = torch.empty(m * n, dtype=torch.complex64, device=dev)
@@ -249,6 +249,14 @@ def run_ours(args, rank, world, local_rank):
     ref_rows = At.astype(np.complex128) @ Bt.astype(np.complex128)
     got_rows = C.view(m, n)[:rows].cpu().numpy()
     rel_err = float(np.linalg.norm(got_rows - ref_rows) / np.linalg.norm(ref_rows))
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"ms_per_step": ms_step, "value": value, "rel_err_vs_fp64": rel_err,
+                              "stages_ms": {"split_a": statistics.mean(split_a),
+                                            "split_b": statistics.mean(split_b),
+                                            "gemm_tf32x3": statistics.mean(gemm)},
+                              "m": m, "n": n, "k": k, "clocks": clocks}), flush=True)
+        return
 
     # Plain FP32 form of the same step (permute + SIMT complex GEMM), 2 runs.
     ws_need = capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
@@ -352,10 +360,14 @@ def run_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: rank-25 x rank-25 (M = N = 2^12, K = 2^13)")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="skip the plain-FP32, end-to-end and CPU legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

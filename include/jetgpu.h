@@ -45,6 +45,48 @@ extern "C" {
 /* Complex product algorithms for the tensor-core form. */
 #define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
 
+/* ---------------------------------------------------------------------------
+ * Memory, streams and graphs: the runtime under the C++ host API.
+ * The reference allocates per operation (CudaTensor.hpp:158-160, 638-640);
+ * here device memory comes from a caching allocator (freed blocks are kept
+ * per size and reused, stream-ordered on the library stream) or from a
+ * caller-sized arena for captured graphs.
+ * ------------------------------------------------------------------------- */
+
+/* Allocates `bytes` of device memory from the caching allocator (256-byte
+ * aligned). Allocates device memory (cudaMalloc) only when no cached block
+ * of the size class is free. */
+int jetgpu_malloc(size_t bytes, void **ptr);
+
+/* Returns a block from jetgpu_malloc to the cache. */
+int jetgpu_free(void *ptr);
+
+/* Releases every cached (free) block to the device. */
+int jetgpu_release_cached(void);
+
+/* Bytes currently handed out by / held in the caching allocator. */
+int jetgpu_memory_stats(size_t *in_use, size_t *cached, size_t *peak_in_use);
+
+/* The library's default stream for the host API (created on first use,
+ * non-blocking with respect to the legacy stream). */
+void *jetgpu_default_stream(void);
+
+/* Copies: kind 0 host->device, 1 device->host, 2 device->device,
+ * stream-ordered on `stream`. */
+int jetgpu_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+
+/* Fills `bytes` of device memory with zero bytes (stream-ordered). */
+int jetgpu_memset_zero(void *dst, size_t bytes, void *stream);
+
+int jetgpu_stream_synchronize(void *stream);
+
+/* Stream capture into an executable CUDA graph (cudaStreamBeginCapture /
+ * EndCapture / GraphInstantiate), replay and destruction. */
+int jetgpu_graph_begin(void *stream);
+int jetgpu_graph_end(void *stream, void **graph_exec);
+int jetgpu_graph_launch(void *graph_exec, void *stream);
+int jetgpu_graph_destroy(void *graph_exec);
+
 /* Message of the last failing call made by this host thread ("" if none). */
 const char *jetgpu_last_error(void);
 

@@ -199,15 +199,19 @@ def _size(labels, dims) -> float:
 
 
 def greedy_path(net: Network, seed: int = 0, sliced: Sequence[str] = (),
-                temperature: float = 0.0) -> List[Tuple[int, int]]:
-    """Seeded greedy min-intermediate-size path.
+                temperature: float = 0.0, score: str = "size") -> List[Tuple[int, int]]:
+    """Seeded greedy path.
 
-    Repeatedly contracts the pair of connected nodes whose result is
-    smallest (ties, and with temperature > 0 also near-ties, broken by a
-    seeded random key; score = log2 size(out) - temperature * log(-log u));
-    disconnected remainders are then contracted smallest first. Sliced
+    Repeatedly contracts the connected pair of nodes with the lowest score:
+    score "size" is log2 of the result's size (the min-intermediate-size
+    heuristic); score "gain" is size(result) - size(a) - size(b), the
+    memory a contraction adds (as in opt_einsum's greedy), signed-log2
+    compressed. Ties -- and with temperature > 0 near-ties, through Gumbel
+    noise -temperature * log(-log u) -- are broken by a seeded random key.
+    Disconnected remainders are then contracted smallest first. Sliced
     indices count as dimension 1."""
     rng = np.random.default_rng(seed)
+    score_kind = score
     dims = dict(net.index_dims())
     for x in sliced:
         dims[x] = 1
@@ -229,7 +233,11 @@ def greedy_path(net: Network, seed: int = 0, sliced: Sequence[str] = (),
         return res
 
     def score(a: int, b: int) -> float:
-        s = math.log2(max(_size(out_labels(a, b), dims), 1.0))
+        if score_kind == "gain":
+            g = (_size(out_labels(a, b), dims) - _size(nodes[a], dims) - _size(nodes[b], dims))
+            s = math.copysign(math.log2(abs(g) + 1.0), g)
+        else:
+            s = math.log2(max(_size(out_labels(a, b), dims), 1.0))
         noise = float(rng.random())
         if temperature > 0:
             s -= temperature * math.log(-math.log(max(noise, 1e-300)))
@@ -281,6 +289,20 @@ def greedy_path(net: Network, seed: int = 0, sliced: Sequence[str] = (),
         path.append((a, b))
         rest = sorted(nodes.keys(), key=lambda i: (_size(nodes[i], dims), i))
     return path
+
+
+def find_path(net: Network, restarts: int = 16, seed: int = 0,
+              sliced: Sequence[str] = ()) -> List[Tuple[int, int]]:
+    """Best of `restarts` seeded greedy runs (both scores, with and without
+    noise) by total flops, then by the largest intermediate."""
+    best = None
+    for r in range(restarts):
+        for score, temp in (("gain", 0.0), ("gain", 0.3), ("size", 0.0)):
+            p = greedy_path(net, seed=seed * 1000 + r, sliced=sliced, temperature=temp, score=score)
+            flops, big = path_cost(net, p, sliced)
+            if best is None or (flops, big) < best[0]:
+                best = ((flops, big), p)
+    return best[1]
 
 
 def path_cost(net: Network, path: Sequence[Tuple[int, int]], sliced: Sequence[str] = ()):

@@ -145,6 +145,20 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Compensated (Kahan) running sum: vector-shaped products reduce long k
+// ranges in one thread, where plain FP32 accumulation would lose ~log2(k)
+// bits; the extra adds are free in these bandwidth-bound kernels.
+template <typename T> struct KahanSum {
+    T s = 0, c = 0;
+    __device__ __forceinline__ void add(T x)
+    {
+        const T y = x - c;
+        const T t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
 // y[m] (+ partial s) = sum_{k in chunk s} A[m, k] x[k]; one warp per row.
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -161,14 +175,13 @@ __global__ void __launch_bounds__(256)
         return;
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
-    T re = 0, im = 0;
+    KahanSum<T> sr, si;
     for (int64_t k = k_begin + lane; k < k_end; k += 32) {
         V a = A[m * K + k], b = x[k];
-        re = fma(a.x, b.x, re);
-        re = fma(-a.y, b.y, re);
-        im = fma(a.x, b.y, im);
-        im = fma(a.y, b.x, im);
+        sr.add(fma(a.x, b.x, -a.y * b.y));
+        si.add(fma(a.x, b.y, a.y * b.x));
     }
+    T re = sr.s, im = si.s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -192,14 +205,13 @@ __global__ void __launch_bounds__(256)
     const int64_t k_end = min(K, k_begin + kchunk);
     if (N == 1) {
         // Dot product: the block reduces its k chunk.
-        T re = 0, im = 0;
+        KahanSum<T> sr, si;
         for (int64_t k = k_begin + threadIdx.x; k < k_end; k += blockDim.x) {
             V a = x[k], b = B[k];
-            re = fma(a.x, b.x, re);
-            re = fma(-a.y, b.y, re);
-            im = fma(a.x, b.y, im);
-            im = fma(a.y, b.x, im);
+            sr.add(fma(a.x, b.x, -a.y * b.y));
+            si.add(fma(a.x, b.y, a.y * b.x));
         }
+        T re = sr.s, im = si.s;
         __shared__ T sre[256], sim[256];
         sre[threadIdx.x] = re;
         sim[threadIdx.x] = im;
@@ -218,15 +230,13 @@ __global__ void __launch_bounds__(256)
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N)
         return;
-    T re = 0, im = 0;
+    KahanSum<T> sr, si;
     for (int64_t k = k_begin; k < k_end; ++k) {
         V a = x[k], b = B[k * N + n];
-        re = fma(a.x, b.x, re);
-        re = fma(-a.y, b.y, re);
-        im = fma(a.x, b.y, im);
-        im = fma(a.y, b.x, im);
+        sr.add(fma(a.x, b.x, -a.y * b.y));
+        si.add(fma(a.x, b.y, a.y * b.x));
     }
-    out[s * N + n] = V{re * scale, im * scale};
+    out[s * N + n] = V{sr.s * scale, si.s * scale};
 }
 
 template <typename T>

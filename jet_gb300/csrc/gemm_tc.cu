@@ -10,11 +10,12 @@
 // TF32 products (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM:
 //   Cr += Ar Br - Ai Bi,   Ci += Ar Bi + Ai Br.
 //
-// One CTA computes a 128 x 128 complex tile: Cr in TMEM columns [0,128),
-// Ci in [128,256). Warp 0 lane 0 feeds a 3-stage ring of shared-memory
-// stages with TMA (8 boxes of 128 rows x 16 floats, 64-byte swizzle); warp 1
-// lane 0 issues tcgen05.mma (M=128, N=128, K=8) and releases stages with
-// tcgen05.commit; all four warps drain TMEM with tcgen05.ld in the epilogue.
+// One CTA computes a 128 x 128 complex tile. Warp 0 lane 0 feeds a 3-stage
+// ring of shared-memory stages with TMA (8 boxes of 128 rows x 16 floats,
+// 64-byte swizzle); warp 1 lane 0 issues tcgen05.mma (M=128, N=128, K=8) into
+// one of two TMEM accumulator sets (Cr, Ci: 2 x 256 columns) and releases
+// stages with tcgen05.commit; eight accumulator warps fold each finished
+// 128-deep K chunk into FP32 registers (see the kernel comment) and write C.
 // Every mbarrier wait is bounded: on timeout the kernel records
 // JETGPU_ERR_TIMEOUT in a device status word, skips the remaining work,
 // frees its TMEM and returns.
@@ -37,8 +38,10 @@ constexpr int kBK = 16;                    // complex k per stage (64 bytes of f
 constexpr int kStages = 3;
 constexpr int kTileBytes = kBM * kBK * 4;  // one plane box: 8 KB
 constexpr int kStageBytes = 8 * kTileBytes; // 4 A planes + 4 B planes: 64 KB
-constexpr int kTmemCols = 256;
-constexpr int kThreads = 128;
+constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
+constexpr int kAccWarps = 8;                  // accumulator warps
+constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
+constexpr int kChunkStages = 8;               // stages (x16 complex k) per TMEM chunk
 constexpr unsigned long long kWaitNs = 4000000000ull; // 4 s bound per wait
 
 __device__ __forceinline__ uint32_t SmemAddr(const void *p)
@@ -171,6 +174,15 @@ __device__ __forceinline__ void TmemWaitLoad()
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Warp roles: warp 0 issues TMA loads, warp 1 allocates TMEM and issues the
+// MMAs, warps 2..9 ("accumulator warps") drain finished K chunks from TMEM.
+// Precision: the tensor core rounds its FP32 accumulator at every MMA
+// instruction, so a long K makes the rounding error grow with K. The MMAs
+// therefore accumulate only kChunkStages stages (128 complex k) into one of
+// two TMEM accumulator sets; the accumulator warps add every finished chunk
+// into FP32 registers (round-to-nearest) while the next chunk accumulates in
+// the other set. Accumulator warp w (w = 2..9) owns TMEM lanes 32*(w%4)..+31
+// (tile rows) and columns [64*h, 64*h + 64) of Cr and Ci, h = (w - 2) / 4.
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
@@ -180,7 +192,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
-    __shared__ __align__(8) uint64_t acc_bar;
+    __shared__ __align__(8) uint64_t acc_full[2];
+    __shared__ __align__(8) uint64_t acc_empty[2];
     __shared__ uint32_t tmem_slot;
 
     uint8_t *smem = reinterpret_cast<uint8_t *>(
@@ -189,13 +202,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int lane = threadIdx.x & 31;
     const int m0 = blockIdx.y * kBM;
     const int n0 = blockIdx.x * kBN;
+    const int nchunks = (ktiles + kChunkStages - 1) / kChunkStages;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             MbarInit(SmemAddr(&full_bar[s]), 1);
             MbarInit(SmemAddr(&empty_bar[s]), 1);
         }
-        MbarInit(SmemAddr(&acc_bar), 1);
+        for (int b = 0; b < 2; ++b) {
+            MbarInit(SmemAddr(&acc_full[b]), 1);
+            MbarInit(SmemAddr(&acc_empty[b]), kAccWarps);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -236,10 +253,17 @@ __global__ void __launch_bounds__(kThreads, 1)
             // MMA issuer.
             constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false);
             constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true);
-            const uint32_t d_re = tmem;
-            const uint32_t d_im = tmem + kBN;
             bool ok = true;
             for (int kt = 0; kt < ktiles && ok; ++kt) {
+                const int chunk = kt / kChunkStages;
+                const int buf = chunk & 1;
+                const bool chunk_start = (kt % kChunkStages) == 0;
+                const bool chunk_end = (kt % kChunkStages) == kChunkStages - 1 || kt == ktiles - 1;
+                if (chunk_start &&
+                    !MbarWait(SmemAddr(&acc_empty[buf]), ((uint32_t)(chunk >> 1) & 1u) ^ 1u)) {
+                    ok = false;
+                    break;
+                }
                 const int s = kt % kStages;
                 const uint32_t phase = (uint32_t)(kt / kStages) & 1u;
                 if (!MbarWait(SmemAddr(&full_bar[s]), phase)) {
@@ -247,6 +271,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 FenceAfterSync();
+                const uint32_t d_re = tmem + buf * 2 * kBN;
+                const uint32_t d_im = d_re + kBN;
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
 #pragma unroll
                 for (int kk = 0; kk < kBK / 8; ++kk) {
@@ -259,9 +285,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint64_t brl = SmemDesc(base + 5 * kTileBytes + koff);
                     const uint64_t bih = SmemDesc(base + 6 * kTileBytes + koff);
                     const uint64_t bil = SmemDesc(base + 7 * kTileBytes + koff);
-                    const uint32_t first = (kt == 0 && kk == 0) ? 0u : 1u;
+                    const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                     // Cr += Ar Br
-                    MmaTf32(d_re, arh, brh, kIdesc, first);
+                    MmaTf32(d_re, arh, brh, kIdesc, acc);
                     MmaTf32(d_re, arh, brl, kIdesc, 1u);
                     MmaTf32(d_re, arl, brh, kIdesc, 1u);
                     // Cr -= Ai Bi
@@ -269,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     MmaTf32(d_re, aih, bil, kIdescNeg, 1u);
                     MmaTf32(d_re, ail, bih, kIdescNeg, 1u);
                     // Ci += Ar Bi
-                    MmaTf32(d_im, arh, bih, kIdesc, first);
+                    MmaTf32(d_im, arh, bih, kIdesc, acc);
                     MmaTf32(d_im, arh, bil, kIdesc, 1u);
                     MmaTf32(d_im, arl, bih, kIdesc, 1u);
                     // Ci += Ai Br
@@ -278,42 +304,68 @@ __global__ void __launch_bounds__(kThreads, 1)
                     MmaTf32(d_im, ail, brh, kIdesc, 1u);
                 }
                 MmaCommit(SmemAddr(&empty_bar[s]));
+                if (chunk_end)
+                    MmaCommit(SmemAddr(&acc_full[buf]));
             }
-            // Signals the epilogue once every issued MMA has completed.
-            MmaCommit(SmemAddr(&acc_bar));
         }
         __syncwarp();
     }
-
-    // Epilogue: warp w owns TMEM lanes / tile rows [32w, 32w + 32).
-    const bool ready = MbarWait(SmemAddr(&acc_bar), 0);
-    __syncwarp();
-    FenceAfterSync();
-    const int row = m0 + warp * 32 + lane;
-    if (ready && ktiles > 0) {
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
-        for (int c = 0; c < kBN; c += 16) {
-            float re[16], im[16];
-            TmemLoad16(tmem + lane_base + c, re);
-            TmemLoad16(tmem + lane_base + kBN + c, im);
-            TmemWaitLoad();
-            if (row < M) {
-                float2 *dst = C + (size_t)row * N + n0 + c;
-                if (n0 + c + 16 <= N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+    else {
+        // Accumulator warps.
+        const int quad = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+        float acc_re[64], acc_im[64];
 #pragma unroll
-                    for (int j = 0; j < 16; j += 2) {
-                        float4 v = make_float4(re[j] * scale, im[j] * scale,
-                                               re[j + 1] * scale, im[j + 1] * scale);
-                        *reinterpret_cast<float4 *>(dst + j) = v;
-                    }
-                }
-                else {
+        for (int j = 0; j < 64; ++j) {
+            acc_re[j] = 0.f;
+            acc_im[j] = 0.f;
+        }
+        bool ok = true;
+        for (int chunk = 0; chunk < nchunks; ++chunk) {
+            const int buf = chunk & 1;
+            ok = MbarWait(SmemAddr(&acc_full[buf]), (uint32_t)(chunk >> 1) & 1u);
+            __syncwarp();
+            if (!ok)
+                break;
+            FenceAfterSync();
+            const uint32_t col0 = tmem + lane_base + buf * 2 * kBN + half * 64;
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (n0 + c + j < N)
-                            dst[j] = make_float2(re[j] * scale, im[j] * scale);
+            for (int c = 0; c < 64; c += 16) {
+                float re[16], im[16];
+                TmemLoad16(col0 + c, re);
+                TmemLoad16(col0 + kBN + c, im);
+                TmemWaitLoad();
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    acc_re[c + j] += re[j];
+                    acc_im[c + j] += im[j];
                 }
+            }
+            FenceBeforeSync();
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                 SmemAddr(&acc_empty[buf]))
+                             : "memory");
+        }
+        const int row = m0 + quad * 32 + lane;
+        if (ok && row < M) {
+            const int cbase = n0 + half * 64;
+            float2 *dst = C + (size_t)row * N + cbase;
+            if (cbase + 64 <= N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+#pragma unroll
+                for (int j = 0; j < 64; j += 2) {
+                    float4 v = make_float4(acc_re[j] * scale, acc_im[j] * scale,
+                                           acc_re[j + 1] * scale, acc_im[j + 1] * scale);
+                    *reinterpret_cast<float4 *>(dst + j) = v;
+                }
+            }
+            else {
+#pragma unroll
+                for (int j = 0; j < 64; ++j)
+                    if (cbase + j < N)
+                        dst[j] = make_float2(acc_re[j] * scale, acc_im[j] * scale);
             }
         }
     }

@@ -83,3 +83,174 @@ int jetgpu_device_info(int *sm_count, int *cc_major, int *cc_minor)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Memory, streams and graphs.
+// Device memory comes from the device's stream-ordered memory pool
+// (cudaMallocAsync on the library stream) with its release threshold raised so
+// freed blocks stay cached for reuse instead of returning to the driver.
+// ---------------------------------------------------------------------------
+namespace jetgpu {
+namespace {
+std::mutex g_stream_mutex;
+cudaStream_t g_streams[64] = {nullptr};
+bool g_pool_configured[64] = {false};
+
+int CurrentDevice()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return 0;
+    return dev;
+}
+} // namespace
+
+cudaStream_t LibraryStream()
+{
+    const int dev = CurrentDevice();
+    std::lock_guard<std::mutex> lock(g_stream_mutex);
+    if (g_streams[dev] == nullptr) {
+        cudaStream_t s = nullptr;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+            return nullptr;
+        g_streams[dev] = s;
+    }
+    if (!g_pool_configured[dev]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t threshold = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        }
+        g_pool_configured[dev] = true;
+    }
+    return g_streams[dev];
+}
+
+} // namespace jetgpu
+
+extern "C" {
+
+void *jetgpu_default_stream(void) { return (void *)jetgpu::LibraryStream(); }
+
+int jetgpu_malloc(size_t bytes, void **ptr)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(ptr != nullptr, "null output pointer");
+    *ptr = nullptr;
+    if (bytes == 0)
+        return JETGPU_OK;
+    cudaStream_t s = jetgpu::LibraryStream();
+    JETGPU_CUDA_TRY(cudaMallocAsync(ptr, (bytes + 255) / 256 * 256, s));
+    return JETGPU_OK;
+}
+
+int jetgpu_free(void *ptr)
+{
+    jetgpu::ClearError();
+    if (ptr == nullptr)
+        return JETGPU_OK;
+    JETGPU_CUDA_TRY(cudaFreeAsync(ptr, jetgpu::LibraryStream()));
+    return JETGPU_OK;
+}
+
+int jetgpu_release_cached(void)
+{
+    jetgpu::ClearError();
+    cudaMemPool_t pool;
+    JETGPU_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, jetgpu::CurrentDevice()));
+    JETGPU_CUDA_TRY(cudaStreamSynchronize(jetgpu::LibraryStream()));
+    JETGPU_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return JETGPU_OK;
+}
+
+int jetgpu_memory_stats(size_t *in_use, size_t *cached, size_t *peak_in_use)
+{
+    jetgpu::ClearError();
+    cudaMemPool_t pool;
+    JETGPU_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, jetgpu::CurrentDevice()));
+    uint64_t used = 0, reserved = 0, high = 0;
+    JETGPU_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+    JETGPU_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+    JETGPU_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high));
+    if (in_use)
+        *in_use = used;
+    if (cached)
+        *cached = reserved > used ? reserved - used : 0;
+    if (peak_in_use)
+        *peak_in_use = high;
+    return JETGPU_OK;
+}
+
+int jetgpu_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream)
+{
+    jetgpu::ClearError();
+    if (bytes == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(dst != nullptr && src != nullptr, "null pointer");
+    cudaMemcpyKind k = kind == 0   ? cudaMemcpyHostToDevice
+                       : kind == 1 ? cudaMemcpyDeviceToHost
+                       : kind == 2 ? cudaMemcpyDeviceToDevice
+                                   : cudaMemcpyDefault;
+    JETGPU_REQUIRE(kind >= 0 && kind <= 2, "bad copy kind");
+    JETGPU_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, k, jetgpu::AsStream(stream)));
+    return JETGPU_OK;
+}
+
+int jetgpu_memset_zero(void *dst, size_t bytes, void *stream)
+{
+    jetgpu::ClearError();
+    if (bytes == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(dst != nullptr, "null pointer");
+    JETGPU_CUDA_TRY(cudaMemsetAsync(dst, 0, bytes, jetgpu::AsStream(stream)));
+    return JETGPU_OK;
+}
+
+int jetgpu_stream_synchronize(void *stream)
+{
+    jetgpu::ClearError();
+    JETGPU_CUDA_TRY(cudaStreamSynchronize(jetgpu::AsStream(stream)));
+    return JETGPU_OK;
+}
+
+int jetgpu_graph_begin(void *stream)
+{
+    jetgpu::ClearError();
+    JETGPU_CUDA_TRY(cudaStreamBeginCapture(jetgpu::AsStream(stream),
+                                           cudaStreamCaptureModeThreadLocal));
+    return JETGPU_OK;
+}
+
+int jetgpu_graph_end(void *stream, void **graph_exec)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(graph_exec != nullptr, "null output pointer");
+    cudaGraph_t graph = nullptr;
+    JETGPU_CUDA_TRY(cudaStreamEndCapture(jetgpu::AsStream(stream), &graph));
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess)
+        return jetgpu::SetError(JETGPU_ERR_CUDA, std::string("cudaGraphInstantiate: ") +
+                                                     cudaGetErrorString(err));
+    *graph_exec = (void *)exec;
+    return JETGPU_OK;
+}
+
+int jetgpu_graph_launch(void *graph_exec, void *stream)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(graph_exec != nullptr, "null graph");
+    JETGPU_CUDA_TRY(cudaGraphLaunch((cudaGraphExec_t)graph_exec, jetgpu::AsStream(stream)));
+    return JETGPU_OK;
+}
+
+int jetgpu_graph_destroy(void *graph_exec)
+{
+    jetgpu::ClearError();
+    if (graph_exec)
+        JETGPU_CUDA_TRY(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec));
+    return JETGPU_OK;
+}
+
+} // extern "C"

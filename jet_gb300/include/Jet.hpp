@@ -1,0 +1,9 @@
+// Umbrella header of the GB300 Jet host API.
+#pragma once
+
+#include "jet/Abort.hpp"
+#include "jet/PathInfo.hpp"
+#include "jet/TaskBasedContractor.hpp"
+#include "jet/Tensor.hpp"
+#include "jet/TensorNetwork.hpp"
+#include "jet/Utilities.hpp"
