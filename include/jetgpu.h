@@ -160,6 +160,35 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
                     void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * Batched contraction: C[b] = contract(A[b], B[b]) for b < batch, C packed as
+ * batch x m x n. A batched operand (a_batched / b_batched != 0) holds `batch`
+ * tensors of its shape back to back; a shared one holds one tensor used by
+ * every b. Orderings, m, n, k, precision and scales as in jetgpu_contract.
+ * This is the slice batch of TensorNetwork::SliceIndices /
+ * TaskBasedContractor (TensorNetwork.hpp:210-284, TaskBasedContractor.hpp:
+ * 162-248): slice-dependent tensors carry the batch, slice-independent ones
+ * are shared. A batched A with a shared B folds the batch into M (one product
+ * of batch*m rows); otherwise the tensor-core and SIMT products run with a
+ * batch grid dimension.
+ */
+size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank,
+                                              const uint64_t *a_shape,
+                                              const int32_t *a_perm, int a_batched,
+                                              int b_rank, const uint64_t *b_shape,
+                                              const int32_t *b_perm, int b_batched,
+                                              uint64_t m, uint64_t n, uint64_t k,
+                                              int dtype, int precision);
+
+int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank,
+                            const uint64_t *a_shape, const int32_t *a_perm,
+                            int a_batched, const void *B, int b_rank,
+                            const uint64_t *b_shape, const int32_t *b_perm,
+                            int b_batched, void *C, uint64_t m, uint64_t n,
+                            uint64_t k, int dtype, int precision, int algo,
+                            int scale_a, int scale_b, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
+/*
  * The two stages of the TF32x3 form of jetgpu_contract, for callers that
  * schedule them separately (batched executors, profilers).
  *
@@ -223,6 +252,20 @@ int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
                         int n_axes, const int32_t *axes,
                         const uint64_t *value_strides, uint64_t first_value,
                         uint64_t n_values, void *out, int dtype, void *stream);
+
+/*
+ * jetgpu_slice_gather with the first slice value read from device memory
+ * (*first_value_dev) when the kernel runs, so that one captured CUDA graph can
+ * be replayed over successive chunks of slices; jetgpu_counter_add advances
+ * such a device counter (*counter_dev += delta) in stream order.
+ */
+int jetgpu_slice_gather_at(const void *in, int rank, const uint64_t *shape,
+                           int n_axes, const int32_t *axes,
+                           const uint64_t *value_strides,
+                           const uint64_t *first_value_dev, uint64_t n_values,
+                           void *out, int dtype, void *stream);
+
+int jetgpu_counter_add(uint64_t *counter_dev, uint64_t delta, void *stream);
 
 /*
  * Reads and clears the device status word that bounded waits inside the

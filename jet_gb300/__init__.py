@@ -15,6 +15,8 @@ from ._jet_bindings import (  # noqa: F401
     JetException,
     PathInfo,
     PathStepInfo,
+    SlicedContractorC64,
+    SlicedContractorC128,
     add_tensors,
     conj,
     contract_tensors,

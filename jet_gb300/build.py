@@ -84,10 +84,21 @@ def build_library(verbose: bool = False, ptxas_v: bool = False) -> str:
     return LIB_PATH
 
 
+def _load_sibling(name: str):
+    """Imports a module of this directory by path: building must not import
+    the jet_gb300 package, whose __init__ needs the libraries being built."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("jet_gb300_" + name,
+                                                  os.path.join(PKG_DIR, name + ".py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def build_all(verbose: bool = False) -> None:
     build_library(verbose=verbose)
-    from . import _bindings_build
-    _bindings_build.build_bindings(verbose=verbose)
+    _load_sibling("_bindings_build").build_bindings(verbose=verbose)
 
 
 if __name__ == "__main__":

@@ -77,6 +77,26 @@ int PermuteSplitTf32(const void *in, float *planes, int rank,
                      uint64_t cols, uint64_t pitch, uint64_t plane_stride,
                      int scale_exp, cudaStream_t stream);
 
+// Permute + TF32 split of `batch` tensors stored back to back; tensor b lands
+// in rows [b * rows, (b + 1) * rows) of every plane (plane_stride >= batch *
+// rows * pitch).
+int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int rank,
+                            const uint64_t *shape, const int32_t *perm, uint64_t rows,
+                            uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                            int scale_exp, cudaStream_t stream);
+
+// C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
+// operand), C packed as batch x m x n.
+int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, uint64_t sa,
+                         uint64_t sb, uint64_t m, uint64_t n, uint64_t k, int dtype,
+                         int scale_exp, cudaStream_t stream);
+
+// Batched TF32x3 product: operand planes laid out [plane][batch][rows][kpitch]
+// when batched (a_batched / b_batched), [plane][rows][kpitch] when shared.
+int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b_planes,
+                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
+                            uint64_t k, uint64_t kpitch, float out_scale, cudaStream_t stream);
+
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,
                   void *workspace, size_t ws_bytes, cudaStream_t stream);

@@ -204,3 +204,156 @@ int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C, ui
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched contraction (the slice batch of the sliced-network executor).
+// ---------------------------------------------------------------------------
+namespace jetgpu {
+namespace {
+
+struct BatchPlan {
+    bool fold;     // A batched, B shared: the batch folds into M
+    bool tc;       // tensor-core form
+    uint64_t ba;   // tensors of A (batch or 1)
+    uint64_t bb;   // tensors of B
+};
+
+BatchPlan PlanBatch(uint64_t batch, int a_batched, int b_batched, uint64_t m, uint64_t n,
+                    uint64_t k, int dtype, int precision)
+{
+    BatchPlan p;
+    p.fold = batch > 1 && a_batched && !b_batched;
+    p.tc = UseTensorCores(p.fold ? batch * m : m, n, k, dtype, precision);
+    p.ba = (batch > 1 && a_batched) ? batch : 1;
+    p.bb = (batch > 1 && b_batched) ? batch : 1;
+    return p;
+}
+
+void FoldShape(int rank, const uint64_t *shape, const int32_t *perm, uint64_t batch,
+               std::vector<uint64_t> &s, std::vector<int32_t> &pm)
+{
+    s.assign(1, batch);
+    s.insert(s.end(), shape, shape + rank);
+    pm.assign(1, 0);
+    for (int j = 0; j < rank; ++j)
+        pm.push_back(perm[j] + 1);
+}
+
+} // namespace
+} // namespace jetgpu
+
+extern "C" {
+
+size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const uint64_t *a_shape,
+                                              const int32_t *a_perm, int a_batched, int b_rank,
+                                              const uint64_t *b_shape, const int32_t *b_perm,
+                                              int b_batched, uint64_t m, uint64_t n, uint64_t k,
+                                              int dtype, int precision)
+{
+    const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
+    if (batch <= 1 || (!a_batched && !b_batched))
+        return jetgpu_contract_workspace_size(a_rank, a_shape, a_perm, b_rank, b_shape, b_perm, m,
+                                              n, k, dtype, precision);
+    if (p.fold) {
+        std::vector<uint64_t> s;
+        std::vector<int32_t> pm;
+        FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
+        return jetgpu_contract_workspace_size(a_rank + 1, s.data(), pm.data(), b_rank, b_shape,
+                                              b_perm, batch * m, n, k, dtype, precision);
+    }
+    if (p.tc) {
+        const uint64_t kp = (k + 3) / 4 * 4;
+        return AlignUp(4 * p.ba * m * kp * sizeof(float)) +
+               AlignUp(4 * p.bb * n * kp * sizeof(float));
+    }
+    const size_t eb = ElemBytes(dtype);
+    size_t ws = 0;
+    if (!IsIdentity(a_rank, a_perm))
+        ws += AlignUp(p.ba * m * k * eb);
+    if (!IsIdentity(b_rank, b_perm))
+        ws += AlignUp(p.bb * k * n * eb);
+    return ws;
+}
+
+int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                            const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                            const uint64_t *b_shape, const int32_t *b_perm, int b_batched,
+                            void *C, uint64_t m, uint64_t n, uint64_t k, int dtype, int precision,
+                            int algo, int scale_a, int scale_b, void *workspace,
+                            size_t workspace_bytes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(batch >= 1, "batch must be at least 1");
+    if (batch == 1 || (!a_batched && !b_batched)) {
+        JETGPU_REQUIRE(batch == 1, "a batch needs at least one batched operand");
+        return jetgpu_contract(A, a_rank, a_shape, a_perm, B, b_rank, b_shape, b_perm, C, m, n, k,
+                               dtype, precision, algo, scale_a, scale_b, workspace,
+                               workspace_bytes, stream);
+    }
+    const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
+    if (p.fold) {
+        std::vector<uint64_t> s;
+        std::vector<int32_t> pm;
+        FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
+        return jetgpu_contract(A, a_rank + 1, s.data(), pm.data(), B, b_rank, b_shape, b_perm, C,
+                               batch * m, n, k, dtype, precision, algo, scale_a, scale_b,
+                               workspace, workspace_bytes, stream);
+    }
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
+    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
+    if (rc)
+        return rc;
+    rc = Validate(b_rank, b_shape, b_perm, k, n, "B");
+    if (rc)
+        return rc;
+    if (m * n == 0)
+        return JETGPU_OK;
+    const size_t need = jetgpu_contract_batched_workspace_size(
+        batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm, b_batched, m, n, k,
+        dtype, precision);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return SetError(JETGPU_ERR_WORKSPACE,
+                        "workspace too small: need " + std::to_string(need) + " bytes");
+    cudaStream_t st = AsStream(stream);
+    uint8_t *ws = static_cast<uint8_t *>(workspace);
+    if (k > 0 && p.tc) {
+        const uint64_t kp = (k + 3) / 4 * 4;
+        float *pa = reinterpret_cast<float *>(ws);
+        float *pb = reinterpret_cast<float *>(ws + AlignUp(4 * p.ba * m * kp * sizeof(float)));
+        const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
+        std::vector<int32_t> bt(b_rank);
+        for (int j = 0; j < b_rank; ++j)
+            bt[j] = b_perm[(j + nc) % b_rank];
+        rc = PermuteSplitTf32Batched(A, pa, p.ba, a_rank, a_shape, a_perm, m, k, kp,
+                                     p.ba * m * kp, scale_a, st);
+        if (rc)
+            return rc;
+        rc = PermuteSplitTf32Batched(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, kp,
+                                     p.bb * n * kp, scale_b, st);
+        if (rc)
+            return rc;
+        return GemmTf32x3PlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, kp, 1.0f,
+                                       st);
+    }
+    const size_t eb = ElemBytes(dtype);
+    const void *at = A;
+    const void *btp = B;
+    if (k > 0 && !IsIdentity(a_rank, a_perm)) {
+        rc = PermuteImpl(A, ws, p.ba, a_rank, a_shape, a_perm, dtype, st);
+        if (rc)
+            return rc;
+        at = ws;
+        ws += AlignUp(p.ba * m * k * eb);
+    }
+    if (k > 0 && !IsIdentity(b_rank, b_perm)) {
+        rc = PermuteImpl(B, ws, p.bb, b_rank, b_shape, b_perm, dtype, st);
+        if (rc)
+            return rc;
+        btp = ws;
+    }
+    return MultiplyPlainBatched(at, btp, C, batch, p.ba > 1 ? m * k : 0, p.bb > 1 ? k * n : 0, m,
+                                n, k, dtype, scale_a + scale_b, st);
+}
+
+} // extern "C"

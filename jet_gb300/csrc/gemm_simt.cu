@@ -41,10 +41,14 @@ __global__ void __launch_bounds__(256)
     gemm_kernel(const typename C2<T>::type *__restrict__ A,
                 const typename C2<T>::type *__restrict__ B,
                 typename C2<T>::type *__restrict__ C, int64_t M, int64_t N,
-                int64_t K, T scale)
+                int64_t K, T scale, int64_t sa, int64_t sb)
 {
     using V = typename C2<T>::type;
     constexpr int TM = GemmCfg<T>::TM;
+    // Batch b = blockIdx.z: operand strides sa, sb (0 = shared), C packed.
+    A += (int64_t)blockIdx.z * sa;
+    B += (int64_t)blockIdx.z * sb;
+    C += (int64_t)blockIdx.z * M * N;
     constexpr int BM = TM * kTY;
     constexpr int BN = kTN * kTX;
     constexpr int A_PER = BM * kBK / 256; // A elements loaded per thread
@@ -239,6 +243,62 @@ __global__ void __launch_bounds__(256)
     out[s * N + n] = V{sr.s * scale, si.s * scale};
 }
 
+// Batched vector products: row r of batch b (n == 1) or column c of batch b
+// (m == 1); operand strides sa, sb (0 = shared).
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemv_rows_batched(const typename C2<T>::type *__restrict__ A,
+                      const typename C2<T>::type *__restrict__ x,
+                      typename C2<T>::type *__restrict__ out, int64_t batch, int64_t M,
+                      int64_t K, int64_t sa, int64_t sb, T scale)
+{
+    using V = typename C2<T>::type;
+    const int lane = threadIdx.x & 31;
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= batch * M)
+        return;
+    const int64_t b = row / M, m = row - b * M;
+    const V *a = A + b * sa + m * K;
+    const V *v = x + b * sb;
+    KahanSum<T> sr, si;
+    for (int64_t k = lane; k < K; k += 32) {
+        V p = a[k], q = v[k];
+        sr.add(fma(p.x, q.x, -p.y * q.y));
+        si.add(fma(p.x, q.y, p.y * q.x));
+    }
+    T re = sr.s, im = si.s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0)
+        out[row] = V{re * scale, im * scale};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemv_cols_batched(const typename C2<T>::type *__restrict__ x,
+                      const typename C2<T>::type *__restrict__ B,
+                      typename C2<T>::type *__restrict__ out, int64_t batch, int64_t N,
+                      int64_t K, int64_t sa, int64_t sb, T scale)
+{
+    using V = typename C2<T>::type;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= batch * N)
+        return;
+    const int64_t b = idx / N, n = idx - b * N;
+    const V *v = x + b * sa;
+    const V *bb = B + b * sb + n;
+    KahanSum<T> sr, si;
+    for (int64_t k = 0; k < K; ++k) {
+        V p = v[k], q = bb[k * N];
+        sr.add(fma(p.x, q.x, -p.y * q.y));
+        si.add(fma(p.x, q.y, p.y * q.x));
+    }
+    out[idx] = V{sr.s * scale, si.s * scale};
+}
+
 template <typename T>
 __global__ void reduce_partials(const typename C2<T>::type *__restrict__ part,
                                 typename C2<T>::type *__restrict__ out,
@@ -314,7 +374,7 @@ int MultiplyT(const void *Av, const void *Bv, void *Cv, int64_t M, int64_t N,
         constexpr int BN = kTN * kTX;
         dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
         JETGPU_REQUIRE(grid.y <= 65535u, "m too large for one launch");
-        gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale);
+        gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, 0, 0);
         return CheckLaunch("gemm_kernel");
     }
     // Split over k only when the caller supplied room for the partial sums.
@@ -349,7 +409,55 @@ int MultiplyT(const void *Av, const void *Bv, void *Cv, int64_t M, int64_t N,
     return CheckLaunch("reduce_partials");
 }
 
+template <typename T>
+int MultiplyBatchedT(const void *Av, const void *Bv, void *Cv, int64_t batch, int64_t sa,
+                     int64_t sb, int64_t M, int64_t N, int64_t K, int scale_exp,
+                     cudaStream_t stream)
+{
+    using V = typename C2<T>::type;
+    const V *A = (const V *)Av;
+    const V *B = (const V *)Bv;
+    V *C = (V *)Cv;
+    const T scale = (T)ldexp(1.0, scale_exp);
+    if (M == 0 || N == 0 || batch == 0)
+        return JETGPU_OK;
+    if (K == 0) {
+        fill_zero<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(C, batch * M * N);
+        return CheckLaunch("fill_zero");
+    }
+    if (M > 1 && N > 1) {
+        constexpr int BM = GemmCfg<T>::TM * kTY;
+        constexpr int BN = kTN * kTX;
+        dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
+        JETGPU_REQUIRE(grid.y <= 65535u && grid.z <= 65535u, "batched product too large");
+        gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, sa, sb);
+        return CheckLaunch("gemm_kernel (batched)");
+    }
+    if (N == 1) {
+        const int64_t rows = batch * M;
+        gemv_rows_batched<T><<<(unsigned)((rows + 7) / 8), 256, 0, stream>>>(A, B, C, batch, M, K,
+                                                                            sa, sb, scale);
+        return CheckLaunch("gemv_rows_batched");
+    }
+    const int64_t cols = batch * N;
+    gemv_cols_batched<T><<<(unsigned)((cols + 255) / 256), 256, 0, stream>>>(A, B, C, batch, N,
+                                                                            K, sa, sb, scale);
+    return CheckLaunch("gemv_cols_batched");
+}
+
 } // namespace
+
+int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, uint64_t sa,
+                         uint64_t sb, uint64_t m, uint64_t n, uint64_t k, int dtype,
+                         int scale_exp, cudaStream_t stream)
+{
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    if (dtype == JETGPU_C128)
+        return MultiplyBatchedT<double>(A, B, C, (int64_t)batch, (int64_t)sa, (int64_t)sb,
+                                        (int64_t)m, (int64_t)n, (int64_t)k, scale_exp, stream);
+    return MultiplyBatchedT<float>(A, B, C, (int64_t)batch, (int64_t)sa, (int64_t)sb, (int64_t)m,
+                                   (int64_t)n, (int64_t)k, scale_exp, stream);
+}
 
 size_t MultiplyPlainWorkspace(uint64_t m, uint64_t n, uint64_t k, int dtype)
 {

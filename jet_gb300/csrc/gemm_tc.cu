@@ -107,6 +107,16 @@ __device__ __forceinline__ void TmaLoad3d(uint32_t dst, const CUtensorMap *map,
                  : "memory");
 }
 
+__device__ __forceinline__ void TmaLoad4d(uint32_t dst, const CUtensorMap *map,
+                                          int c0, int c1, int c2, int c3, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::"
+                 "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+                 "r"(bar)
+                 : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major operand, 64-byte swizzle, 8-row
 // groups 512 bytes apart.
 __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
@@ -187,8 +197,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles,
-                          float scale)
+                          float scale, int a_batched, int b_batched)
 {
+    // Batch b = blockIdx.z: a batched operand is read through a 4-D map
+    // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
+    const int bz = blockIdx.z;
+    C += (size_t)bz * M * N;
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
@@ -241,8 +255,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int k0 = kt * kBK;
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
-                    TmaLoad3d(base + p * kTileBytes, &tmA, k0, m0, p, fb);
-                    TmaLoad3d(base + (4 + p) * kTileBytes, &tmB, k0, n0, p, fb);
+                    if (a_batched)
+                        TmaLoad4d(base + p * kTileBytes, &tmA, k0, m0, bz, p, fb);
+                    else
+                        TmaLoad3d(base + p * kTileBytes, &tmA, k0, m0, p, fb);
+                    if (b_batched)
+                        TmaLoad4d(base + (4 + p) * kTileBytes, &tmB, k0, n0, bz, p, fb);
+                    else
+                        TmaLoad3d(base + (4 + p) * kTileBytes, &tmB, k0, n0, p, fb);
                 }
             }
         }
@@ -416,12 +436,45 @@ int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
     return JETGPU_OK;
 }
 
+// 4-D map over batched planes laid out [plane][batch][rows][kpitch]:
+// (k, row, batch, plane), box 16 x 128 x 1 x 1.
+int EncodePlanesBatched(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
+                        uint64_t kpitch, uint64_t batch)
+{
+    cuuint64_t dims[4] = {k, rows, batch, 4};
+    cuuint64_t strides[3] = {kpitch * 4, rows * kpitch * 4, batch * rows * kpitch * 4};
+    cuuint32_t box[4] = {kBK, kBM, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                          const_cast<float *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return SetError(JETGPU_ERR_CUDA,
+                        "cuTensorMapEncodeTiled (4-D) failed: " + std::to_string((int)r));
+    return JETGPU_OK;
+}
+
 } // namespace
 
 int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
                      uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                      float out_scale, cudaStream_t stream)
 {
+    return GemmTf32x3PlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
+                                   stream);
+}
+
+int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b_planes,
+                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
+                            uint64_t k, uint64_t kpitch, float out_scale, cudaStream_t stream)
+{
+    JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
+    if (batch == 1) {
+        a_batched = 0;
+        b_batched = 0;
+    }
     JETGPU_REQUIRE(m > 0 && n > 0 && k > 0, "empty product");
     JETGPU_REQUIRE(m < (1ull << 31) && n < (1ull << 31) && k < (1ull << 31),
                    "dimension too large");
@@ -436,9 +489,11 @@ int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
     if (rc)
         return rc;
     CUtensorMap ta, tb;
-    if ((rc = EncodePlanes(&ta, a_planes, m, k, kpitch)))
+    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch)
+                        : EncodePlanes(&ta, a_planes, m, k, kpitch)))
         return rc;
-    if ((rc = EncodePlanes(&tb, b_planes, n, k, kpitch)))
+    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch)
+                        : EncodePlanes(&tb, b_planes, n, k, kpitch)))
         return rc;
     const size_t smem = (size_t)kStages * kStageBytes + 1024;
     static thread_local int configured_dev = -1;
@@ -449,10 +504,12 @@ int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
             tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured_dev = dev;
     }
-    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM));
+    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM),
+              (unsigned)batch);
     const int ktiles = (int)((k + kBK - 1) / kBK);
     tc_gemm_tf32x3_kernel<<<grid, kThreads, smem, stream>>>(
-        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale);
+        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
+        b_batched);
     return CheckLaunch("tc_gemm_tf32x3_kernel");
 }
 

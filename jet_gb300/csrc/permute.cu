@@ -169,8 +169,9 @@ __global__ void __launch_bounds__(kThreads)
 {
     for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
          idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t o = idx;
-        uint64_t src = 0;
+        const uint64_t b = idx / p.size;
+        uint64_t o = idx - b * p.size;
+        uint64_t src = b * p.size;
         for (int j = p.rank - 1; j >= 0; --j) {
             uint64_t d = p.out_dims[j];
             uint64_t q = o / d;
@@ -511,11 +512,24 @@ int PermuteSplitTf32(const void *in, float *planes, int rank,
                      uint64_t cols, uint64_t pitch, uint64_t plane_stride,
                      int scale_exp, cudaStream_t stream)
 {
+    return PermuteSplitTf32Batched(in, planes, 1, rank, shape, perm, rows, cols, pitch,
+                                   plane_stride, scale_exp, stream);
+}
+
+int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int rank,
+                            const uint64_t *shape, const int32_t *perm, uint64_t rows,
+                            uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                            int scale_exp, cudaStream_t stream)
+{
     Simplified s;
     int rc = Simplify(rank, shape, perm, s);
     if (rc)
         return rc;
     JETGPU_REQUIRE(rows * cols == s.size, "split view does not match size");
+    JETGPU_REQUIRE(batch >= 1, "empty batch");
+    // Tensor b occupies rows [b * rows, (b + 1) * rows): the batch folds into
+    // the row index of the split view.
+    rows *= batch;
     JETGPU_REQUIRE(scale_exp >= -126 && scale_exp <= 127, "scale out of range");
     SplitOut so;
     so.planes = planes;
@@ -526,10 +540,10 @@ int PermuteSplitTf32(const void *in, float *planes, int rank,
     const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
                          (pitch % 2 == 0) && (plane_stride % 2 == 0);
     static thread_local BitParams bp;
-    if (aligned && IsPow2(cols) && cols >= 2 && BuildBitParams(s, 1, 1, bp))
+    if (aligned && IsPow2(cols) && cols >= 2 && BuildBitParams(s, batch, 1, bp))
         return LaunchBitperm<uint2, 1>(bp, in, SplitStore{so}, stream);
     GatherParams gp;
-    BuildGather(s, 1, gp);
+    BuildGather(s, batch, gp);
     unsigned grid = GridFor((gp.total + kThreads - 1) / kThreads, 8);
     gather_split_kernel<<<grid, kThreads, 0, stream>>>(gp, (const float2 *)in,
                                                        so);

@@ -100,13 +100,17 @@ struct SliceParams {
 
 template <typename E>
 __global__ void slice_gather_kernel(const __grid_constant__ SliceParams p,
-                                    const E *__restrict__ in, E *__restrict__ out)
+                                    const E *__restrict__ in, E *__restrict__ out,
+                                    const uint64_t *__restrict__ first_dev)
 {
+    // The first slice value comes from the parameters or, for launches that a
+    // captured graph replays over successive chunks, from device memory.
+    const uint64_t first = first_dev ? *first_dev : p.first_value;
     for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
          idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t s = idx / p.out_size;
         uint64_t o = idx - s * p.out_size;
-        const uint64_t v = p.first_value + s;
+        const uint64_t v = first + s;
         uint64_t src = 0;
         for (int j = 0; j < p.n_axes; ++j)
             src += ((v / p.value_stride[j]) % p.fixed_dim[j]) * p.fixed_stride[j];
@@ -121,6 +125,8 @@ __global__ void slice_gather_kernel(const __grid_constant__ SliceParams p,
 }
 
 __global__ void init_exp_kernel(int *e) { *e = -1000; }
+
+__global__ void counter_add_kernel(uint64_t *c, uint64_t delta) { *c += delta; }
 
 template <typename V, typename U>
 __global__ void max_exp_kernel(const V *__restrict__ x, uint64_t n, int *e)
@@ -238,10 +244,42 @@ int jetgpu_slice_sum_f64(const void *results, uint64_t n_slices, uint64_t size,
     return CheckLaunch("slice_sum");
 }
 
+static int SliceGatherImpl(const void *in, int rank, const uint64_t *shape, int n_axes,
+                           const int32_t *axes, const uint64_t *value_strides,
+                           uint64_t first_value, const uint64_t *first_dev, uint64_t n_values,
+                           void *out, int dtype, void *stream);
+
 int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
                         int n_axes, const int32_t *axes,
                         const uint64_t *value_strides, uint64_t first_value,
                         uint64_t n_values, void *out, int dtype, void *stream)
+{
+    return SliceGatherImpl(in, rank, shape, n_axes, axes, value_strides, first_value, nullptr,
+                           n_values, out, dtype, stream);
+}
+
+int jetgpu_slice_gather_at(const void *in, int rank, const uint64_t *shape, int n_axes,
+                           const int32_t *axes, const uint64_t *value_strides,
+                           const uint64_t *first_value_dev, uint64_t n_values, void *out,
+                           int dtype, void *stream)
+{
+    JETGPU_REQUIRE(first_value_dev != nullptr, "null first-value pointer");
+    return SliceGatherImpl(in, rank, shape, n_axes, axes, value_strides, 0, first_value_dev,
+                           n_values, out, dtype, stream);
+}
+
+int jetgpu_counter_add(uint64_t *counter_dev, uint64_t delta, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(counter_dev != nullptr, "null counter");
+    counter_add_kernel<<<1, 1, 0, AsStream(stream)>>>(counter_dev, delta);
+    return CheckLaunch("counter_add_kernel");
+}
+
+static int SliceGatherImpl(const void *in, int rank, const uint64_t *shape, int n_axes,
+                           const int32_t *axes, const uint64_t *value_strides,
+                           uint64_t first_value, const uint64_t *first_dev, uint64_t n_values,
+                           void *out, int dtype, void *stream)
 {
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
@@ -279,10 +317,10 @@ int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
     unsigned grid = GridFor((p.total + kThreads - 1) / kThreads, 8);
     if (dtype == JETGPU_C64)
         slice_gather_kernel<uint2><<<grid, kThreads, 0, AsStream(stream)>>>(
-            p, (const uint2 *)in, (uint2 *)out);
+            p, (const uint2 *)in, (uint2 *)out, first_dev);
     else
         slice_gather_kernel<uint4><<<grid, kThreads, 0, AsStream(stream)>>>(
-            p, (const uint4 *)in, (uint4 *)out);
+            p, (const uint4 *)in, (uint4 *)out, first_dev);
     return CheckLaunch("slice_gather_kernel");
 }
 

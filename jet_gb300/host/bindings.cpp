@@ -177,6 +177,34 @@ template <class T> void BindContractor(py::module_ &m)
              });
 }
 
+template <class T> void BindSliced(py::module_ &m)
+{
+    using sc_t = Jet::SlicedContractor<T>;
+    using tn_t = Jet::TensorNetwork<Jet::Tensor<T>>;
+    py::class_<sc_t>(m, ("SlicedContractor" + Suffix<T>()).c_str(),
+                     "All slices of a sliced network along one path, batched on the GPU.")
+        .def(py::init<const tn_t &, const Jet::PathInfo::Path &, const std::vector<std::string> &,
+                      int>(),
+             py::arg("tn"), py::arg("path"), py::arg("sliced_indices"), py::arg("precision") = 0)
+        .def("set_batch_size", &sc_t::SetBatchSize, py::arg("slices_per_batch"))
+        .def("set_leaf_alternatives", &sc_t::SetLeafAlternatives, py::arg("node_id"),
+             py::arg("values"), py::arg("count"))
+        .def("contract",
+             [](sc_t &s, size_t first, py::object count) {
+                 const size_t c = count.is_none() ? SIZE_MAX : count.cast<size_t>();
+                 py::gil_scoped_release release;
+                 return s.Contract(first, c);
+             },
+             py::arg("first") = 0, py::arg("count") = py::none())
+        .def_property_readonly("batch_size", &sc_t::GetBatchSize)
+        .def_property_readonly("num_slices", &sc_t::GetNumSlices)
+        .def_property_readonly("result_indices", &sc_t::GetResultIndices)
+        .def_property_readonly("result_shape", &sc_t::GetResultShape)
+        .def_property_readonly("slice_flops", &sc_t::GetSliceFlops)
+        .def_property_readonly("slice_dependent_flops", &sc_t::GetSliceDependentFlops)
+        .def_property_readonly("arena_bytes", &sc_t::GetArenaBytes);
+}
+
 template <class T> void BindPathInfoCtor(py::class_<Jet::PathInfo> &c)
 {
     c.def(py::init<const Jet::TensorNetwork<Jet::Tensor<T>> &, const Jet::PathInfo::Path &>(),
@@ -217,6 +245,8 @@ PYBIND11_MODULE(_jet_bindings, m)
     BindPathInfoCtor<std::complex<double>>(pi);
     BindContractor<std::complex<float>>(m);
     BindContractor<std::complex<double>>(m);
+    BindSliced<std::complex<float>>(m);
+    BindSliced<std::complex<double>>(m);
     m.def("version", [] { return std::string("0.2.3-gb300"); });
     m.def("set_precision", &Jet::Gpu::SetPrecision, py::arg("precision"),
           "ContractTensors arithmetic for complex64: 0 plain FP32, 1 TF32x3, 2 auto.");

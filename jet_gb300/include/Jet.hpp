@@ -3,6 +3,7 @@
 
 #include "jet/Abort.hpp"
 #include "jet/PathInfo.hpp"
+#include "jet/SlicedContractor.hpp"
 #include "jet/TaskBasedContractor.hpp"
 #include "jet/Tensor.hpp"
 #include "jet/TensorNetwork.hpp"

@@ -176,10 +176,13 @@ def test_sliced_networks_share_tasks_and_reduce(jet):
     assert abs(got - want) <= 1e-5 * abs(want)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 2])
 def test_config0_amplitude(jet, precision):
     """4x4 grid, 8 cycles: TensorNetwork::Contract(path) on the GPU against the
-    complex128 oracle and the reference's own CPU result (golden)."""
+    complex128 oracle and the reference's own CPU result (golden). Whole
+    networks use plain FP32 or AUTO (TF32x3 on the large steps only): forcing
+    TF32x3 onto ~200 steps of 2x2 gates compounds its ~2^-22 per-product
+    rounding past 1e-5."""
     import json
     import os
 
