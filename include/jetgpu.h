@@ -189,6 +189,35 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank,
                             size_t workspace_bytes, void *stream);
 
 /*
+ * jetgpu_contract without a workspace argument and without allocating: for
+ * callers that cannot allocate device memory when they contract -- inside a
+ * CUDA stream capture, where cudaMalloc is illegal; under a host's own fixed
+ * GPU memory budget (JNI/cgo services, embedded runtimes); in latency-bound
+ * loops where cudaMalloc/cudaFree would synchronise the device. This entry
+ * point has no counterpart in the reference.
+ *
+ * Scratch comes from one 32 MiB device array inside the library (every GPU
+ * that loads the library holds it until the process exits); a contraction
+ * whose jetgpu_contract_workspace_size exceeds
+ * jetgpu_contract_noalloc_max_scratch() is rejected with
+ * JETGPU_ERR_WORKSPACE. The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture. All calls share the one array: calls
+ * whose executions overlap on the GPU (different streams, or concurrent
+ * graphs) race on it and must be serialised by the caller. Arguments and
+ * results are those of jetgpu_contract.
+ */
+int jetgpu_contract_noalloc(const void *A, int a_rank, const uint64_t *a_shape,
+                            const int32_t *a_perm, const void *B, int b_rank,
+                            const uint64_t *b_shape, const int32_t *b_perm, void *C,
+                            uint64_t m, uint64_t n, uint64_t k, int dtype,
+                            int precision, int algo, int scale_a, int scale_b,
+                            void *stream);
+
+/* Bytes of scratch jetgpu_contract_noalloc can use (its size limit). */
+size_t jetgpu_contract_noalloc_max_scratch(void);
+
+/*
  * The two stages of the TF32x3 form of jetgpu_contract, for callers that
  * schedule them separately (batched executors, profilers).
  *
