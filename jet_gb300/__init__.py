@@ -28,6 +28,7 @@ from ._jet_bindings import (  # noqa: F401
     version,
 )
 from .factory import *  # noqa: F401,F403
+from .io import TensorFileException, TensorNetworkFile, TensorNetworkSerializer  # noqa: F401
 
 PREC_FP32 = 0
 PREC_TF32X3 = 1

@@ -1,0 +1,181 @@
+"""Differentiable network contraction with a hand-written adjoint.
+
+`contract_network(leaves, labels, path)` contracts a tensor network on the
+GPU along `path` (the reference's node-id convention, TensorNetwork.hpp:
+301-328) and returns the result as a torch tensor that carries gradients back
+to every leaf.
+
+Each pairwise step is the reference's Tensor::ContractTensors
+(Tensor.hpp:708-752): labels left = A\\B, right = B\\A, common = A∩B (A
+order), C[left ++ right] = sum_common A B. Its adjoint is two conjugate
+contractions, replayed along the path in reverse:
+
+    grad_A[left, common] = sum_right grad_C[left, right] conj(B[common, right])
+    grad_B[common, right] = sum_left conj(A[left, common]) grad_C[left, right]
+
+(PyTorch's convention for complex gradients: grad = dL/d(conj z)), each
+followed by a transpose back to the operand's own label order. The forward
+keeps only the leaves: backward recomputes the intermediates (checkpointing),
+so memory stays at one forward's worth plus the gradients. Every contraction,
+conjugation and transpose runs in libjetgpu.so (jetgpu_contract,
+jetgpu_conj, jetgpu_permute).
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Sequence, Tuple
+
+import torch
+
+from . import capi
+
+
+@dataclasses.dataclass
+class _Step:
+    a: int
+    b: int
+    out_labels: List[str]
+    a_perm: List[int]
+    b_perm: List[int]
+    m: int
+    n: int
+    k: int
+
+
+class ContractionPlan:
+    """Label bookkeeping of a path: per step, the operand orders and the
+    product dimensions ContractTensors derives (left, right, common)."""
+
+    def __init__(self, labels: Sequence[Sequence[str]], shapes: Sequence[Sequence[int]],
+                 path: Sequence[Tuple[int, int]]):
+        self.labels: List[List[str]] = [list(l) for l in labels]
+        self.shapes: List[List[int]] = [list(s) for s in shapes]
+        self.num_leaves = len(self.labels)
+        self.dims = {}
+        for lab, sh in zip(self.labels, self.shapes):
+            for x, d in zip(lab, sh):
+                self.dims[x] = int(d)
+        self.steps: List[_Step] = []
+        for a, b in path:
+            la, lb = self.labels[a], self.labels[b]
+            sb, sa = set(lb), set(la)
+            left = [x for x in la if x not in sb]
+            right = [x for x in lb if x not in sa]
+            common = [x for x in la if x in sb]
+            step = _Step(a, b, left + right, [la.index(x) for x in left + common],
+                         [lb.index(x) for x in common + right], self._prod(left),
+                         self._prod(right), self._prod(common))
+            self.steps.append(step)
+            self.labels.append(step.out_labels)
+            self.shapes.append([self.dims[x] for x in step.out_labels])
+
+    def _prod(self, labels) -> int:
+        p = 1
+        for x in labels:
+            p *= self.dims[x]
+        return p
+
+    @property
+    def out_labels(self) -> List[str]:
+        return self.labels[-1]
+
+    @property
+    def out_shape(self) -> List[int]:
+        return self.shapes[-1]
+
+
+def _contract(a, a_labels, a_shape, b, b_labels, b_shape, precision):
+    """ContractTensors on device tensors; returns (C, C labels)."""
+    sb, sa = set(b_labels), set(a_labels)
+    left = [x for x in a_labels if x not in sb]
+    right = [x for x in b_labels if x not in sa]
+    common = [x for x in a_labels if x in sb]
+    dims = dict(zip(a_labels, a_shape))
+    dims.update(zip(b_labels, b_shape))
+    m = n = k = 1
+    for x in left:
+        m *= dims[x]
+    for x in right:
+        n *= dims[x]
+    for x in common:
+        k *= dims[x]
+    out = capi.contract(a, list(a_shape), [a_labels.index(x) for x in left + common], b,
+                        list(b_shape), [b_labels.index(x) for x in common + right], m, n, k,
+                        precision=precision)
+    return out[: m * n], left + right, [dims[x] for x in left + right]
+
+
+def _to_order(x, labels, shape, target):
+    if labels == target:
+        return x
+    return capi.permute(x, list(shape), [labels.index(t) for t in target])
+
+
+def _forward(plan: ContractionPlan, leaves, precision: int, keep: bool):
+    vals = list(leaves)
+    for st in plan.steps:
+        out = capi.contract(vals[st.a], plan.shapes[st.a], st.a_perm, vals[st.b],
+                            plan.shapes[st.b], st.b_perm, st.m, st.n, st.k,
+                            precision=precision)[: st.m * st.n]
+        vals.append(out)
+        if not keep:
+            # Release operands that are intermediates (each is used once).
+            for i in (st.a, st.b):
+                if i >= plan.num_leaves:
+                    vals[i] = None
+    return vals
+
+
+def _backward(plan: ContractionPlan, vals, grad_out, precision: int):
+    grads = [None] * len(vals)
+    grads[-1] = grad_out
+    for idx in range(len(plan.steps) - 1, -1, -1):
+        st = plan.steps[idx]
+        c_id = plan.num_leaves + idx
+        gc = grads[c_id]
+        if gc is None:
+            continue
+        la, lb, lc = plan.labels[st.a], plan.labels[st.b], plan.labels[c_id]
+        sa, sb, sc = plan.shapes[st.a], plan.shapes[st.b], plan.shapes[c_id]
+        # grad_A = contract(grad_C, conj(B)) -> transpose to A's labels.
+        ga, lga, sga = _contract(gc, lc, sc, capi.conj(vals[st.b]), lb, sb, precision)
+        ga = _to_order(ga, lga, sga, la)
+        # grad_B = contract(conj(A), grad_C) -> transpose to B's labels.
+        gb, lgb, sgb = _contract(capi.conj(vals[st.a]), la, sa, gc, lc, sc, precision)
+        gb = _to_order(gb, lgb, sgb, lb)
+        grads[st.a] = ga if grads[st.a] is None else capi.add(grads[st.a], ga)
+        grads[st.b] = gb if grads[st.b] is None else capi.add(grads[st.b], gb)
+        grads[c_id] = None
+        vals[c_id] = None
+    return grads[: plan.num_leaves]
+
+
+class _NetworkContraction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan: ContractionPlan, precision: int, *leaves):
+        flat = [l.contiguous().reshape(-1) for l in leaves]
+        vals = _forward(plan, flat, precision, keep=False)
+        ctx.plan = plan
+        ctx.precision = precision
+        ctx.leaf_shapes = [tuple(l.shape) for l in leaves]
+        ctx.save_for_backward(*leaves)
+        return vals[-1].reshape(plan.out_shape)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        leaves = [l.contiguous().reshape(-1) for l in ctx.saved_tensors]
+        vals = _forward(ctx.plan, leaves, ctx.precision, keep=True)
+        g = grad_out.contiguous().reshape(-1).to(vals[-1].dtype)
+        grads = _backward(ctx.plan, vals, g, ctx.precision)
+        out = [None if gr is None else gr.reshape(s) for gr, s in zip(grads, ctx.leaf_shapes)]
+        return (None, None, *out)
+
+
+def contract_network(leaves: Sequence[torch.Tensor], labels: Sequence[Sequence[str]],
+                     path: Sequence[Tuple[int, int]], precision: int = capi.PREC_AUTO,
+                     plan: ContractionPlan = None) -> torch.Tensor:
+    """Contracts CUDA complex tensors `leaves` (labels[i] per leaf) along
+    `path`; differentiable with respect to every leaf."""
+    if plan is None:
+        plan = ContractionPlan(labels, [list(l.shape) for l in leaves], path)
+    return _NetworkContraction.apply(plan, precision, *leaves)

@@ -329,23 +329,47 @@ def path_cost(net: Network, path: Sequence[Tuple[int, int]], sliced: Sequence[st
     return flops, math.log2(max(biggest, 1.0))
 
 
+def _largest_intermediates(net: Network, path, sliced, top: int = 4):
+    """Label sets of the `top` largest intermediates of the path."""
+    dims = dict(net.index_dims())
+    for x in sliced:
+        dims[x] = 1
+    open_set = set(net.open_labels)
+    nodes = {i: list(l) for i, (l, _, _) in enumerate(net.tensors)}
+    nid = len(nodes)
+    sizes = []
+    for a, b in path:
+        la, lb = nodes.pop(a), nodes.pop(b)
+        sa, sb = set(la), set(lb)
+        out = [x for x in la if x not in sb or x in open_set] + [x for x in lb if x not in sa]
+        sizes.append((_size(out, dims), out))
+        nodes[nid] = out
+        nid += 1
+    sizes.sort(key=lambda t: -t[0])
+    return [lab for _, lab in sizes[:top]]
+
+
 def choose_slices(net: Network, path: Sequence[Tuple[int, int]], count: int,
                   seed: int = 0) -> List[str]:
     """Greedy slicer: `count` times, slice the bond that most reduces
-    (largest intermediate, total flops); seeded tie-break. Open and
+    (largest intermediate, total flops); seeded tie-break. Only bonds of the
+    largest intermediates can shrink the largest intermediate, so the
+    candidates are the labels of the few largest ones. Open and
     already-sliced indices are excluded."""
     rng = np.random.default_rng(seed)
     dims = net.index_dims()
     open_set = set(net.open_labels)
-    candidates = sorted(x for x, d in dims.items() if d > 1 and x not in open_set)
     chosen: List[str] = []
     for _ in range(count):
-        best = None
-        order = list(candidates)
+        cands = set()
+        for lab in _largest_intermediates(net, path, chosen):
+            cands.update(x for x in lab if dims[x] > 1 and x not in open_set and x not in chosen)
+        if not cands:
+            cands = {x for x, d in dims.items() if d > 1 and x not in open_set and x not in chosen}
+        order = sorted(cands)
         rng.shuffle(order)
+        best = None
         for x in order:
-            if x in chosen:
-                continue
             flops, big = path_cost(net, path, chosen + [x])
             key = (big, flops)
             if best is None or key < best[0]:

@@ -1,0 +1,142 @@
+"""Expectation values of parameterised circuits as doubled (bra-ket)
+networks, with light-cone pruning, for gradient computations.
+
+Circuit: a rows x cols grid, `layers` layers; each layer applies RX(theta)
+then RZ(phi) on every qubit, then CZ on one of four alternating
+nearest-neighbour coupler patterns (A B C D ... as in circuits.couplers).
+Observable: Z_i Z_j. The network of <psi| Z_i Z_j |psi> keeps only the gates
+in the backward light cone of {i, j}: a gate later than the moment its
+qubits enter the cone cancels against its conjugate (U^dagger U = 1), so the
+ket and bra wires of such a qubit are joined directly.
+
+Leaves are described symbolically (`Leaf`), so that `build_leaves` can
+create them from angle tensors that require gradients: the gates are torch
+functions of the angles and the bra gates their conjugates, and
+jet_gb300.autograd.contract_network carries the gradient from the contracted
+value back to every angle.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from . import circuits
+
+
+@dataclasses.dataclass
+class Leaf:
+    labels: List[str]
+    shape: List[int]
+    kind: str  # "const", "rx", "rz"
+    layer: int = -1
+    qubit: int = -1
+    conj: bool = False
+    data: np.ndarray = None
+
+
+def zz_network(rows: int, cols: int, layers: int, pair: Tuple[int, int],
+               lightcone: bool = True) -> List[Leaf]:
+    n = rows * cols
+    pats = circuits.couplers(rows, cols)
+    # Backward light cone: the set of qubits whose gates matter at each layer.
+    keep_cz = [[] for _ in range(layers)]
+    keep_1q = [set() for _ in range(layers)]
+    cone = set(pair)
+    for layer in reversed(range(layers)):
+        for a, b in pats["ABCD"[layer % 4]]:
+            if not lightcone or a in cone or b in cone:
+                keep_cz[layer].append((a, b))
+        for a, b in keep_cz[layer]:
+            cone |= {a, b}
+        keep_1q[layer] = set(range(n)) if not lightcone else set(cone)
+    active = set(range(n)) if not lightcone else cone
+    ver = {q: 0 for q in range(n)}
+    leaves: List[Leaf] = []
+    ket = lambda q: "k%d_%d" % (q, ver[q])  # noqa: E731
+    bra = lambda q: "b%d_%d" % (q, ver[q])  # noqa: E731
+    zero = np.array([1, 0], dtype=np.complex128)
+    for q in sorted(active):
+        leaves.append(Leaf([ket(q)], [2], "const", data=zero))
+        leaves.append(Leaf([bra(q)], [2], "const", data=zero))
+    cz = circuits.gate_cz().reshape(-1)
+    for layer in range(layers):
+        for kind in ("rx", "rz"):
+            for q in sorted(keep_1q[layer]):
+                ki, bi = ket(q), bra(q)
+                ver[q] += 1
+                leaves.append(Leaf([ket(q), ki], [2, 2], kind, layer, q, False))
+                leaves.append(Leaf([bra(q), bi], [2, 2], kind, layer, q, True))
+        for a, b in keep_cz[layer]:
+            ka, kb, ba, bb = ket(a), ket(b), bra(a), bra(b)
+            ver[a] += 1
+            ver[b] += 1
+            leaves.append(Leaf([ket(a), ket(b), ka, kb], [2, 2, 2, 2], "const", data=cz))
+            leaves.append(Leaf([bra(a), bra(b), ba, bb], [2, 2, 2, 2], "const", data=cz.conj()))
+    # Close the wires: Z on the pair, identity (shared label) elsewhere.
+    zmat = np.diag([1.0, -1.0]).astype(np.complex128).reshape(-1)
+    rename = {}
+    for q in sorted(active):
+        if q in pair:
+            leaves.append(Leaf([bra(q), ket(q)], [2, 2], "const", data=zmat))
+        else:
+            rename[bra(q)] = ket(q)
+    for lf in leaves:
+        lf.labels = [rename.get(x, x) for x in lf.labels]
+    return leaves
+
+
+def numeric_network(leaves: Sequence[Leaf], thetas: np.ndarray, phis: np.ndarray,
+                    dtype=np.complex128) -> circuits.Network:
+    """The network with every gate evaluated at the given angles (numpy)."""
+    out = []
+    for lf in leaves:
+        if lf.kind == "const":
+            d = lf.data
+        elif lf.kind == "rx":
+            d = circuits.gate_rx(thetas[lf.layer, lf.qubit]).reshape(-1)
+        else:
+            d = circuits.gate_rz(phis[lf.layer, lf.qubit]).reshape(-1)
+        if lf.conj and lf.kind != "const":
+            d = np.conj(d)
+        out.append((list(lf.labels), list(lf.shape), np.asarray(d, dtype=dtype)))
+    return circuits.Network(out)
+
+
+def build_leaves(leaves: Sequence[Leaf], thetas, phis, dtype=None, device=None):
+    """torch leaves as differentiable functions of the angle tensors."""
+    import torch
+
+    dtype = dtype or torch.complex64
+    real = torch.float32 if dtype == torch.complex64 else torch.float64
+    out = []
+    for lf in leaves:
+        if lf.kind == "const":
+            t = torch.as_tensor(lf.data, dtype=dtype, device=device).reshape(lf.shape)
+        else:
+            ang = (thetas if lf.kind == "rx" else phis)[lf.layer, lf.qubit].to(real)
+            c, s = torch.cos(ang / 2), torch.sin(ang / 2)
+            z = torch.zeros_like(c)
+            if lf.kind == "rx":
+                re = torch.stack([c, z, z, c])
+                im = torch.stack([z, -s, -s, z])
+            else:
+                re = torch.stack([c, z, z, c])
+                im = torch.stack([-s, z, z, s])
+            t = torch.complex(re, im).to(dtype).reshape(2, 2)
+            if device is not None:
+                t = t.to(device)
+            if lf.conj:
+                t = torch.conj(t).resolve_conj()
+        out.append(t)
+    return out
+
+
+def default_pair(rows: int, cols: int, seed: int = 0) -> Tuple[int, int]:
+    """A seeded horizontal nearest-neighbour pair."""
+    rng = np.random.default_rng(seed)
+    r = int(rng.integers(rows))
+    c = int(rng.integers(cols - 1))
+    return (r * cols + c, r * cols + c + 1)

@@ -213,6 +213,7 @@ template <class T = std::complex<float>> class SlicedContractor {
     double slice_flops_ = 0, slice_dep_flops_ = 0;
     size_t arena_bytes_ = 0, ws_bytes_ = 0, tmp_bytes_ = 0;
     bool planned_ = false;
+    bool prefix_done_ = false;
     Gpu::DeviceBuffer arena_, ws_, tmp_a_, tmp_b_, acc_, counter_, final_tmp_;
     std::vector<Gpu::DeviceBuffer> alt_bufs_;
     void *graph_ = nullptr;
@@ -471,6 +472,12 @@ template <class T = std::complex<float>> class SlicedContractor {
         acc_ = Gpu::DeviceBuffer(std::max<size_t>(result_size_ * 16, 16));
         counter_ = Gpu::DeviceBuffer(8);
         final_tmp_ = Gpu::DeviceBuffer(final_perm_needed_ ? nodes_[final_id_].bytes : 0);
+        // Leaves and slice-independent intermediates keep one buffer for the
+        // contractor's lifetime: the captured graph refers to their addresses.
+        for (auto &n : nodes_)
+            if (!n.chunk)
+                n.own = Gpu::DeviceBuffer(n.bytes);
+        prefix_done_ = false;
         planned_ = true;
     }
 
@@ -478,28 +485,23 @@ template <class T = std::complex<float>> class SlicedContractor {
     // prepares the leaves.
     void RunPrefix(void *st)
     {
-        const int dt = Gpu::DtypeCode<T>();
+        if (prefix_done_)
+            return;
         for (size_t i = 0; i < num_leaves_; ++i) {
             Node &n = nodes_[i];
             if (n.chunk)
                 continue;
-            if (!alt_values_[i].empty()) {
-                n.own = Gpu::DeviceBuffer(n.bytes);
+            if (!alt_values_[i].empty())
                 Gpu::Check(jetgpu_memcpy(n.own.get(), alt_values_[i].data(), n.bytes, 0, st),
                            "upload alternatives");
-            }
-            else {
-                n.own = Gpu::DeviceBuffer(n.bytes);
+            else
                 Gpu::Check(jetgpu_memcpy(n.own.get(), leaves_[i].GetDeviceData(), n.bytes, 2, st),
                            "leaf copy");
-            }
         }
         for (const Step &s : steps_)
-            if (!s.chunk) {
-                nodes_[s.out].own = Gpu::DeviceBuffer(nodes_[s.out].bytes);
+            if (!s.chunk)
                 Launch(s, st);
-            }
-        (void)dt;
+        prefix_done_ = true;
     }
 
     void Launch(const Step &s, void *st)

@@ -34,30 +34,52 @@ def _tn(jet, net, dtype):
     return tn
 
 
-@pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 1),
+def _oracle_slice(net, path, sliced, value):
+    from oracle import jet_oracle as jo
+
+    tn = jo.OTensorNetwork()
+    for lab, sh, d in net.tensors:
+        tn.add_tensor(jo.OTensor.make(lab, sh, d, np.complex128))
+    tn.slice_indices(sliced, value)
+    return tn.contract(path).data[0]
+
+
+@pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 2),
                                              ("complex128", 0)])
 @pytest.mark.parametrize("batch", [1, 4, 16])
 def test_sliced_amplitude_matches_unsliced(jet, dtype, precision, batch):
+    """Each slice equals the oracle's SliceIndices + Contract value (1e-5
+    relative in complex64); the slice sum equals the unsliced amplitude within
+    1e-5 of the summed magnitudes sum_v |slice_v| (the slices cancel, so the
+    sum is smaller than its terms); partial ranges add up."""
     from jet_gb300 import circuits
 
     net = circuits.random_circuit_network(4, 4, 8, seed=21, dtype=np.dtype(dtype))
     path = circuits.find_path(net, restarts=2, seed=21)
     sliced = circuits.choose_slices(net, path, 4)
     want = _oracle(net, path).data[0]
+    per_slice = [_oracle_slice(net, path, sliced, v) for v in range(16)]
+    scale = sum(abs(x) for x in per_slice)
     cls = jet.SlicedContractorC64 if dtype == "complex64" else jet.SlicedContractorC128
     sc = cls(_tn(jet, net, dtype), path, sliced, precision)
     sc.set_batch_size(batch)
     assert sc.num_slices == 16 and sc.batch_size == batch
+    tol = 1e-5 if dtype == "complex64" else 1e-12
     got = sc.contract()
     assert sc.result_indices == [] and len(got) == 1
-    tol = 1e-5 if dtype == "complex64" else 1e-12
-    assert abs(got[0] - want) <= tol * abs(want)
-    # A partial range: the sum of two halves is the whole.
+    assert abs(got[0] - want) <= tol * scale
+    if batch == 1:
+        for v in range(16):
+            one = sc.contract(v, 1)[0]
+            assert abs(one - per_slice[v]) <= tol * max(abs(per_slice[v]), 1e-3 * scale), v
     half = 8 if batch <= 8 else 16
     if half < 16:
         a = sc.contract(0, half)[0]
         b = sc.contract(half, 16 - half)[0]
-        assert abs(a + b - want) <= tol * abs(want)
+        assert abs(a - sum(per_slice[:half])) <= tol * scale
+        assert abs(a + b - want) <= tol * scale
+    # Contracting again reuses the captured graph and gives the same value.
+    assert abs(sc.contract()[0] - got[0]) <= tol * scale
 
 
 def test_reference_sliced_network_golden(jet, golden):
@@ -76,7 +98,7 @@ def test_reference_sliced_network_golden(jet, golden):
     assert abs(got - want) <= 1e-5 * abs(want)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 2])
 def test_bitstring_alternatives_share_prefix(jet, precision):
     """Output caps of 8 seeded bitstrings as alternatives of the cap leaves:
     one run yields every bitstring's amplitude (sliced over 3 bonds)."""
