@@ -186,6 +186,8 @@ def run_ours(args, rank, world, local_rank):
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
+    if args.tc_variant is not None:
+        capi.set_tc_variant(args.tc_variant)
     w = workload(12, N_COMMON, 12) if args.small else workload()
     m, n, k = w["m"], w["n"], w["k"]
     kp = k
@@ -195,7 +197,8 @@ def run_ours(args, rank, world, local_rank):
     A = torch.randn(m * k, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
     B = torch.randn(k * n, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
     pa = torch.empty(4 * m * kp, dtype=torch.float32, device=dev)
-    pb = torch.empty(4 * n * kp, dtype=torch.float32, device=dev)
+    bplanes = capi.tc_b_planes()
+    pb = torch.empty(bplanes * n * kp, dtype=torch.float32, device=dev)
     C = torch.empty(m * n, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -205,7 +208,8 @@ def run_ours(args, rank, world, local_rank):
         capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
         if events:
             events[1].record(stream)
-        capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, stream=stream)
+        capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, n_planes=bplanes,
+                        stream=stream)
         if events:
             events[2].record(stream)
         capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
@@ -313,7 +317,7 @@ def run_ours(args, rank, world, local_rank):
     tf32_peak = bf16_peak / 2.0
     gemm_ms = statistics.mean(gemm)
     split_ms = statistics.mean(split_a)
-    split_bytes = 24.0 * m * k  # read 8 B, write 4 planes x 4 B per element
+    split_bytes = 24.0 * m * k  # A: read 8 B, write 4 planes x 4 B per element
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -420,6 +424,25 @@ def run_sliced(args, rank, world, local_rank):
         dep_flops = sc.slice_dependent_flops
         del sc
     rel = abs(amps["auto"] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
+    # One slice in complex128 (FP64 arithmetic on the GPU) as the reference
+    # for the per-slice error of both complex64 forms.
+    slice_check = None
+    if args.check_fp64 and sliced:
+        tn128 = jet.TensorNetwork(dtype="complex128")
+        for lab, sh, d in net.tensors:
+            tn128.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex128"))
+        sc = jet.SlicedContractorC128(tn128, path, sliced, jet.PREC_FP32)
+        sc.set_batch_size(1)
+        ref64 = sc.contract(0, 1)[0]
+        del sc
+        slice_check = {"reference": "complex128 FP64 on the GPU, slice 0",
+                       "value": [ref64.real, ref64.imag]}
+        for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+            sc = jet.SlicedContractorC64(tn, path, sliced, prec)
+            sc.set_batch_size(1)
+            v = sc.contract(0, 1)[0]
+            slice_check["rel_err_" + name] = abs(v - ref64) / max(abs(ref64), 1e-300)
+            del sc
     line = {
         "metric": METRIC, "value": forms["auto"]["slices_per_s"], "unit": "slices/s",
         "n_gpus": world, "steps": 1, "warmup": 1,
@@ -436,8 +459,91 @@ def run_sliced(args, rank, world, local_rank):
         "slice_flops_pathinfo": slice_flops, "slice_dependent_flops": dep_flops,
         "amplitude_sample": [amps["auto"].real, amps["auto"].imag],
         "rel_diff_auto_vs_fp32": rel,
+        "slice_vs_fp64": slice_check,
         "plan_seconds": plan_s,
     }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_grad(args, rank, world, local_rank):
+    """Config 3: d Re<psi|Z_i Z_j|psi> / d(720 angles) of a 6x6, 10-layer
+    RX-RZ-CZ circuit through the hand-written adjoint (light-cone-pruned
+    doubled network, complex64 on the GPU, AUTO form). Reports forward and
+    backward times and the largest deviation from complex128 central finite
+    differences (h = 1e-4, complex128 forward on the GPU) over seeded angles."""
+    import torch
+
+    import jet_gb300 as jet
+    from jet_gb300 import autograd, circuits, expectation as ex
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    rows, cols, layers = 6, 6, 10
+    rng = np.random.default_rng(SEED)
+    th = rng.uniform(0, 2 * np.pi, (layers, rows * cols))
+    ph = rng.uniform(0, 2 * np.pi, (layers, rows * cols))
+    pair = ex.default_pair(rows, cols, SEED)
+    spec = ex.zz_network(rows, cols, layers, pair)
+    path = circuits.find_path(ex.numeric_network(spec, th, ph), restarts=8, seed=SEED)
+    labels = [l.labels for l in spec]
+    t = torch.tensor(th, dtype=torch.float32, device=dev, requires_grad=True)
+    p = torch.tensor(ph, dtype=torch.float32, device=dev, requires_grad=True)
+    plan = autograd.ContractionPlan(labels, [l.shape for l in spec], path)
+
+    def step():
+        t.grad = None
+        p.grad = None
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        lv = ex.build_leaves(spec, t, p, dtype=torch.complex64, device=dev)
+        loss = autograd.contract_network(lv, labels, path, precision=jet.PREC_AUTO, plan=plan).real
+        e1.record()
+        loss.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        return float(loss.item()), e0.elapsed_time(e1), e1.elapsed_time(e2)
+
+    for _ in range(args.warmup):
+        step()
+    fw, bw = [], []
+    for _ in range(args.steps):
+        val, f_ms, b_ms = step()
+        fw.append(f_ms)
+        bw.append(b_ms)
+    g_t = t.grad.double().cpu().numpy()
+    g_p = p.grad.double().cpu().numpy()
+
+    def loss64(a, b):
+        lv = ex.build_leaves(spec, torch.tensor(a, device=dev), torch.tensor(b, device=dev),
+                             dtype=torch.complex128, device=dev)
+        return float(autograd.contract_network(lv, labels, path, precision=jet.PREC_FP32,
+                                               plan=plan).real.item())
+
+    h = 1e-4
+    worst = 0.0
+    picks = [(int(rng.integers(layers)), int(rng.integers(rows * cols)), w)
+             for w in ("t", "p") for _ in range(6)]
+    for l, q, w in picks:
+        a1, b1, a2, b2 = th.copy(), ph.copy(), th.copy(), ph.copy()
+        if w == "t":
+            a1[l, q] += h
+            a2[l, q] -= h
+        else:
+            b1[l, q] += h
+            b2[l, q] -= h
+        fd = (loss64(a1, b1) - loss64(a2, b2)) / (2 * h)
+        worst = max(worst, abs(fd - (g_t if w == "t" else g_p)[l, q]))
+    f_med, b_med = statistics.median(fw), statistics.median(bw)
+    line = {"metric": METRIC, "value": 1e3 / (f_med + b_med), "unit": "gradients/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": f_med + b_med, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded angles)",
+            "config": {"workload": "config 3: 6x6 grid, 10 layers RX-RZ-CZ, 720 angles, "
+                                   "Re<Z_%d Z_%d>, light-cone doubled network (%d tensors)"
+                                   % (pair[0], pair[1], len(spec))},
+            "forward_ms": f_med, "backward_ms": b_med, "backward_over_forward": b_med / f_med,
+            "loss": val, "max_abs_err_vs_fd_complex128": worst, "fd_checks": len(picks)}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -453,6 +559,10 @@ def main():
                     help="profiling case: rank-25 x rank-25 (M = N = 2^12, K = 2^13)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="skip the plain-FP32, end-to-end and CPU legs")
+    ap.add_argument("--check-fp64", action="store_true",
+                    help="sliced configs: also contract slice 0 in complex128")
+    ap.add_argument("--tc-variant", type=int, default=None,
+                    help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",
                     help="1 (default): the pairwise contraction; 0, 2, 4: sliced circuit "
                          "amplitudes through the sliced executor")
@@ -464,6 +574,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.config == "3":
+        run_grad(args, rank, world, local_rank)
         return
     if args.config != "1":
         run_sliced(args, rank, world, local_rank)

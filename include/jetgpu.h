@@ -222,22 +222,32 @@ size_t jetgpu_contract_noalloc_max_scratch(void);
  * schedule them separately (batched executors, profilers).
  *
  * jetgpu_split_tf32: permutes a complex64 tensor (as jetgpu_permute) and
- * writes it, multiplied by 2^scale_exp, as four fp32 planes holding TF32
- * values: plane p at planes + p * plane_stride floats, p = 0 re_hi,
- * 1 re_lo, 2 im_hi, 3 im_lo (x = hi + lo + O(2^-22 |x|)); the permuted
- * tensor is viewed as a rows x cols row-major matrix stored with a row pitch
- * of `pitch` floats (pitch >= cols, pitch % 4 == 0).
+ * writes it, multiplied by 2^scale_exp, as fp32 planes holding TF32 values:
+ * plane p at planes + p * plane_stride floats, p = 0 re_hi, 1 re_lo, 2 im_hi,
+ * 3 im_lo (x = hi + lo + O(2^-22 |x|)) and, when n_planes == 6, 4 -im_hi,
+ * 5 -im_lo; the permuted tensor is viewed as a rows x cols row-major matrix
+ * stored with a row pitch of `pitch` floats (pitch >= cols, pitch % 4 == 0).
  *
  * jetgpu_gemm_tf32x3: C[m x n] (complex64, row-major) = A * B^T from the
- * planes of A (m x k) and B (n x k, i.e. B in (right ++ common) order), with
- * row pitch kpitch; tcgen05 kind::tf32 tensor cores, three products per real
- * product, FP32 accumulation, output multiplied by `out_scale`.
+ * planes of A (m x k, 4 planes) and B (n x k, i.e. B in (right ++ common)
+ * order, jetgpu_tc_b_planes() planes), with row pitch kpitch; tcgen05
+ * kind::tf32 tensor cores, three products per real product, FP32
+ * accumulation, output multiplied by `out_scale`.
  * Replaces the cblas_cgemm call of TensorHelpers.hpp:47-61.
+ *
+ * jetgpu_set_tc_variant selects the main-loop shape of the tensor-core
+ * product for the calling process: 0 = M 128 x N 128 MMAs over 4 B planes,
+ * 1 = M 128 x N 256 MMAs over 6 B planes (stacked [Br; Bi] and [-Bi; Br]
+ * operands, half the MMA count); jetgpu_tc_b_planes() reports the B planes
+ * the current shape reads.
  */
 int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape,
                       const int32_t *perm, uint64_t rows, uint64_t cols,
                       uint64_t pitch, uint64_t plane_stride, int scale_exp,
-                      float *planes, void *stream);
+                      int n_planes, float *planes, void *stream);
+
+int jetgpu_set_tc_variant(int wide);
+int jetgpu_tc_b_planes(void);
 
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,

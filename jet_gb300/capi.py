@@ -64,7 +64,8 @@ lib.jetgpu_contract.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, _vp, ctypes.c_i
                                 ctypes.c_int, _vp, ctypes.c_size_t, _vp]
 lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
-                                  _vp, _vp]
+                                  ctypes.c_int, _vp, _vp]
+lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
 lib.jetgpu_contract_batched_workspace_size.restype = ctypes.c_size_t
@@ -210,11 +211,22 @@ def contract_batched(batch, a, a_shape, a_perm, a_batched, b, b_shape, b_perm, b
     return out
 
 
-def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, stream=None):
-    """Permute + TF32 hi/lo split into 4 planes of rows x pitch floats."""
+def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, n_planes=4,
+               stream=None):
+    """Permute + TF32 hi/lo split into 4 (or 6) planes of rows x pitch floats."""
     check(lib.jetgpu_split_tf32(_ptr(x), len(shape), u64(shape), i32(perm), rows, cols, pitch,
-                                rows * pitch, scale_exp, _ptr(planes), _stream(stream)))
+                                rows * pitch, scale_exp, n_planes, _ptr(planes),
+                                _stream(stream)))
     return planes
+
+
+def set_tc_variant(wide: int) -> None:
+    """0: N = 128 tensor-core main loop; 1: N = 256 (six B planes)."""
+    check(lib.jetgpu_set_tc_variant(int(wide)))
+
+
+def tc_b_planes() -> int:
+    return int(lib.jetgpu_tc_b_planes())
 
 
 def gemm_tf32x3(a_planes, b_planes, m, n, k, kpitch, out, out_scale=1.0, stream=None):

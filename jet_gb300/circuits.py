@@ -151,6 +151,44 @@ def random_circuit_network(rows: int, cols: int, cycles: int, seed: int = 0,
     return Network([(l, s, d.astype(dtype)) for l, s, d in tensors])
 
 
+def haar_unitary(d: int, rng: np.random.Generator) -> np.ndarray:
+    """Haar-random d x d unitary: QR of a complex Gaussian matrix with the
+    phases of R's diagonal folded back into Q (Mezzadri, 2007)."""
+    z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / math.sqrt(2.0)
+    q, r = np.linalg.qr(z)
+    ph = np.diag(r) / np.abs(np.diag(r))
+    return q * ph
+
+
+def qudit_circuit_network(rows: int, cols: int, layers: int, d: int = 3, seed: int = 0,
+                          dtype=np.complex64) -> Network:
+    """<0...0| C |0...0> of a qudit circuit (local dimension d): per layer a
+    seeded Haar-random d x d unitary on every site, then a Haar-random
+    d^2 x d^2 unitary on one of the four alternating nearest-neighbour
+    coupler patterns."""
+    rng = np.random.default_rng(seed)
+    n = rows * cols
+    pats = couplers(rows, cols)
+    wires = _Wires(n)
+    e0 = np.zeros(d, dtype=np.complex128)
+    e0[0] = 1
+    tensors: List[Tuple[List[str], List[int], np.ndarray]] = []
+    for q in range(n):
+        tensors.append(([wires.cur(q)], [d], e0.copy()))
+    for layer in range(layers):
+        for q in range(n):
+            i = wires.cur(q)
+            o = wires.advance(q)
+            tensors.append(([o, i], [d, d], haar_unitary(d, rng).reshape(-1)))
+        for a, b in pats["ABCD"[layer % 4]]:
+            ia, ib = wires.cur(a), wires.cur(b)
+            oa, ob = wires.advance(a), wires.advance(b)
+            tensors.append(([oa, ob, ia, ib], [d, d, d, d], haar_unitary(d * d, rng).reshape(-1)))
+    for q in range(n):
+        tensors.append(([wires.cur(q)], [d], e0.copy()))
+    return Network([(l, s, x.astype(dtype)) for l, s, x in tensors])
+
+
 def parameterised_layers_network(rows: int, cols: int, layers: int,
                                  thetas: np.ndarray, phis: np.ndarray,
                                  dtype=np.complex64) -> Tuple[Network, List[Tuple[int, str]]]:

@@ -80,10 +80,12 @@ int PermuteSplitTf32(const void *in, float *planes, int rank,
 // Permute + TF32 split of `batch` tensors stored back to back; tensor b lands
 // in rows [b * rows, (b + 1) * rows) of every plane (plane_stride >= batch *
 // rows * pitch).
+// neg_im != 0 also writes planes 4, 5 = -im_hi, -im_lo (the B operand of the
+// N = 256 tensor-core product).
 int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int rank,
                             const uint64_t *shape, const int32_t *perm, uint64_t rows,
                             uint64_t cols, uint64_t pitch, uint64_t plane_stride,
-                            int scale_exp, cudaStream_t stream);
+                            int scale_exp, cudaStream_t stream, int neg_im = 0);
 
 // C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
 // operand), C packed as batch x m x n.
@@ -109,5 +111,9 @@ int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
                      float out_scale, cudaStream_t stream);
 
 bool TcAvailable();
+
+// Main-loop shape of the tensor-core product: wide (N = 256 MMAs) needs six B
+// planes (re hi/lo, im hi/lo, -im hi/lo), narrow four.
+bool TcWide();
 
 } // namespace jetgpu

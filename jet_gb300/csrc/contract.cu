@@ -92,7 +92,7 @@ size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
 {
     if (UseTensorCores(m, n, k, dtype, precision)) {
         const uint64_t kp = (k + 3) / 4 * 4;
-        return AlignUp(4 * m * kp * sizeof(float)) + AlignUp(4 * n * kp * sizeof(float));
+        return AlignUp(4 * m * kp * sizeof(float)) + AlignUp(6 * n * kp * sizeof(float));
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -150,7 +150,8 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
         rc = PermuteSplitTf32(A, pa, a_rank, a_shape, a_perm, m, k, kp, m * kp, scale_a, st);
         if (rc)
             return rc;
-        rc = PermuteSplitTf32(B, pb, b_rank, b_shape, bt.data(), n, k, kp, n * kp, scale_b, st);
+        rc = PermuteSplitTf32Batched(B, pb, 1, b_rank, b_shape, bt.data(), n, k, kp, n * kp,
+                                     scale_b, st, TcWide() ? 1 : 0);
         if (rc)
             return rc;
         return GemmTf32x3Planar(pa, pb, C, m, n, k, kp, 1.0f, st);
@@ -183,16 +184,18 @@ extern "C" {
 
 int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
                       uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
-                      int scale_exp, float *planes, void *stream)
+                      int scale_exp, int n_planes, float *planes, void *stream)
 {
     ClearError();
+    JETGPU_REQUIRE(n_planes == 4 || n_planes == 6, "n_planes must be 4 or 6");
     JETGPU_REQUIRE(pitch >= cols && pitch % 4 == 0, "pitch must be >= cols and a multiple of 4");
     JETGPU_REQUIRE(plane_stride >= rows * pitch, "plane stride too small");
     if (rows * cols == 0)
         return JETGPU_OK;
     JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
-    return PermuteSplitTf32(in, planes, rank, shape, perm, rows, cols, pitch, plane_stride,
-                            scale_exp, AsStream(stream));
+    return PermuteSplitTf32Batched(in, planes, 1, rank, shape, perm, rows, cols, pitch,
+                                   plane_stride, scale_exp, AsStream(stream),
+                                   n_planes == 6 ? 1 : 0);
 }
 
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C, uint64_t m,
@@ -264,7 +267,7 @@ size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const 
     if (p.tc) {
         const uint64_t kp = (k + 3) / 4 * 4;
         return AlignUp(4 * p.ba * m * kp * sizeof(float)) +
-               AlignUp(4 * p.bb * n * kp * sizeof(float));
+               AlignUp(6 * p.bb * n * kp * sizeof(float));
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -330,7 +333,7 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
         if (rc)
             return rc;
         rc = PermuteSplitTf32Batched(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, kp,
-                                     p.bb * n * kp, scale_b, st);
+                                     p.bb * n * kp, scale_b, st, TcWide() ? 1 : 0);
         if (rc)
             return rc;
         return GemmTf32x3PlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, kp, 1.0f,

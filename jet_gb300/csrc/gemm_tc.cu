@@ -34,14 +34,30 @@ namespace {
 
 constexpr int kBM = 128;
 constexpr int kBN = 128;
-constexpr int kBK = 16;                    // complex k per stage (64 bytes of fp32)
-constexpr int kStages = 3;
-constexpr int kTileBytes = kBM * kBK * 4;  // one plane box: 8 KB
-constexpr int kStageBytes = 8 * kTileBytes; // 4 A planes + 4 B planes: 64 KB
 constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
-constexpr int kChunkStages = 8;               // stages (x16 complex k) per TMEM chunk
+
+// Two shapes of the main loop.
+//  narrow: 16-deep stages (64-byte rows, 64-byte swizzle), 3 stages of
+//          4 A + 4 B plane boxes; 24 MMAs of N = 128 per stage.
+//  wide:   8-deep stages (32-byte rows, 32-byte swizzle), 5 stages of 4 A
+//          boxes and two B triples [-Bi, Br, Bi] (hi, lo); 6 MMAs of
+//          N = 256 per stage: Ar [Br; Bi] -> [ArBr | ArBi] and
+//          Ai [-Bi; Br] -> [-AiBi | AiBr] land on (Cr | Ci) in one
+//          instruction each, halving the MMA count and cutting the shared
+//          memory read per flop by a quarter.
+template <bool kWide> struct TcCfg;
+template <> struct TcCfg<false> {
+    static constexpr int BK = 16, Stages = 3, Tiles = 8, ChunkStages = 8, RowBytes = 64;
+    static constexpr uint32_t SwizzleCode = 4; // 64-byte swizzle
+};
+template <> struct TcCfg<true> {
+    static constexpr int BK = 8, Stages = 5, Tiles = 10, ChunkStages = 16, RowBytes = 32;
+    static constexpr uint32_t SwizzleCode = 6; // 32-byte swizzle
+};
+template <bool W> constexpr int TileBytes() { return kBM * TcCfg<W>::BK * 4; }
+template <bool W> constexpr int StageBytes() { return TcCfg<W>::Tiles * TileBytes<W>(); }
 constexpr unsigned long long kWaitNs = 4000000000ull; // 4 s bound per wait
 
 __device__ __forceinline__ uint32_t SmemAddr(const void *p)
@@ -117,16 +133,16 @@ __device__ __forceinline__ void TmaLoad4d(uint32_t dst, const CUtensorMap *map,
                  : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 64-byte swizzle, 8-row
-// groups 512 bytes apart.
-__device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
+// Shared-memory matrix descriptor: K-major operand, swizzled rows of
+// RowBytes, 8-row groups 8 * RowBytes apart.
+template <bool kWide> __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
 {
     uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
-    d |= (uint64_t)1 << 16;                   // leading byte offset (unused)
-    d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset
-    d |= (uint64_t)1 << 46;                   // descriptor version
-    d |= (uint64_t)4 << 61;                   // 64-byte swizzle
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);                       // start address
+    d |= (uint64_t)1 << 16;                                        // leading byte offset (unused)
+    d |= (uint64_t)((8 * TcCfg<kWide>::RowBytes) >> 4) << 32;      // stride byte offset
+    d |= (uint64_t)1 << 46;                                        // descriptor version
+    d |= (uint64_t)TcCfg<kWide>::SwizzleCode << 61;                // swizzle mode
     return d;
 }
 
@@ -193,6 +209,7 @@ __device__ __forceinline__ void TmemWaitLoad()
 // into FP32 registers (round-to-nearest) while the next chunk accumulates in
 // the other set. Accumulator warp w (w = 2..9) owns TMEM lanes 32*(w%4)..+31
 // (tile rows) and columns [64*h, 64*h + 64) of Cr and Ci, h = (w - 2) / 4.
+template <bool kWide>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
@@ -203,6 +220,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
     const int bz = blockIdx.z;
     C += (size_t)bz * M * N;
+    using Cfg = TcCfg<kWide>;
+    constexpr int kBK = Cfg::BK;
+    constexpr int kStages = Cfg::Stages;
+    constexpr int kChunkStages = Cfg::ChunkStages;
+    constexpr int kTileBytes = TileBytes<kWide>();
+    constexpr int kStageBytes = StageBytes<kWide>();
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
@@ -259,10 +282,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                         TmaLoad4d(base + p * kTileBytes, &tmA, k0, m0, bz, p, fb);
                     else
                         TmaLoad3d(base + p * kTileBytes, &tmA, k0, m0, p, fb);
+                }
+                // B tiles: narrow {Br_hi, Br_lo, Bi_hi, Bi_lo}; wide
+                // {-Bi_hi, Br_hi, Bi_hi, -Bi_lo, Br_lo, Bi_lo} (plane numbers
+                // 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo, 4 -im_hi, 5 -im_lo).
+                constexpr int kBTiles = Cfg::Tiles - 4;
+#pragma unroll
+                for (int t = 0; t < kBTiles; ++t) {
+                    const int plane = kWide ? (t == 0 ? 4 : t == 1 ? 0 : t == 2 ? 2
+                                               : t == 3 ? 5 : t == 4 ? 1 : 3)
+                                            : t;
                     if (b_batched)
-                        TmaLoad4d(base + (4 + p) * kTileBytes, &tmB, k0, n0, bz, p, fb);
+                        TmaLoad4d(base + (4 + t) * kTileBytes, &tmB, k0, n0, bz, plane, fb);
                     else
-                        TmaLoad3d(base + (4 + p) * kTileBytes, &tmB, k0, n0, p, fb);
+                        TmaLoad3d(base + (4 + t) * kTileBytes, &tmB, k0, n0, plane, fb);
                 }
             }
         }
@@ -294,17 +327,38 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t d_re = tmem + buf * 2 * kBN;
                 const uint32_t d_im = d_re + kBN;
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
+                if constexpr (kWide) {
+                    constexpr uint32_t kIdescW = InstrDesc(kBM, 2 * kBN, false);
+                    const uint64_t arh = SmemDesc<true>(base + 0 * kTileBytes);
+                    const uint64_t arl = SmemDesc<true>(base + 1 * kTileBytes);
+                    const uint64_t aih = SmemDesc<true>(base + 2 * kTileBytes);
+                    const uint64_t ail = SmemDesc<true>(base + 3 * kTileBytes);
+                    const uint64_t b_nr_hi = SmemDesc<true>(base + 4 * kTileBytes); // [-Bi; Br]
+                    const uint64_t b_rc_hi = SmemDesc<true>(base + 5 * kTileBytes); // [Br; Bi]
+                    const uint64_t b_nr_lo = SmemDesc<true>(base + 7 * kTileBytes);
+                    const uint64_t b_rc_lo = SmemDesc<true>(base + 8 * kTileBytes);
+                    const uint32_t acc = chunk_start ? 0u : 1u;
+                    // (Cr | Ci) += Ar [Br; Bi]
+                    MmaTf32(d_re, arh, b_rc_hi, kIdescW, acc);
+                    MmaTf32(d_re, arh, b_rc_lo, kIdescW, 1u);
+                    MmaTf32(d_re, arl, b_rc_hi, kIdescW, 1u);
+                    // (Cr | Ci) += Ai [-Bi; Br]
+                    MmaTf32(d_re, aih, b_nr_hi, kIdescW, 1u);
+                    MmaTf32(d_re, aih, b_nr_lo, kIdescW, 1u);
+                    MmaTf32(d_re, ail, b_nr_hi, kIdescW, 1u);
+                }
+                else
 #pragma unroll
                 for (int kk = 0; kk < kBK / 8; ++kk) {
                     const uint32_t koff = kk * 32; // 8 fp32 per MMA step
-                    const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
-                    const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
-                    const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
-                    const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
-                    const uint64_t brh = SmemDesc(base + 4 * kTileBytes + koff);
-                    const uint64_t brl = SmemDesc(base + 5 * kTileBytes + koff);
-                    const uint64_t bih = SmemDesc(base + 6 * kTileBytes + koff);
-                    const uint64_t bil = SmemDesc(base + 7 * kTileBytes + koff);
+                    const uint64_t arh = SmemDesc<false>(base + 0 * kTileBytes + koff);
+                    const uint64_t arl = SmemDesc<false>(base + 1 * kTileBytes + koff);
+                    const uint64_t aih = SmemDesc<false>(base + 2 * kTileBytes + koff);
+                    const uint64_t ail = SmemDesc<false>(base + 3 * kTileBytes + koff);
+                    const uint64_t brh = SmemDesc<false>(base + 4 * kTileBytes + koff);
+                    const uint64_t brl = SmemDesc<false>(base + 5 * kTileBytes + koff);
+                    const uint64_t bih = SmemDesc<false>(base + 6 * kTileBytes + koff);
+                    const uint64_t bil = SmemDesc<false>(base + 7 * kTileBytes + koff);
                     const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                     // Cr += Ar Br
                     MmaTf32(d_re, arh, brh, kIdesc, acc);
@@ -417,17 +471,18 @@ int GetEncoder()
     return JETGPU_OK;
 }
 
-// 3-D map over planes: (k, row, plane), box 16 x 128 x 1, 64-byte swizzle.
+// 3-D map over planes: (k, row, plane), box BK x 128 x 1.
 int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
-                 uint64_t kpitch)
+                 uint64_t kpitch, bool wide, int planes)
 {
-    cuuint64_t dims[3] = {k, rows, 4};
+    cuuint64_t dims[3] = {k, rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {kpitch * 4, rows * kpitch * 4};
-    cuuint32_t box[3] = {kBK, kBM, 1};
+    cuuint32_t box[3] = {(cuuint32_t)(wide ? TcCfg<true>::BK : TcCfg<false>::BK), kBM, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                           const_cast<float *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          wide ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
@@ -437,17 +492,18 @@ int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
 }
 
 // 4-D map over batched planes laid out [plane][batch][rows][kpitch]:
-// (k, row, batch, plane), box 16 x 128 x 1 x 1.
+// (k, row, batch, plane), box BK x 128 x 1 x 1.
 int EncodePlanesBatched(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
-                        uint64_t kpitch, uint64_t batch)
+                        uint64_t kpitch, uint64_t batch, bool wide, int planes)
 {
-    cuuint64_t dims[4] = {k, rows, batch, 4};
+    cuuint64_t dims[4] = {k, rows, batch, (cuuint64_t)planes};
     cuuint64_t strides[3] = {kpitch * 4, rows * kpitch * 4, batch * rows * kpitch * 4};
-    cuuint32_t box[4] = {kBK, kBM, 1, 1};
+    cuuint32_t box[4] = {(cuuint32_t)(wide ? TcCfg<true>::BK : TcCfg<false>::BK), kBM, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                           const_cast<float *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          wide ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
@@ -455,6 +511,32 @@ int EncodePlanesBatched(CUtensorMap *map, const float *base, uint64_t rows, uint
                         "cuTensorMapEncodeTiled (4-D) failed: " + std::to_string((int)r));
     return JETGPU_OK;
 }
+
+template <bool kWide>
+int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
+             uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
+             cudaStream_t stream)
+{
+    const size_t smem = (size_t)TcCfg<kWide>::Stages * StageBytes<kWide>() + 1024;
+    static thread_local int configured_dev = -1;
+    int dev = 0;
+    JETGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (configured_dev != dev) {
+        JETGPU_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel<kWide>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem));
+        configured_dev = dev;
+    }
+    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM),
+              (unsigned)batch);
+    const int ktiles = (int)((k + TcCfg<kWide>::BK - 1) / TcCfg<kWide>::BK);
+    tc_gemm_tf32x3_kernel<kWide><<<grid, kThreads, smem, stream>>>(
+        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
+        b_batched);
+    return CheckLaunch("tc_gemm_tf32x3_kernel");
+}
+
+int g_tc_wide = 0; // main-loop shape of the tensor-core product (jetgpu_set_tc_variant)
 
 } // namespace
 
@@ -488,32 +570,34 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
     int rc = GetEncoder();
     if (rc)
         return rc;
+    const bool wide = g_tc_wide != 0;
     CUtensorMap ta, tb;
-    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch)
-                        : EncodePlanes(&ta, a_planes, m, k, kpitch)))
+    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, wide, 4)
+                        : EncodePlanes(&ta, a_planes, m, k, kpitch, wide, 4)))
         return rc;
-    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch)
-                        : EncodePlanes(&tb, b_planes, n, k, kpitch)))
+    const int bplanes = wide ? 6 : 4;
+    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, wide, bplanes)
+                        : EncodePlanes(&tb, b_planes, n, k, kpitch, wide, bplanes)))
         return rc;
-    const size_t smem = (size_t)kStages * kStageBytes + 1024;
-    static thread_local int configured_dev = -1;
-    int dev = 0;
-    JETGPU_CUDA_TRY(cudaGetDevice(&dev));
-    if (configured_dev != dev) {
-        JETGPU_CUDA_TRY(cudaFuncSetAttribute(
-            tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured_dev = dev;
-    }
-    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM),
-              (unsigned)batch);
-    const int ktiles = (int)((k + kBK - 1) / kBK);
-    tc_gemm_tf32x3_kernel<<<grid, kThreads, smem, stream>>>(
-        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
-        b_batched);
-    return CheckLaunch("tc_gemm_tf32x3_kernel");
+    return wide ? LaunchTc<true>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
+                                 stream)
+                : LaunchTc<false>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
+                                  stream);
 }
 
+bool TcWide() { return g_tc_wide != 0; }
+
 } // namespace jetgpu
+
+extern "C" int jetgpu_tc_b_planes(void) { return jetgpu::TcWide() ? 6 : 4; }
+
+extern "C" int jetgpu_set_tc_variant(int wide)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(wide == 0 || wide == 1, "variant must be 0 (N = 128) or 1 (N = 256)");
+    jetgpu::g_tc_wide = wide;
+    return JETGPU_OK;
+}
 
 extern "C" int jetgpu_take_device_status(int *status)
 {

@@ -141,11 +141,12 @@ __device__ __forceinline__ float RoundTf32(float x)
 }
 
 struct SplitOut {
-    float *planes;         // 4 planes
+    float *planes;         // 4 planes, or 6 with the negated imaginary pair
     uint64_t plane_stride; // floats between planes
     uint64_t cols;         // logical columns of the permuted view
     uint64_t pitch;        // floats per row in a plane
     float scale;           // exact power of two
+    int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo
 };
 
 __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
@@ -161,6 +162,10 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
     so.planes[off + so.plane_stride] = rl;
     so.planes[off + 2 * so.plane_stride] = ih;
     so.planes[off + 3 * so.plane_stride] = il;
+    if (so.neg_im) {
+        so.planes[off + 4 * so.plane_stride] = -ih;
+        so.planes[off + 5 * so.plane_stride] = -il;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -275,6 +280,12 @@ struct SplitStore {
         *reinterpret_cast<float2 *>(so.planes + base + so.plane_stride) = rl;
         *reinterpret_cast<float2 *>(so.planes + base + 2 * so.plane_stride) = ih;
         *reinterpret_cast<float2 *>(so.planes + base + 3 * so.plane_stride) = il;
+        if (so.neg_im) {
+            *reinterpret_cast<float2 *>(so.planes + base + 4 * so.plane_stride) =
+                make_float2(-ih.x, -ih.y);
+            *reinterpret_cast<float2 *>(so.planes + base + 5 * so.plane_stride) =
+                make_float2(-il.x, -il.y);
+        }
     }
 };
 
@@ -519,7 +530,7 @@ int PermuteSplitTf32(const void *in, float *planes, int rank,
 int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int rank,
                             const uint64_t *shape, const int32_t *perm, uint64_t rows,
                             uint64_t cols, uint64_t pitch, uint64_t plane_stride,
-                            int scale_exp, cudaStream_t stream)
+                            int scale_exp, cudaStream_t stream, int neg_im)
 {
     Simplified s;
     int rc = Simplify(rank, shape, perm, s);
@@ -537,6 +548,7 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
     so.cols = cols;
     so.pitch = pitch;
     so.scale = ldexpf(1.0f, scale_exp);
+    so.neg_im = neg_im;
     const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
                          (pitch % 2 == 0) && (plane_stride % 2 == 0);
     static thread_local BitParams bp;

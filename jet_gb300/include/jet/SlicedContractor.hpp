@@ -214,6 +214,8 @@ template <class T = std::complex<float>> class SlicedContractor {
     size_t arena_bytes_ = 0, ws_bytes_ = 0, tmp_bytes_ = 0;
     bool planned_ = false;
     bool prefix_done_ = false;
+    std::vector<char> persist_;
+    std::vector<int> prefix_last_use_;
     Gpu::DeviceBuffer arena_, ws_, tmp_a_, tmp_b_, acc_, counter_, final_tmp_;
     std::vector<Gpu::DeviceBuffer> alt_bufs_;
     void *graph_ = nullptr;
@@ -472,11 +474,27 @@ template <class T = std::complex<float>> class SlicedContractor {
         acc_ = Gpu::DeviceBuffer(std::max<size_t>(result_size_ * 16, 16));
         counter_ = Gpu::DeviceBuffer(8);
         final_tmp_ = Gpu::DeviceBuffer(final_perm_needed_ ? nodes_[final_id_].bytes : 0);
-        // Leaves and slice-independent intermediates keep one buffer for the
-        // contractor's lifetime: the captured graph refers to their addresses.
-        for (auto &n : nodes_)
-            if (!n.chunk)
-                n.own = Gpu::DeviceBuffer(n.bytes);
+        // Slice-independent tensors that the captured graph reads (leaves,
+        // prefix outputs consumed by "$s" steps, the final result) keep one
+        // buffer for the contractor's lifetime; other prefix intermediates
+        // live only while the prefix runs.
+        persist_.assign(nodes_.size(), 0);
+        for (size_t i = 0; i < num_leaves_; ++i)
+            persist_[i] = 1;
+        for (const Step &s : steps_)
+            if (s.chunk)
+                for (int id : {s.a, s.b})
+                    persist_[id] = 1;
+        persist_[final_id_] = 1;
+        prefix_last_use_.assign(nodes_.size(), -1);
+        for (size_t i = 0; i < steps_.size(); ++i)
+            if (!steps_[i].chunk) {
+                prefix_last_use_[steps_[i].a] = (int)i;
+                prefix_last_use_[steps_[i].b] = (int)i;
+            }
+        for (size_t i = 0; i < nodes_.size(); ++i)
+            if (!nodes_[i].chunk && persist_[i])
+                nodes_[i].own = Gpu::DeviceBuffer(nodes_[i].bytes);
         prefix_done_ = false;
         planned_ = true;
     }
@@ -498,9 +516,17 @@ template <class T = std::complex<float>> class SlicedContractor {
                 Gpu::Check(jetgpu_memcpy(n.own.get(), leaves_[i].GetDeviceData(), n.bytes, 2, st),
                            "leaf copy");
         }
-        for (const Step &s : steps_)
-            if (!s.chunk)
-                Launch(s, st);
+        for (size_t i = 0; i < steps_.size(); ++i) {
+            const Step &s = steps_[i];
+            if (s.chunk)
+                continue;
+            if (!persist_[s.out])
+                nodes_[s.out].own = Gpu::DeviceBuffer(nodes_[s.out].bytes);
+            Launch(s, st);
+            for (int id : {s.a, s.b})
+                if (!persist_[id] && prefix_last_use_[id] == (int)i)
+                    nodes_[id].own.reset(); // stream-ordered free
+        }
         prefix_done_ = true;
     }
 

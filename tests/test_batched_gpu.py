@@ -34,8 +34,13 @@ def _case(seed, nl, nc, nr, dtype, batch, a_b, b_b, dev):
 @pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 1),
                                              ("complex128", 0)])
 @pytest.mark.parametrize("shape", [(7, 6, 8), (1, 9, 3), (4, 10, 1), (0, 5, 0), (8, 8, 8)])
-def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape, variant):
     from jet_gb300 import capi
+
+    if variant and precision == 0:
+        pytest.skip("the main-loop shape only affects the tensor-core form")
+    capi.set_tc_variant(variant)
 
     batch = 5
     nl, nc, nr = shape
@@ -54,3 +59,4 @@ def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape):
         err = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
         assert err <= tol, (bi, err)
     assert capi.take_device_status() == 0
+    capi.set_tc_variant(0)

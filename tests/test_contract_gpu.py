@@ -35,6 +35,16 @@ def _plan(a_labels, a_shape, b_labels, b_shape):
     return a_perm, b_perm, m, n, k, left + right
 
 
+@pytest.fixture(params=[0, 1], ids=["n128", "n256"])
+def tc_variant(request, cuda):
+    """Runs a test under both main-loop shapes of the tensor-core product."""
+    from jet_gb300 import capi
+
+    capi.set_tc_variant(request.param)
+    yield request.param
+    capi.set_tc_variant(0)
+
+
 def _rel(got, want):
     return np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
 
@@ -61,7 +71,7 @@ def test_reference_contractions_plain(cuda, golden):
         assert _rel(got, want) <= tol, c
 
 
-def test_reference_contractions_tf32x3(cuda, golden):
+def test_reference_contractions_tf32x3(cuda, golden, tc_variant):
     from jet_gb300 import capi
 
     for c in golden["ref"]["contract"]:
@@ -90,7 +100,7 @@ def test_reference_literal_values(cuda):
 @pytest.mark.parametrize("m,n,k", [(128, 128, 16), (256, 128, 64), (200, 136, 100),
                                    (1024, 512, 256), (130, 300, 33), (4096, 256, 1024),
                                    (64, 512, 2048)])
-def test_tf32x3_random_gemm(cuda, m, n, k):
+def test_tf32x3_random_gemm(cuda, m, n, k, tc_variant):
     """Random N(0, 1/2) complex entries scaled by 2^-10 (the config-1
     distribution) against the complex128 product."""
     import torch
@@ -112,7 +122,7 @@ def test_tf32x3_random_gemm(cuda, m, n, k):
     assert capi.take_device_status() == 0
 
 
-def test_tf32x3_transposed_operands_config1_shape_reduced(cuda):
+def test_tf32x3_transposed_operands_config1_shape_reduced(cuda, tc_variant):
     """Config-1 structure at reduced size: A rank 21, B rank 19, 10 shared
     labels, both seeded-randomly permuted."""
     from jet_gb300 import capi
@@ -163,7 +173,7 @@ def test_multiply_vector_and_edge_shapes(cuda, m, n, k, dtype):
         assert _rel(direct.reshape(m, n), want) <= (1e-5 if dtype == np.complex64 else 1e-12)
 
 
-def test_power_of_two_scales(cuda):
+def test_power_of_two_scales(cuda, tc_variant):
     from jet_gb300 import capi
 
     m = n = 256
