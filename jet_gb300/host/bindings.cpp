@@ -92,6 +92,14 @@ template <class T> void BindTensor(py::module_ &m)
              py::arg("ptr"));
 
     m.def("conj", [](const tensor_t &t) { return tensor_t::Conj(t); }, py::arg("tensor"));
+    // Permuter<QFlexPermuter<>>::Transpose on host data (the permuter plugin point).
+    m.def("permuter_transpose",
+          [](const std::vector<T> &data, const std::vector<size_t> &shape,
+             const std::vector<std::string> &current, const std::vector<std::string> &target) {
+              Jet::Permuter<Jet::QFlexPermuter<>> p;
+              return p.Transpose(data, shape, current, target);
+          },
+          py::arg("data"), py::arg("shape"), py::arg("current_order"), py::arg("new_order"));
     m.def("add_tensors", [](const tensor_t &a, const tensor_t &b) { return tensor_t::AddTensors(a, b); },
           py::arg("A"), py::arg("B"));
     m.def("contract_tensors",

@@ -8,3 +8,4 @@
 #include "jet/Tensor.hpp"
 #include "jet/TensorNetwork.hpp"
 #include "jet/Utilities.hpp"
+#include "jet/permute/Permuter.hpp"
