@@ -196,72 +196,100 @@ def run_ours(args, rank, world, local_rank):
     # torch.randn on complex draws re, im i.i.d. N(0, 1/2).
     A = torch.randn(m * k, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
     B = torch.randn(k * n, dtype=torch.complex64, device=dev, generator=g) * 2.0**-10
-    pa = torch.empty(4 * m * kp, dtype=torch.float32, device=dev)
-    bplanes = capi.tc_b_planes()
-    pb = torch.empty(bplanes * n * kp, dtype=torch.float32, device=dev)
     C = torch.empty(m * n, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
-
-    def step(events=None):
-        if events:
-            events[0].record(stream)
-        capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
-        if events:
-            events[1].record(stream)
-        capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, n_planes=bplanes,
-                        stream=stream)
-        if events:
-            events[2].record(stream)
-        capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
-        if events:
-            events[3].record(stream)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize(dev)
-    if capi.take_device_status() != 0:
-        raise RuntimeError("device status reports a timeout in the warm-up")
-
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize(dev)
-    with Clocks(local_rank) as clk:
-        t0 = time.perf_counter()
-        for s in range(args.steps):
-            step(evs[s])
-        torch.cuda.synchronize(dev)
-        wall = time.perf_counter() - t0
-    if world > 1:
-        torch.distributed.barrier()
-    clocks = clk.summary()
-    split_a = [e[0].elapsed_time(e[1]) for e in evs]
-    split_b = [e[1].elapsed_time(e[2]) for e in evs]
-    gemm = [e[2].elapsed_time(e[3]) for e in evs]
-    total = evs[0][0].elapsed_time(evs[-1][3])
-    ms_step = total / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
     flops = 8.0 * m * n * k  # = 4 x PathInfo flops (size(C) * 2 * K)
-    value = world * flops / (ms_step * 1e-3) / 1e12
 
-    # Accuracy of this step's C against complex128 on 32 rows.
+    # Accuracy of a step's C against complex128 on 32 rows.
     rows = 32
     At = capi.permute(A, w["a_shape"], w["a_perm"]).view(m, k)[:rows].cpu().numpy()
     Bt = capi.permute(B, w["b_shape"], w["b_perm_kn"]).view(k, n).cpu().numpy()
     ref_rows = At.astype(np.complex128) @ Bt.astype(np.complex128)
-    got_rows = C.view(m, n)[:rows].cpu().numpy()
-    rel_err = float(np.linalg.norm(got_rows - ref_rows) / np.linalg.norm(ref_rows))
+    del At, Bt
+
+    def rel_err_of(c):
+        got = c.view(m, n)[:rows].cpu().numpy()
+        return float(np.linalg.norm(got - ref_rows) / np.linalg.norm(ref_rows))
+
+    def run_form(form):
+        """Times `args.steps` steps of split A, split B, split product."""
+        bf = form == "bf16x3"
+        word = torch.int16 if bf else torch.float32
+        bplanes = 4 if bf else capi.tc_b_planes()
+        pa = torch.empty(4 * m * kp, dtype=word, device=dev)
+        pb = torch.empty(bplanes * n * kp, dtype=word, device=dev)
+
+        def step(events=None):
+            if events:
+                events[0].record(stream)
+            if bf:
+                capi.split_bf16(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
+            else:
+                capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
+            if events:
+                events[1].record(stream)
+            if bf:
+                capi.split_bf16(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, stream=stream)
+            else:
+                capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb,
+                                n_planes=bplanes, stream=stream)
+            if events:
+                events[2].record(stream)
+            if bf:
+                capi.gemm_bf16x3(pa, pb, m, n, k, kp, C, stream=stream)
+            else:
+                capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
+            if events:
+                events[3].record(stream)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize(dev)
+        if capi.take_device_status() != 0:
+            raise RuntimeError("device status reports a timeout in the warm-up")
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+               for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        with Clocks(local_rank) as clk:
+            t0 = time.perf_counter()
+            for s in range(args.steps):
+                step(evs[s])
+            torch.cuda.synchronize(dev)
+            wall = time.perf_counter() - t0
+        if world > 1:
+            torch.distributed.barrier()
+        ms_step = evs[0][0].elapsed_time(evs[-1][3]) / args.steps
+        if world > 1:
+            t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_step = float(t.item())
+        out = {"ms_per_step": ms_step, "value": world * flops / (ms_step * 1e-3) / 1e12,
+               "rel_err_vs_fp64": rel_err_of(C),
+               "stages_ms": {"split_a": statistics.mean(e[0].elapsed_time(e[1]) for e in evs),
+                             "split_b": statistics.mean(e[1].elapsed_time(e[2]) for e in evs),
+                             "gemm": statistics.mean(e[2].elapsed_time(e[3]) for e in evs)},
+               "clocks": clk.summary(), "wall_s_timed": wall}
+        del pa, pb
+        return out
+
+    forms = ["tf32x3", "bf16x3"] if args.form == "auto" else [args.form]
+    results = {f: run_form(f) for f in forms}
+    if args.form == "auto":
+        # The faster form if it meets the 1e-5 bound on this step, else TF32x3.
+        head = "bf16x3" if results["bf16x3"]["rel_err_vs_fp64"] <= 1e-5 else "tf32x3"
+    else:
+        head = args.form
+    hr = results[head]
     if args.kernels_only:
         if rank == 0:
-            print(json.dumps({"ms_per_step": ms_step, "value": value, "rel_err_vs_fp64": rel_err,
-                              "stages_ms": {"split_a": statistics.mean(split_a),
-                                            "split_b": statistics.mean(split_b),
-                                            "gemm_tf32x3": statistics.mean(gemm)},
-                              "m": m, "n": n, "k": k, "clocks": clocks}), flush=True)
+            print(json.dumps({"head": head, "forms": results, "m": m, "n": n, "k": k}),
+                  flush=True)
         return
+    ms_step, value, rel_err = hr["ms_per_step"], hr["value"], hr["rel_err_vs_fp64"]
+    clocks, wall = hr["clocks"], hr["wall_s_timed"]
+    head_prec = capi.PREC_BF16X3 if head == "bf16x3" else capi.PREC_TF32X3
 
     # Plain FP32 form of the same step (permute + SIMT complex GEMM), 2 runs.
     ws_need = capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
@@ -278,23 +306,22 @@ def run_ours(args, rank, world, local_rank):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     plain_ms = e0.elapsed_time(e1) / 2
-    plain_err = float(np.linalg.norm(C2.view(m, n)[:rows].cpu().numpy() - ref_rows)
-                      / np.linalg.norm(ref_rows))
+    plain_err = rel_err_of(C2)
     del ws, C2
 
     # End to end through the public API with host buffers: every step copies
     # its A and B from pinned host memory to the device, contracts them with
-    # jetgpu_contract (TF32x3) and copies C back to pinned host memory. Steps
+    # jetgpu_contract (the headline form) and copies C back to pinned host
+    # memory. Steps
     # are pipelined over two device buffer sets, so step i's uploads and step
     # i-1's download (copy streams) overlap step i-1's and i's contractions.
-    del pa, pb
     hA = A.cpu().pin_memory()
     hB = B.cpu().pin_memory()
     slots = [dict(a=torch.empty_like(A), b=torch.empty_like(B), c=torch.empty_like(C),
                   hc=torch.empty(C.shape, dtype=C.dtype).pin_memory()) for _ in range(2)]
     ws_tc = torch.empty(capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
                                                      w["b_perm_kn"], m, n, k, capi.C64,
-                                                     capi.PREC_TF32X3),
+                                                     head_prec),
                         dtype=torch.uint8, device=dev)
     cs_in = torch.cuda.Stream(dev)
     cs_out = torch.cuda.Stream(dev)
@@ -314,7 +341,7 @@ def run_ours(args, rank, world, local_rank):
         stream.wait_event(ev["in"][j])
         stream.wait_event(ev["out"][j])           # slot j's C read back by step i-2
         capi.contract(sl["a"], w["a_shape"], w["a_perm"], sl["b"], w["b_shape"], w["b_perm_kn"],
-                      m, n, k, precision=capi.PREC_TF32X3, out=sl["c"], workspace=ws_tc,
+                      m, n, k, precision=head_prec, out=sl["c"], workspace=ws_tc,
                       stream=stream)
         ev["comp"][j].record(stream)
         with torch.cuda.stream(cs_out):
@@ -334,35 +361,45 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_value = world * flops / (e2e_ms * 1e-3) / 1e12
+    e2e_err = rel_err_of(slots[(e2e_steps - 1) % 2]["hc"])
     del slots, ws_tc
 
     hbm_peak, bf16_peak, peak_src = measured_peaks()
-    tf32_peak = bf16_peak / 2.0
-    gemm_ms = statistics.mean(gemm)
-    split_ms = statistics.mean(split_a)
-    split_bytes = 24.0 * m * k  # A: read 8 B, write 4 planes x 4 B per element
+    # Dense tensor rate of the headline form's operand type: BF16 = measured
+    # bf16, TF32 = half of it.
+    tc_peak = bf16_peak if head == "bf16x3" else bf16_peak / 2.0
+    gemm_ms = hr["stages_ms"]["gemm"]
+    split_ms = hr["stages_ms"]["split_a"]
+    # A per element: read 8 B, write 4 planes x (2 B BF16 | 4 B TF32).
+    split_bytes = (16.0 if head == "bf16x3" else 24.0) * m * k
+    achieved = flops / (gemm_ms * 1e-3) / 1e12
+    form_names = {"tf32x3": "TF32x3 4M (tcgen05 kind::tf32, hi/lo split, 3 products)",
+                  "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)"}
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 (fp32 data, TF32x3 tensor-core products, fp32 accumulate)",
+        "dtype": "c64 (fp32 data, split-precision tensor-core products, fp32 accumulate)",
         "data": "synthetic (seeded N(0,1/2) * 2^-10 complex64)",
         "config": {"workload": "config 1: rank-27 x rank-25 contraction, 13 shared labels, "
                                "seeded label permutations (M=2^14, N=2^12, K=2^13)",
-                   "form": "TF32x3 4M", "l2": "inputs 1.34 GB > L2, no flush",
+                   "form": form_names[head], "l2": "inputs 1.34 GB > L2, no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "rel_err_vs_fp64": rel_err,
-        "stages_ms": {"split_a": split_ms, "split_b": statistics.mean(split_b),
-                      "gemm_tf32x3": gemm_ms},
+        "stages_ms": hr["stages_ms"],
+        "forms": {f: {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                      "rel_err_vs_fp64": r["rel_err_vs_fp64"], "stages_ms": r["stages_ms"]}
+                  for f, r in results.items()},
         "plain_fp32": {"ms_per_step": plain_ms,
                        "value": world * flops / (plain_ms * 1e-3) / 1e12,
                        "rel_err_vs_fp64": plain_err},
-        "roofline": {"bound": "tensor", "kernel": "tc_gemm_tf32x3_kernel",
-                     "achieved": flops / (gemm_ms * 1e-3) / 1e12,
-                     "peak": tf32_peak, "unit": "TFLOP/s",
-                     "frac": flops / (gemm_ms * 1e-3) / 1e12 / tf32_peak,
-                     "tensor_pipe_frac": 3 * flops / (gemm_ms * 1e-3) / 1e12 / tf32_peak,
-                     "peak_source": "TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak),
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_split_kernel<%d>" % (2 if head == "bf16x3" else 0),
+                     "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                     "frac": achieved / tc_peak,
+                     "tensor_pipe_frac": 3 * achieved / tc_peak,
+                     "peak_source": ("%s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak))
+                     if head == "bf16x3" else
+                     ("TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak)),
                      "traffic": None},
         "roofline_split": {"bound": "hbm", "kernel": "bitperm_kernel (split store)",
                            "achieved": split_bytes / (split_ms * 1e-3) / 1e9, "peak": hbm_peak,
@@ -372,6 +409,7 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": int(A.numel() * 8 + B.numel() * 8),
                 "d2h_bytes_per_step": int(C.numel() * 8), "ms_per_step": e2e_ms,
+                "rel_err_vs_fp64": e2e_err,
                 "pipeline": "two device buffer sets; H2D and D2H on copy streams overlap "
                             "the contractions"},
         "gpu_launches": 3 * args.steps,
@@ -586,6 +624,9 @@ def main():
                     help="skip the plain-FP32, end-to-end and CPU legs")
     ap.add_argument("--check-fp64", action="store_true",
                     help="sliced configs: also contract slice 0 in complex128")
+    ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3"],
+                    help="split form of the config-1 step (auto: both timed, the headline is "
+                         "BF16x3 when its error on the step is within 1e-5, else TF32x3)")
     ap.add_argument("--tc-variant", type=int, default=None,
                     help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",

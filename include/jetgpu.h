@@ -41,6 +41,8 @@ extern "C" {
 #define JETGPU_PREC_FP32 0   /* plain: complex FMA in the element type (FP32 or FP64) */
 #define JETGPU_PREC_TF32X3 1 /* tcgen05 kind::tf32, hi/lo split, 3 products, FP32 accumulate */
 #define JETGPU_PREC_AUTO 2   /* TF32x3 where the shape suits the tensor cores, else plain */
+#define JETGPU_PREC_BF16X3 3 /* tcgen05 kind::f16 on BF16 hi/lo splits, 3 products, FP32
+                                accumulate: twice the TF32 rate, ~2^-17 truncation per product */
 
 /* Complex product algorithms for the tensor-core form. */
 #define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
@@ -138,7 +140,8 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
  * dimensions. Replaces Tensor::ContractTensors (include/jet/Tensor.hpp:708-752)
  * after its label algebra; the label algebra stays on the host.
  *
- * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3 (complex64 only) or
+ * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3 or JETGPU_PREC_BF16X3
+ * (complex64 only; shapes with m or n below 2 take the plain form) or
  * JETGPU_PREC_AUTO. algo: JETGPU_ALGO_4M.
  * scale_a, scale_b: power-of-two exponents applied exactly to A and B before
  * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
@@ -250,6 +253,28 @@ int jetgpu_set_tc_variant(int wide);
 int jetgpu_tc_b_planes(void);
 
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
+                       uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
+                       float out_scale, void *stream);
+
+/*
+ * The two stages of the BF16x3 form (JETGPU_PREC_BF16X3).
+ *
+ * jetgpu_split_bf16: as jetgpu_split_tf32 with 16-bit BF16 words: plane p
+ * (0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo; hi = RN_bf16(x), lo = RN_bf16(x - hi),
+ * x = hi + lo + O(2^-17 |x|)) at planes + p * plane_stride words, row pitch
+ * `pitch` words (pitch >= cols, pitch % 8 == 0).
+ *
+ * jetgpu_gemm_bf16x3: C[m x n] = A * B^T from four BF16 planes of A (m x k)
+ * and of B (n x k) with row pitch kpitch words; tcgen05 kind::f16 (BF16 in,
+ * FP32 accumulate), three products per real product, output multiplied by
+ * `out_scale`. Replaces the cblas_cgemm call of TensorHelpers.hpp:47-61.
+ */
+int jetgpu_split_bf16(const void *in, int rank, const uint64_t *shape,
+                      const int32_t *perm, uint64_t rows, uint64_t cols,
+                      uint64_t pitch, uint64_t plane_stride, int scale_exp,
+                      uint16_t *planes, void *stream);
+
+int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                        float out_scale, void *stream);
 

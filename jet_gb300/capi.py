@@ -41,6 +41,7 @@ C128 = 1
 PREC_FP32 = 0
 PREC_TF32X3 = 1
 PREC_AUTO = 2
+PREC_BF16X3 = 3
 
 ALGO_4M = 0
 
@@ -67,6 +68,11 @@ lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   ctypes.c_int, _vp, _vp]
 lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
+lib.jetgpu_split_bf16.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                  _vp, _vp]
+lib.jetgpu_gemm_bf16x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
 lib.jetgpu_contract_batched_workspace_size.restype = ctypes.c_size_t
 lib.jetgpu_contract_batched_workspace_size.argtypes = [
@@ -231,6 +237,19 @@ def tc_b_planes() -> int:
 
 def gemm_tf32x3(a_planes, b_planes, m, n, k, kpitch, out, out_scale=1.0, stream=None):
     check(lib.jetgpu_gemm_tf32x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
+                                 out_scale, _stream(stream)))
+    return out
+
+
+def split_bf16(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, stream=None):
+    """Permute + BF16 hi/lo split into 4 planes of rows x pitch 16-bit words."""
+    check(lib.jetgpu_split_bf16(_ptr(x), len(shape), u64(shape), i32(perm), rows, cols, pitch,
+                                rows * pitch, scale_exp, _ptr(planes), _stream(stream)))
+    return planes
+
+
+def gemm_bf16x3(a_planes, b_planes, m, n, k, kpitch, out, out_scale=1.0, stream=None):
+    check(lib.jetgpu_gemm_bf16x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
                                  out_scale, _stream(stream)))
     return out
 

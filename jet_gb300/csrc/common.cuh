@@ -87,6 +87,19 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
                             uint64_t cols, uint64_t pitch, uint64_t plane_stride,
                             int scale_exp, cudaStream_t stream, int neg_im = 0);
 
+// Word format of the split planes: TF32 (FP32 words, 13 low mantissa bits
+// zero) or BF16 (16-bit words). pitch and plane_stride count words; a row
+// pitch must span a multiple of 16 bytes (SplitPitchAlign words).
+enum class SplitFormat { kTf32 = 0, kBf16 = 1 };
+inline uint64_t SplitWordBytes(SplitFormat f) { return f == SplitFormat::kBf16 ? 2 : 4; }
+inline uint64_t SplitPitchAlign(SplitFormat f) { return f == SplitFormat::kBf16 ? 8 : 4; }
+
+// PermuteSplitTf32Batched for either word format (neg_im with TF32 only).
+int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
+                       const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
+                       uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
+                       int neg_im, cudaStream_t stream);
+
 // C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
 // operand), C packed as batch x m x n.
 int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, uint64_t sa,
@@ -98,6 +111,12 @@ int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, 
 int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b_planes,
                             int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                             uint64_t k, uint64_t kpitch, float out_scale, cudaStream_t stream);
+
+// The batched split product for either word format (kpitch in words).
+int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
+                           int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
+                           uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
+                           cudaStream_t stream);
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,

@@ -7,9 +7,10 @@
 //
 // Plain form:  At = permute(A), Bt = permute(B) into the workspace (skipped
 //              when already ordered), then the SIMT complex product.
-// TF32x3 form: A is permuted straight into TF32 hi/lo planes (M x K), B into
-//              planes of its (right ++ common) order (N x K, K-major), then the
-//              tcgen05 product writes C.
+// Split form: A is permuted straight into hi/lo planes (M x K; TF32 words for
+//              TF32x3, BF16 words for BF16x3), B into planes of its
+//              (right ++ common) order (N x K, K-major), then the tcgen05
+//              product writes C.
 #include <vector>
 
 #include "common.cuh"
@@ -20,6 +21,27 @@ namespace {
 constexpr size_t kAlign = 256;
 
 inline size_t AlignUp(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Word format, row pitch and plane counts of the split form.
+struct SplitLayout {
+    SplitFormat fmt;
+    uint64_t kp;      // row pitch in words
+    uint64_t word;    // bytes per word
+    int b_planes;     // 4, or 6 for the N = 256 TF32 main loop
+    size_t a_bytes(uint64_t rows) const { return AlignUp(4 * rows * kp * word); }
+    size_t b_bytes(uint64_t rows) const { return AlignUp(b_planes * rows * kp * word); }
+};
+
+SplitLayout LayoutFor(int precision, uint64_t k)
+{
+    SplitLayout l;
+    l.fmt = precision == JETGPU_PREC_BF16X3 ? SplitFormat::kBf16 : SplitFormat::kTf32;
+    const uint64_t al = SplitPitchAlign(l.fmt);
+    l.kp = (k + al - 1) / al * al;
+    l.word = SplitWordBytes(l.fmt);
+    l.b_planes = (l.fmt == SplitFormat::kTf32 && TcWide()) ? 6 : 4;
+    return l;
+}
 
 bool IsIdentity(int rank, const int32_t *perm)
 {
@@ -91,8 +113,8 @@ size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
                                       int precision)
 {
     if (UseTensorCores(m, n, k, dtype, precision)) {
-        const uint64_t kp = (k + 3) / 4 * 4;
-        return AlignUp(4 * m * kp * sizeof(float)) + AlignUp(6 * n * kp * sizeof(float));
+        const SplitLayout l = LayoutFor(precision, k);
+        return l.a_bytes(m) + AlignUp((l.fmt == SplitFormat::kBf16 ? 4 : 6) * n * l.kp * l.word);
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -114,11 +136,12 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     JETGPU_REQUIRE(precision == JETGPU_PREC_FP32 || precision == JETGPU_PREC_TF32X3 ||
-                       precision == JETGPU_PREC_AUTO,
+                       precision == JETGPU_PREC_AUTO || precision == JETGPU_PREC_BF16X3,
                    "bad precision");
     JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
-    if (precision == JETGPU_PREC_TF32X3 && dtype != JETGPU_C64)
-        return SetError(JETGPU_ERR_UNSUPPORTED, "TF32x3 needs complex64 operands");
+    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3) &&
+        dtype != JETGPU_C64)
+        return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
     int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
     if (rc)
         return rc;
@@ -139,22 +162,23 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
     uint8_t *ws = static_cast<uint8_t *>(workspace);
 
     if (k > 0 && UseTensorCores(m, n, k, dtype, precision)) {
-        const uint64_t kp = (k + 3) / 4 * 4;
-        float *pa = reinterpret_cast<float *>(ws);
-        float *pb = reinterpret_cast<float *>(ws + AlignUp(4 * m * kp * sizeof(float)));
+        const SplitLayout l = LayoutFor(precision, k);
+        uint8_t *pa = ws;
+        uint8_t *pb = ws + l.a_bytes(m);
         // B is wanted as (right ++ common): rotate its (common ++ right) order.
         const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
         std::vector<int32_t> bt(b_rank);
         for (int j = 0; j < b_rank; ++j)
             bt[j] = b_perm[(j + nc) % b_rank];
-        rc = PermuteSplitTf32(A, pa, a_rank, a_shape, a_perm, m, k, kp, m * kp, scale_a, st);
+        rc = PermuteSplitPlanes(A, pa, 1, a_rank, a_shape, a_perm, m, k, l.kp, m * l.kp, scale_a,
+                                l.fmt, 0, st);
         if (rc)
             return rc;
-        rc = PermuteSplitTf32Batched(B, pb, 1, b_rank, b_shape, bt.data(), n, k, kp, n * kp,
-                                     scale_b, st, TcWide() ? 1 : 0);
+        rc = PermuteSplitPlanes(B, pb, 1, b_rank, b_shape, bt.data(), n, k, l.kp, n * l.kp,
+                                scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st);
         if (rc)
             return rc;
-        return GemmTf32x3Planar(pa, pb, C, m, n, k, kp, 1.0f, st);
+        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, 1.0f, l.fmt, st);
     }
 
     const size_t eb = ElemBytes(dtype);
@@ -204,6 +228,29 @@ int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C, ui
     ClearError();
     JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
     return GemmTf32x3Planar(a_planes, b_planes, C, m, n, k, kpitch, out_scale, AsStream(stream));
+}
+
+int jetgpu_split_bf16(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
+                      uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                      int scale_exp, uint16_t *planes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(pitch >= cols && pitch % 8 == 0, "pitch must be >= cols and a multiple of 8");
+    JETGPU_REQUIRE(plane_stride >= rows * pitch, "plane stride too small");
+    if (rows * cols == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
+    return PermuteSplitPlanes(in, planes, 1, rank, shape, perm, rows, cols, pitch, plane_stride,
+                              scale_exp, SplitFormat::kBf16, 0, AsStream(stream));
+}
+
+int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C, uint64_t m,
+                       uint64_t n, uint64_t k, uint64_t kpitch, float out_scale, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
+    return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
+                                  SplitFormat::kBf16, AsStream(stream));
 }
 
 } // extern "C"
@@ -265,9 +312,9 @@ size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const 
                                               b_perm, batch * m, n, k, dtype, precision);
     }
     if (p.tc) {
-        const uint64_t kp = (k + 3) / 4 * 4;
-        return AlignUp(4 * p.ba * m * kp * sizeof(float)) +
-               AlignUp(6 * p.bb * n * kp * sizeof(float));
+        const SplitLayout l = LayoutFor(precision, k);
+        return l.a_bytes(p.ba * m) +
+               AlignUp((l.fmt == SplitFormat::kBf16 ? 4 : 6) * p.bb * n * l.kp * l.word);
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -321,23 +368,23 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
     cudaStream_t st = AsStream(stream);
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc) {
-        const uint64_t kp = (k + 3) / 4 * 4;
-        float *pa = reinterpret_cast<float *>(ws);
-        float *pb = reinterpret_cast<float *>(ws + AlignUp(4 * p.ba * m * kp * sizeof(float)));
+        const SplitLayout l = LayoutFor(precision, k);
+        uint8_t *pa = ws;
+        uint8_t *pb = ws + l.a_bytes(p.ba * m);
         const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
         std::vector<int32_t> bt(b_rank);
         for (int j = 0; j < b_rank; ++j)
             bt[j] = b_perm[(j + nc) % b_rank];
-        rc = PermuteSplitTf32Batched(A, pa, p.ba, a_rank, a_shape, a_perm, m, k, kp,
-                                     p.ba * m * kp, scale_a, st);
+        rc = PermuteSplitPlanes(A, pa, p.ba, a_rank, a_shape, a_perm, m, k, l.kp,
+                                p.ba * m * l.kp, scale_a, l.fmt, 0, st);
         if (rc)
             return rc;
-        rc = PermuteSplitTf32Batched(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, kp,
-                                     p.bb * n * kp, scale_b, st, TcWide() ? 1 : 0);
+        rc = PermuteSplitPlanes(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, l.kp,
+                                p.bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st);
         if (rc)
             return rc;
-        return GemmTf32x3PlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, kp, 1.0f,
-                                       st);
+        return GemmSplitPlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, l.kp, 1.0f,
+                                      l.fmt, st);
     }
     const size_t eb = ElemBytes(dtype);
     const void *at = A;

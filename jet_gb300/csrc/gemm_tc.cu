@@ -1,21 +1,25 @@
-// Tensor-core complex product in split precision (3xTF32), sm_103a.
+// Tensor-core complex product in split precision (3xTF32 or 3xBF16), sm_103a.
 //
 // Replaces the cgemm of TensorHelpers::MultiplyTensorData
 // (include/jet/TensorHelpers.hpp:47-61, 147-152) for large steps.
 //
-// Operands arrive as planar TF32 splits written by PermuteSplitTf32:
+// Operands arrive as planar hi/lo splits written by PermuteSplitPlanes:
 //   A: planes {Ar_hi, Ar_lo, Ai_hi, Ai_lo}, each M x K (K contiguous)
 //   B: planes {Br_hi, Br_lo, Bi_hi, Bi_lo}, each N x K (K contiguous)
 // and the complex product uses four real products ("4M"), each as three
-// TF32 products (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM:
+// tensor-core products (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM:
 //   Cr += Ar Br - Ai Bi,   Ci += Ar Bi + Ai Br.
+// TF32 planes (FP32 words with 13 zero mantissa bits) leave a relative
+// truncation of about 2^-22 per product; BF16 planes (16-bit words, twice the
+// tensor rate and half the bytes) about 2^-17.
 //
 // One CTA computes a 128 x 128 complex tile. Warp 0 lane 0 feeds a 3-stage
-// ring of shared-memory stages with TMA (8 boxes of 128 rows x 16 floats,
-// 64-byte swizzle); warp 1 lane 0 issues tcgen05.mma (M=128, N=128, K=8) into
-// one of two TMEM accumulator sets (Cr, Ci: 2 x 256 columns) and releases
-// stages with tcgen05.commit; eight accumulator warps fold each finished
-// 128-deep K chunk into FP32 registers (see the kernel comment) and write C.
+// ring of shared-memory stages with TMA (8 boxes of 128 rows x 64 bytes,
+// 64-byte swizzle); warp 1 lane 0 issues tcgen05.mma (M=128, N=128, 32 bytes
+// of K per instruction: K=8 kind::tf32 or K=16 kind::f16) into one of two
+// TMEM accumulator sets (Cr, Ci: 2 x 256 columns) and releases stages with
+// tcgen05.commit; eight accumulator warps fold each finished K chunk into
+// FP32 registers (see the kernel comment) and write C.
 // Every mbarrier wait is bounded: on timeout the kernel records
 // JETGPU_ERR_TIMEOUT in a device status word, skips the remaining work,
 // frees its TMEM and returns.
@@ -38,26 +42,35 @@ constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
 
-// Two shapes of the main loop.
-//  narrow: 16-deep stages (64-byte rows, 64-byte swizzle), 3 stages of
-//          4 A + 4 B plane boxes; 24 MMAs of N = 128 per stage.
-//  wide:   8-deep stages (32-byte rows, 32-byte swizzle), 5 stages of 4 A
-//          boxes and two B triples [-Bi, Br, Bi] (hi, lo); 6 MMAs of
-//          N = 256 per stage: Ar [Br; Bi] -> [ArBr | ArBi] and
-//          Ai [-Bi; Br] -> [-AiBi | AiBr] land on (Cr | Ci) in one
-//          instruction each, halving the MMA count and cutting the shared
-//          memory read per flop by a quarter.
-template <bool kWide> struct TcCfg;
-template <> struct TcCfg<false> {
-    static constexpr int BK = 16, Stages = 3, Tiles = 8, ChunkStages = 8, RowBytes = 64;
-    static constexpr uint32_t SwizzleCode = 4; // 64-byte swizzle
+// Every stage holds boxes of 128 rows x 64 bytes (64-byte swizzle); every
+// MMA consumes 32 bytes of K per row, two per stage. Main-loop variants:
+//  0 TF32 narrow: 16-deep stages, 3 stages of 4 A + 4 B plane boxes; 12 MMAs
+//                 of N = 128 per k step.
+//  1 TF32 wide:   2 stages of 4 A boxes and two B triples [-Bi, Br, Bi]
+//                 (hi, lo); 6 MMAs of N = 256 per k step: Ar [Br; Bi] ->
+//                 [ArBr | ArBi] and Ai [-Bi; Br] -> [-AiBi | AiBr] land on
+//                 (Cr | Ci) in one instruction each.
+//  2 BF16 narrow: variant 0 with 32-deep stages of BF16 planes (kind::f16).
+// A chunk (the K extent accumulated in TMEM before the FP32 fold) is 128
+// deep in every variant.
+template <int V> struct TcCfg;
+template <> struct TcCfg<0> {
+    static constexpr bool Wide = false, Bf16 = false;
+    static constexpr int Stages = 3, Tiles = 8, ChunkStages = 8;
 };
-template <> struct TcCfg<true> {
-    static constexpr int BK = 8, Stages = 5, Tiles = 10, ChunkStages = 16, RowBytes = 32;
-    static constexpr uint32_t SwizzleCode = 6; // 32-byte swizzle
+template <> struct TcCfg<1> {
+    static constexpr bool Wide = true, Bf16 = false;
+    static constexpr int Stages = 2, Tiles = 10, ChunkStages = 8;
 };
-template <bool W> constexpr int TileBytes() { return kBM * TcCfg<W>::BK * 4; }
-template <bool W> constexpr int StageBytes() { return TcCfg<W>::Tiles * TileBytes<W>(); }
+template <> struct TcCfg<2> {
+    static constexpr bool Wide = false, Bf16 = true;
+    static constexpr int Stages = 3, Tiles = 8, ChunkStages = 4;
+};
+constexpr int kRowBytes = 64;
+constexpr int kTileBytes = kBM * kRowBytes;
+template <int V> constexpr int ElemBytes() { return TcCfg<V>::Bf16 ? 2 : 4; }
+template <int V> constexpr int BlockK() { return kRowBytes / ElemBytes<V>(); }
+template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * kTileBytes; }
 constexpr unsigned long long kWaitNs = 4000000000ull; // 4 s bound per wait
 
 __device__ __forceinline__ uint32_t SmemAddr(const void *p)
@@ -133,34 +146,46 @@ __device__ __forceinline__ void TmaLoad4d(uint32_t dst, const CUtensorMap *map,
                  : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, swizzled rows of
-// RowBytes, 8-row groups 8 * RowBytes apart.
-template <bool kWide> __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
+// Shared-memory matrix descriptor: K-major operand, 64-byte swizzled rows,
+// 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
 {
     uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);                       // start address
-    d |= (uint64_t)1 << 16;                                        // leading byte offset (unused)
-    d |= (uint64_t)((8 * TcCfg<kWide>::RowBytes) >> 4) << 32;      // stride byte offset
-    d |= (uint64_t)1 << 46;                                        // descriptor version
-    d |= (uint64_t)TcCfg<kWide>::SwizzleCode << 61;                // swizzle mode
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);         // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused)
+    d |= (uint64_t)((8 * kRowBytes) >> 4) << 32;     // stride byte offset
+    d |= (uint64_t)1 << 46;                          // descriptor version
+    d |= (uint64_t)4 << 61;                          // 64-byte swizzle
     return d;
 }
 
-// Instruction descriptor: D = F32, A = B = TF32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t InstrDesc(int m, int n, bool neg_a)
+// Instruction descriptor: D = F32, both operands K-major, M x N; operand
+// format 2 = TF32 (kind::tf32), 1 = BF16 (kind::f16). A and B share it.
+__host__ __device__ constexpr uint32_t InstrDesc(int m, int n, bool neg_a, bool bf16)
 {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((neg_a ? 1u : 0u) << 13) |
-           ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+    return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) |
+           ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ void MmaTf32(uint32_t d_tmem, uint64_t a, uint64_t b,
-                                        uint32_t idesc, uint32_t accumulate)
+template <bool kBf16>
+__device__ __forceinline__ void Mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                    uint32_t accumulate)
 {
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "setp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-                 "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-                 : "memory");
+    if constexpr (kBf16)
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "setp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                         d_tmem),
+                     "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                     : "memory");
+    else
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "setp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                         d_tmem),
+                     "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                     : "memory");
 }
 
 __device__ __forceinline__ void MmaCommit(uint32_t bar)
@@ -209,9 +234,9 @@ __device__ __forceinline__ void TmemWaitLoad()
 // into FP32 registers (round-to-nearest) while the next chunk accumulates in
 // the other set. Accumulator warp w (w = 2..9) owns TMEM lanes 32*(w%4)..+31
 // (tile rows) and columns [64*h, 64*h + 64) of Cr and Ci, h = (w - 2) / 4.
-template <bool kWide>
+template <int V>
 __global__ void __launch_bounds__(kThreads, 1)
-    tc_gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
+    tc_gemm_split_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles,
                           float scale, int a_batched, int b_batched)
@@ -220,12 +245,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
     const int bz = blockIdx.z;
     C += (size_t)bz * M * N;
-    using Cfg = TcCfg<kWide>;
-    constexpr int kBK = Cfg::BK;
+    using Cfg = TcCfg<V>;
+    constexpr bool kWide = Cfg::Wide;
+    constexpr bool kBf16 = Cfg::Bf16;
+    constexpr int kBK = BlockK<V>();
     constexpr int kStages = Cfg::Stages;
     constexpr int kChunkStages = Cfg::ChunkStages;
-    constexpr int kTileBytes = TileBytes<kWide>();
-    constexpr int kStageBytes = StageBytes<kWide>();
+    constexpr int kStageBytes = StageBytes<V>();
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
@@ -304,8 +330,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer.
-            constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false);
-            constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true);
+            constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false, kBf16);
+            constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kBf16);
             bool ok = true;
             for (int kt = 0; kt < ktiles && ok; ++kt) {
                 const int chunk = kt / kChunkStages;
@@ -328,54 +354,59 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t d_im = d_re + kBN;
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
                 if constexpr (kWide) {
-                    constexpr uint32_t kIdescW = InstrDesc(kBM, 2 * kBN, false);
-                    const uint64_t arh = SmemDesc<true>(base + 0 * kTileBytes);
-                    const uint64_t arl = SmemDesc<true>(base + 1 * kTileBytes);
-                    const uint64_t aih = SmemDesc<true>(base + 2 * kTileBytes);
-                    const uint64_t ail = SmemDesc<true>(base + 3 * kTileBytes);
-                    const uint64_t b_nr_hi = SmemDesc<true>(base + 4 * kTileBytes); // [-Bi; Br]
-                    const uint64_t b_rc_hi = SmemDesc<true>(base + 5 * kTileBytes); // [Br; Bi]
-                    const uint64_t b_nr_lo = SmemDesc<true>(base + 7 * kTileBytes);
-                    const uint64_t b_rc_lo = SmemDesc<true>(base + 8 * kTileBytes);
-                    const uint32_t acc = chunk_start ? 0u : 1u;
-                    // (Cr | Ci) += Ar [Br; Bi]
-                    MmaTf32(d_re, arh, b_rc_hi, kIdescW, acc);
-                    MmaTf32(d_re, arh, b_rc_lo, kIdescW, 1u);
-                    MmaTf32(d_re, arl, b_rc_hi, kIdescW, 1u);
-                    // (Cr | Ci) += Ai [-Bi; Br]
-                    MmaTf32(d_re, aih, b_nr_hi, kIdescW, 1u);
-                    MmaTf32(d_re, aih, b_nr_lo, kIdescW, 1u);
-                    MmaTf32(d_re, ail, b_nr_hi, kIdescW, 1u);
+                    constexpr uint32_t kIdescW = InstrDesc(kBM, 2 * kBN, false, kBf16);
+#pragma unroll
+                    for (int kk = 0; kk < kRowBytes / 32; ++kk) {
+                        const uint32_t koff = kk * 32; // 32 bytes of K per MMA
+                        const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
+                        const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
+                        const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
+                        const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
+                        // [-Bi; Br] starts at tile 4, [Br; Bi] at tile 5 (hi); 7, 8 (lo).
+                        const uint64_t b_nr_hi = SmemDesc(base + 4 * kTileBytes + koff);
+                        const uint64_t b_rc_hi = SmemDesc(base + 5 * kTileBytes + koff);
+                        const uint64_t b_nr_lo = SmemDesc(base + 7 * kTileBytes + koff);
+                        const uint64_t b_rc_lo = SmemDesc(base + 8 * kTileBytes + koff);
+                        const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
+                        // (Cr | Ci) += Ar [Br; Bi]
+                        Mma<kBf16>(d_re, arh, b_rc_hi, kIdescW, acc);
+                        Mma<kBf16>(d_re, arh, b_rc_lo, kIdescW, 1u);
+                        Mma<kBf16>(d_re, arl, b_rc_hi, kIdescW, 1u);
+                        // (Cr | Ci) += Ai [-Bi; Br]
+                        Mma<kBf16>(d_re, aih, b_nr_hi, kIdescW, 1u);
+                        Mma<kBf16>(d_re, aih, b_nr_lo, kIdescW, 1u);
+                        Mma<kBf16>(d_re, ail, b_nr_hi, kIdescW, 1u);
+                    }
                 }
                 else
 #pragma unroll
-                for (int kk = 0; kk < kBK / 8; ++kk) {
-                    const uint32_t koff = kk * 32; // 8 fp32 per MMA step
-                    const uint64_t arh = SmemDesc<false>(base + 0 * kTileBytes + koff);
-                    const uint64_t arl = SmemDesc<false>(base + 1 * kTileBytes + koff);
-                    const uint64_t aih = SmemDesc<false>(base + 2 * kTileBytes + koff);
-                    const uint64_t ail = SmemDesc<false>(base + 3 * kTileBytes + koff);
-                    const uint64_t brh = SmemDesc<false>(base + 4 * kTileBytes + koff);
-                    const uint64_t brl = SmemDesc<false>(base + 5 * kTileBytes + koff);
-                    const uint64_t bih = SmemDesc<false>(base + 6 * kTileBytes + koff);
-                    const uint64_t bil = SmemDesc<false>(base + 7 * kTileBytes + koff);
+                for (int kk = 0; kk < kRowBytes / 32; ++kk) {
+                    const uint32_t koff = kk * 32; // 32 bytes of K per MMA
+                    const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
+                    const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
+                    const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
+                    const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
+                    const uint64_t brh = SmemDesc(base + 4 * kTileBytes + koff);
+                    const uint64_t brl = SmemDesc(base + 5 * kTileBytes + koff);
+                    const uint64_t bih = SmemDesc(base + 6 * kTileBytes + koff);
+                    const uint64_t bil = SmemDesc(base + 7 * kTileBytes + koff);
                     const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                     // Cr += Ar Br
-                    MmaTf32(d_re, arh, brh, kIdesc, acc);
-                    MmaTf32(d_re, arh, brl, kIdesc, 1u);
-                    MmaTf32(d_re, arl, brh, kIdesc, 1u);
+                    Mma<kBf16>(d_re, arh, brh, kIdesc, acc);
+                    Mma<kBf16>(d_re, arh, brl, kIdesc, 1u);
+                    Mma<kBf16>(d_re, arl, brh, kIdesc, 1u);
                     // Cr -= Ai Bi
-                    MmaTf32(d_re, aih, bih, kIdescNeg, 1u);
-                    MmaTf32(d_re, aih, bil, kIdescNeg, 1u);
-                    MmaTf32(d_re, ail, bih, kIdescNeg, 1u);
+                    Mma<kBf16>(d_re, aih, bih, kIdescNeg, 1u);
+                    Mma<kBf16>(d_re, aih, bil, kIdescNeg, 1u);
+                    Mma<kBf16>(d_re, ail, bih, kIdescNeg, 1u);
                     // Ci += Ar Bi
-                    MmaTf32(d_im, arh, bih, kIdesc, acc);
-                    MmaTf32(d_im, arh, bil, kIdesc, 1u);
-                    MmaTf32(d_im, arl, bih, kIdesc, 1u);
+                    Mma<kBf16>(d_im, arh, bih, kIdesc, acc);
+                    Mma<kBf16>(d_im, arh, bil, kIdesc, 1u);
+                    Mma<kBf16>(d_im, arl, bih, kIdesc, 1u);
                     // Ci += Ai Br
-                    MmaTf32(d_im, aih, brh, kIdesc, 1u);
-                    MmaTf32(d_im, aih, brl, kIdesc, 1u);
-                    MmaTf32(d_im, ail, brh, kIdesc, 1u);
+                    Mma<kBf16>(d_im, aih, brh, kIdesc, 1u);
+                    Mma<kBf16>(d_im, aih, brl, kIdesc, 1u);
+                    Mma<kBf16>(d_im, ail, brh, kIdesc, 1u);
                 }
                 MmaCommit(SmemAddr(&empty_bar[s]));
                 if (chunk_end)
@@ -471,20 +502,20 @@ int GetEncoder()
     return JETGPU_OK;
 }
 
-// 3-D map over planes: (k, row, plane), box BK x 128 x 1.
-int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
-                 uint64_t kpitch, bool wide, int planes)
+// 3-D map over planes: (k, row, plane), box (64 bytes of k) x 128 x 1.
+int EncodePlanes(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
+                 uint64_t kpitch, bool bf16, int planes)
 {
+    const uint64_t eb = bf16 ? 2 : 4;
     cuuint64_t dims[3] = {k, rows, (cuuint64_t)planes};
-    cuuint64_t strides[2] = {kpitch * 4, rows * kpitch * 4};
-    cuuint32_t box[3] = {(cuuint32_t)(wide ? TcCfg<true>::BK : TcCfg<false>::BK), kBM, 1};
+    cuuint64_t strides[2] = {kpitch * eb, rows * kpitch * eb};
+    cuuint32_t box[3] = {(cuuint32_t)(kRowBytes / eb), kBM, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                          const_cast<float *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          wide ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = g_encode(map,
+                          bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          3, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return SetError(JETGPU_ERR_CUDA,
                         "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -492,51 +523,51 @@ int EncodePlanes(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
 }
 
 // 4-D map over batched planes laid out [plane][batch][rows][kpitch]:
-// (k, row, batch, plane), box BK x 128 x 1 x 1.
-int EncodePlanesBatched(CUtensorMap *map, const float *base, uint64_t rows, uint64_t k,
-                        uint64_t kpitch, uint64_t batch, bool wide, int planes)
+// (k, row, batch, plane), box (64 bytes of k) x 128 x 1 x 1.
+int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
+                        uint64_t kpitch, uint64_t batch, bool bf16, int planes)
 {
+    const uint64_t eb = bf16 ? 2 : 4;
     cuuint64_t dims[4] = {k, rows, batch, (cuuint64_t)planes};
-    cuuint64_t strides[3] = {kpitch * 4, rows * kpitch * 4, batch * rows * kpitch * 4};
-    cuuint32_t box[4] = {(cuuint32_t)(wide ? TcCfg<true>::BK : TcCfg<false>::BK), kBM, 1, 1};
+    cuuint64_t strides[3] = {kpitch * eb, rows * kpitch * eb, batch * rows * kpitch * eb};
+    cuuint32_t box[4] = {(cuuint32_t)(kRowBytes / eb), kBM, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
-                          const_cast<float *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          wide ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = g_encode(map,
+                          bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          4, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return SetError(JETGPU_ERR_CUDA,
                         "cuTensorMapEncodeTiled (4-D) failed: " + std::to_string((int)r));
     return JETGPU_OK;
 }
 
-template <bool kWide>
+template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
              cudaStream_t stream)
 {
-    const size_t smem = (size_t)TcCfg<kWide>::Stages * StageBytes<kWide>() + 1024;
+    const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + 1024;
     static thread_local int configured_dev = -1;
     int dev = 0;
     JETGPU_CUDA_TRY(cudaGetDevice(&dev));
     if (configured_dev != dev) {
-        JETGPU_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel<kWide>,
+        JETGPU_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_split_kernel<V>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem));
         configured_dev = dev;
     }
     dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM),
               (unsigned)batch);
-    const int ktiles = (int)((k + TcCfg<kWide>::BK - 1) / TcCfg<kWide>::BK);
-    tc_gemm_tf32x3_kernel<kWide><<<grid, kThreads, smem, stream>>>(
+    const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
+    tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
         b_batched);
-    return CheckLaunch("tc_gemm_tf32x3_kernel");
+    return CheckLaunch("tc_gemm_split_kernel");
 }
 
-int g_tc_wide = 0; // main-loop shape of the tensor-core product (jetgpu_set_tc_variant)
+int g_tc_wide = 0; // main-loop shape of the TF32 product (jetgpu_set_tc_variant)
 
 } // namespace
 
@@ -544,23 +575,33 @@ int GemmTf32x3Planar(const float *a_planes, const float *b_planes, void *C,
                      uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                      float out_scale, cudaStream_t stream)
 {
-    return GemmTf32x3PlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
-                                   stream);
+    return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
+                                  SplitFormat::kTf32, stream);
 }
 
 int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b_planes,
                             int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                             uint64_t k, uint64_t kpitch, float out_scale, cudaStream_t stream)
 {
+    return GemmSplitPlanarBatched(a_planes, a_batched, b_planes, b_batched, C, batch, m, n, k,
+                                  kpitch, out_scale, SplitFormat::kTf32, stream);
+}
+
+int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
+                           int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
+                           uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
+                           cudaStream_t stream)
+{
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
         a_batched = 0;
         b_batched = 0;
     }
+    const bool bf16 = fmt == SplitFormat::kBf16;
     JETGPU_REQUIRE(m > 0 && n > 0 && k > 0, "empty product");
     JETGPU_REQUIRE(m < (1ull << 31) && n < (1ull << 31) && k < (1ull << 31),
                    "dimension too large");
-    JETGPU_REQUIRE(kpitch >= k && kpitch % 4 == 0, "bad k pitch");
+    JETGPU_REQUIRE(kpitch >= k && kpitch % SplitPitchAlign(fmt) == 0, "bad k pitch");
     JETGPU_REQUIRE(((uintptr_t)a_planes % 16) == 0 && ((uintptr_t)b_planes % 16) == 0,
                    "planes must be 16-byte aligned");
     JETGPU_REQUIRE((n + kBN - 1) / kBN <= 0x7fffffffull && (m + kBM - 1) / kBM <= 65535ull,
@@ -570,19 +611,20 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
     int rc = GetEncoder();
     if (rc)
         return rc;
-    const bool wide = g_tc_wide != 0;
+    const bool wide = !bf16 && g_tc_wide != 0;
     CUtensorMap ta, tb;
-    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, wide, 4)
-                        : EncodePlanes(&ta, a_planes, m, k, kpitch, wide, 4)))
+    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, bf16, 4)
+                        : EncodePlanes(&ta, a_planes, m, k, kpitch, bf16, 4)))
         return rc;
     const int bplanes = wide ? 6 : 4;
-    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, wide, bplanes)
-                        : EncodePlanes(&tb, b_planes, n, k, kpitch, wide, bplanes)))
+    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, bf16, bplanes)
+                        : EncodePlanes(&tb, b_planes, n, k, kpitch, bf16, bplanes)))
         return rc;
-    return wide ? LaunchTc<true>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
-                                 stream)
-                : LaunchTc<false>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
-                                  stream);
+    if (bf16)
+        return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
+    return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream)
+                : LaunchTc<0>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
+                              stream);
 }
 
 bool TcWide() { return g_tc_wide != 0; }

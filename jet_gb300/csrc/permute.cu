@@ -140,13 +140,31 @@ __device__ __forceinline__ float RoundTf32(float x)
     return __uint_as_float((u + 0x1000u) & 0xffffe000u);
 }
 
+// BF16 rounding to nearest, ties to even: add 0x7fff plus the lowest kept
+// bit, then drop the 16 low bits. Returns the BF16 word.
+__device__ __forceinline__ uint32_t Bf16Bits(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7f800000u) == 0x7f800000u) // inf stays inf, nan stays (quiet) nan
+        return (u >> 16) | ((u & 0x7fffffu) ? 0x40u : 0u);
+    return (u + 0x7fffu + ((u >> 16) & 1u)) >> 16;
+}
+
+// hi = RN_bf16(x), lo = RN_bf16(x - hi); x - hi is exact in FP32.
+__device__ __forceinline__ void SplitBf16(float x, uint32_t &hi, uint32_t &lo)
+{
+    hi = Bf16Bits(x);
+    lo = Bf16Bits(x - __uint_as_float(hi << 16));
+}
+
 struct SplitOut {
-    float *planes;         // 4 planes, or 6 with the negated imaginary pair
-    uint64_t plane_stride; // floats between planes
+    void *planes;          // 4 planes, or 6 with the negated imaginary pair
+    uint64_t plane_stride; // words between planes
     uint64_t cols;         // logical columns of the permuted view
-    uint64_t pitch;        // floats per row in a plane
+    uint64_t pitch;        // words per row in a plane
     float scale;           // exact power of two
-    int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo
+    int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo (TF32)
+    int bf16;              // 16-bit BF16 words instead of TF32-in-FP32 words
 };
 
 __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
@@ -156,15 +174,27 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
     uint64_t col = o - row * so.cols;
     uint64_t off = row * so.pitch + col;
     float re = v.x * so.scale, im = v.y * so.scale;
+    if (so.bf16) {
+        uint16_t *pl = static_cast<uint16_t *>(so.planes);
+        uint32_t rh, rl, ih, il;
+        SplitBf16(re, rh, rl);
+        SplitBf16(im, ih, il);
+        pl[off] = (uint16_t)rh;
+        pl[off + so.plane_stride] = (uint16_t)rl;
+        pl[off + 2 * so.plane_stride] = (uint16_t)ih;
+        pl[off + 3 * so.plane_stride] = (uint16_t)il;
+        return;
+    }
+    float *planes = static_cast<float *>(so.planes);
     float rh = RoundTf32(re), ih = RoundTf32(im);
     float rl = RoundTf32(re - rh), il = RoundTf32(im - ih);
-    so.planes[off] = rh;
-    so.planes[off + so.plane_stride] = rl;
-    so.planes[off + 2 * so.plane_stride] = ih;
-    so.planes[off + 3 * so.plane_stride] = il;
+    planes[off] = rh;
+    planes[off + so.plane_stride] = rl;
+    planes[off + 2 * so.plane_stride] = ih;
+    planes[off + 3 * so.plane_stride] = il;
     if (so.neg_im) {
-        so.planes[off + 4 * so.plane_stride] = -ih;
-        so.planes[off + 5 * so.plane_stride] = -il;
+        planes[off + 4 * so.plane_stride] = -ih;
+        planes[off + 5 * so.plane_stride] = -il;
     }
 }
 
@@ -256,7 +286,7 @@ template <typename E> struct PlainStore {
     }
 };
 
-// Store stage functor: TF32 hi/lo planes (complex64 only, 2 elements).
+// Store stage functor: hi/lo planes (complex64 only, 2 elements).
 struct SplitStore {
     SplitOut so;
     __device__ __forceinline__ void operator()(uint64_t off, const uint2 *v,
@@ -270,20 +300,35 @@ struct SplitStore {
         float2 b = make_float2(__uint_as_float(v[1].x), __uint_as_float(v[1].y));
         float ar = a.x * so.scale, ai = a.y * so.scale;
         float br = b.x * so.scale, bi = b.y * so.scale;
+        if (so.bf16) {
+            // Two BF16 words per plane: one 4-byte store (base is even).
+            uint16_t *pl = static_cast<uint16_t *>(so.planes);
+            uint32_t arh, arl, aih, ail, brh, brl, bih, bil;
+            SplitBf16(ar, arh, arl);
+            SplitBf16(ai, aih, ail);
+            SplitBf16(br, brh, brl);
+            SplitBf16(bi, bih, bil);
+            *reinterpret_cast<uint32_t *>(pl + base) = arh | (brh << 16);
+            *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = arl | (brl << 16);
+            *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = aih | (bih << 16);
+            *reinterpret_cast<uint32_t *>(pl + base + 3 * so.plane_stride) = ail | (bil << 16);
+            return;
+        }
+        float *planes = static_cast<float *>(so.planes);
         float arh = RoundTf32(ar), aih = RoundTf32(ai);
         float brh = RoundTf32(br), bih = RoundTf32(bi);
         float2 rh = make_float2(arh, brh);
         float2 rl = make_float2(RoundTf32(ar - arh), RoundTf32(br - brh));
         float2 ih = make_float2(aih, bih);
         float2 il = make_float2(RoundTf32(ai - aih), RoundTf32(bi - bih));
-        *reinterpret_cast<float2 *>(so.planes + base) = rh;
-        *reinterpret_cast<float2 *>(so.planes + base + so.plane_stride) = rl;
-        *reinterpret_cast<float2 *>(so.planes + base + 2 * so.plane_stride) = ih;
-        *reinterpret_cast<float2 *>(so.planes + base + 3 * so.plane_stride) = il;
+        *reinterpret_cast<float2 *>(planes + base) = rh;
+        *reinterpret_cast<float2 *>(planes + base + so.plane_stride) = rl;
+        *reinterpret_cast<float2 *>(planes + base + 2 * so.plane_stride) = ih;
+        *reinterpret_cast<float2 *>(planes + base + 3 * so.plane_stride) = il;
         if (so.neg_im) {
-            *reinterpret_cast<float2 *>(so.planes + base + 4 * so.plane_stride) =
+            *reinterpret_cast<float2 *>(planes + base + 4 * so.plane_stride) =
                 make_float2(-ih.x, -ih.y);
-            *reinterpret_cast<float2 *>(so.planes + base + 5 * so.plane_stride) =
+            *reinterpret_cast<float2 *>(planes + base + 5 * so.plane_stride) =
                 make_float2(-il.x, -il.y);
         }
     }
@@ -532,6 +577,16 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
                             uint64_t cols, uint64_t pitch, uint64_t plane_stride,
                             int scale_exp, cudaStream_t stream, int neg_im)
 {
+    return PermuteSplitPlanes(in, planes, batch, rank, shape, perm, rows, cols, pitch,
+                              plane_stride, scale_exp, SplitFormat::kTf32, neg_im, stream);
+}
+
+int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
+                       const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
+                       uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
+                       int neg_im, cudaStream_t stream)
+{
+    JETGPU_REQUIRE(!(neg_im && fmt == SplitFormat::kBf16), "negated planes are TF32 only");
     Simplified s;
     int rc = Simplify(rank, shape, perm, s);
     if (rc)
@@ -549,6 +604,7 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
     so.pitch = pitch;
     so.scale = ldexpf(1.0f, scale_exp);
     so.neg_im = neg_im;
+    so.bf16 = fmt == SplitFormat::kBf16 ? 1 : 0;
     const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
                          (pitch % 2 == 0) && (plane_stride % 2 == 0);
     static thread_local BitParams bp;
