@@ -188,6 +188,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(dev)
     if args.tc_variant is not None:
         capi.set_tc_variant(args.tc_variant)
+    if args.tc_chunk is not None:
+        capi.set_tc_chunk_depth(args.tc_chunk)
     w = workload(12, N_COMMON, 12) if args.small else workload()
     m, n, k = w["m"], w["n"], w["k"]
     kp = k
@@ -465,7 +467,9 @@ def run_sliced(args, rank, world, local_rank):
         tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
     forms = {}
     amps = {}
-    for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+    sliced_forms = (("auto", jet.PREC_AUTO), ("bf16x3", jet.PREC_BF16X3),
+                    ("fp32", jet.PREC_FP32))
+    for name, prec in sliced_forms:
         sc = jet.SlicedContractorC64(tn, path, sliced, prec)
         sc.set_batch_size(batch)
         n_all = sc.num_slices
@@ -487,6 +491,7 @@ def run_sliced(args, rank, world, local_rank):
         dep_flops = sc.slice_dependent_flops
         del sc
     rel = abs(amps["auto"] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
+    rel_bf = abs(amps["bf16x3"] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
     # One slice in complex128 (FP64 arithmetic on the GPU) as the reference
     # for the per-slice error of both complex64 forms.
     slice_check = None
@@ -500,7 +505,7 @@ def run_sliced(args, rank, world, local_rank):
         del sc
         slice_check = {"reference": "complex128 FP64 on the GPU, slice 0",
                        "value": [ref64.real, ref64.imag]}
-        for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+        for name, prec in sliced_forms:
             sc = jet.SlicedContractorC64(tn, path, sliced, prec)
             sc.set_batch_size(1)
             v = sc.contract(0, 1)[0]
@@ -522,6 +527,7 @@ def run_sliced(args, rank, world, local_rank):
         "slice_flops_pathinfo": slice_flops, "slice_dependent_flops": dep_flops,
         "amplitude_sample": [amps["auto"].real, amps["auto"].imag],
         "rel_diff_auto_vs_fp32": rel,
+        "rel_diff_bf16x3_vs_fp32": rel_bf,
         "slice_vs_fp64": slice_check,
         "plan_seconds": plan_s,
     }
@@ -627,6 +633,8 @@ def main():
     ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3"],
                     help="split form of the config-1 step (auto: both timed, the headline is "
                          "BF16x3 when its error on the step is within 1e-5, else TF32x3)")
+    ap.add_argument("--tc-chunk", type=int, default=None,
+                    help="K depth accumulated in tensor memory per fold (0 = defaults)")
     ap.add_argument("--tc-variant", type=int, default=None,
                     help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",

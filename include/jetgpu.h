@@ -252,6 +252,17 @@ int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape,
 int jetgpu_set_tc_variant(int wide);
 int jetgpu_tc_b_planes(void);
 
+/*
+ * jetgpu_set_tc_chunk_depth sets, for the calling process, the K depth the
+ * tensor-core products accumulate in tensor memory before folding the partial
+ * sum into FP32 registers (round to nearest); 0 restores the defaults (16 for
+ * TF32x3, 128 for BF16x3). The tensor core's own accumulation loses accuracy
+ * with the depth it accumulates: shorter chunks are more accurate, longer
+ * ones fold less often. Rounded down to whole stages (16 k for TF32, 32 for
+ * BF16), at least one stage.
+ */
+int jetgpu_set_tc_chunk_depth(int k_depth);
+
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                        float out_scale, void *stream);

@@ -67,6 +67,7 @@ lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                   ctypes.c_int, _vp, _vp]
 lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
+lib.jetgpu_set_tc_chunk_depth.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
 lib.jetgpu_split_bf16.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
@@ -229,6 +230,11 @@ def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, n_planes=
 def set_tc_variant(wide: int) -> None:
     """0: N = 128 tensor-core main loop; 1: N = 256 (six B planes)."""
     check(lib.jetgpu_set_tc_variant(int(wide)))
+
+
+def set_tc_chunk_depth(k_depth: int) -> None:
+    """K depth accumulated in tensor memory per fold (0 = defaults)."""
+    check(lib.jetgpu_set_tc_chunk_depth(int(k_depth)))
 
 
 def tc_b_planes() -> int:

@@ -41,6 +41,7 @@ constexpr int kBN = 128;
 constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
+constexpr int kGroupM = 8;                    // tile rows per group of the tile order
 
 // Every stage holds boxes of 128 rows x 64 bytes (64-byte swizzle); every
 // MMA consumes 32 bytes of K per row, two per stage. Main-loop variants:
@@ -51,26 +52,45 @@ constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
 //                 [ArBr | ArBi] and Ai [-Bi; Br] -> [-AiBi | AiBr] land on
 //                 (Cr | Ci) in one instruction each.
 //  2 BF16 narrow: variant 0 with 32-deep stages of BF16 planes (kind::f16).
-// A chunk (the K extent accumulated in TMEM before the FP32 fold) is 128
-// deep in every variant.
+// A chunk is the K extent accumulated in TMEM before the FP32 fold, in
+// stages (a kernel argument; see the kernel comment).
 template <int V> struct TcCfg;
 template <> struct TcCfg<0> {
     static constexpr bool Wide = false, Bf16 = false;
-    static constexpr int Stages = 3, Tiles = 8, ChunkStages = 8;
+    static constexpr int Stages = 3, Tiles = 8;
 };
 template <> struct TcCfg<1> {
     static constexpr bool Wide = true, Bf16 = false;
-    static constexpr int Stages = 2, Tiles = 10, ChunkStages = 8;
+    static constexpr int Stages = 2, Tiles = 10;
 };
 template <> struct TcCfg<2> {
     static constexpr bool Wide = false, Bf16 = true;
-    static constexpr int Stages = 3, Tiles = 8, ChunkStages = 4;
+    static constexpr int Stages = 3, Tiles = 8;
 };
 constexpr int kRowBytes = 64;
 constexpr int kTileBytes = kBM * kRowBytes;
 template <int V> constexpr int ElemBytes() { return TcCfg<V>::Bf16 ? 2 : 4; }
 template <int V> constexpr int BlockK() { return kRowBytes / ElemBytes<V>(); }
 template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * kTileBytes; }
+
+// Default K depth accumulated in TMEM per chunk. TF32: 16, one fold per
+// stage. The tensor core's accumulation rounds magnitudes toward zero, so its
+// error does not average out along a network: measured on a 53-qubit sliced
+// circuit amplitude (AUTO form), depth 16 / 32 / 64 / 128 gave relative
+// errors 7.0e-6 / 1.0e-5 / 1.2e-5 / 1.9e-5 against FP64, at 1.10 / 1.04 /
+// 1.01 / 1.00 times the depth-128 product time. BF16: 128, since its split
+// truncation (about 4.5e-6 per product) dominates any accumulation error.
+constexpr int kDefaultChunkKTf32 = 16;
+constexpr int kDefaultChunkKBf16 = 128;
+int g_tc_chunk_k = 0; // K depth per TMEM chunk (jetgpu_set_tc_chunk_depth; 0 = default)
+
+inline int ChunkStages(bool bf16)
+{
+    const int stage_k = bf16 ? BlockK<2>() : BlockK<0>();
+    int depth = g_tc_chunk_k > 0 ? g_tc_chunk_k : (bf16 ? kDefaultChunkKBf16 : kDefaultChunkKTf32);
+    int stages = depth / stage_k;
+    return stages < 1 ? 1 : stages;
+}
 constexpr unsigned long long kWaitNs = 4000000000ull; // 4 s bound per wait
 
 __device__ __forceinline__ uint32_t SmemAddr(const void *p)
@@ -227,19 +247,23 @@ __device__ __forceinline__ void TmemWaitLoad()
 
 // Warp roles: warp 0 issues TMA loads, warp 1 allocates TMEM and issues the
 // MMAs, warps 2..9 ("accumulator warps") drain finished K chunks from TMEM.
-// Precision: the tensor core rounds its FP32 accumulator at every MMA
-// instruction, so a long K makes the rounding error grow with K. The MMAs
-// therefore accumulate only kChunkStages stages (128 complex k) into one of
-// two TMEM accumulator sets; the accumulator warps add every finished chunk
-// into FP32 registers (round-to-nearest) while the next chunk accumulates in
-// the other set. Accumulator warp w (w = 2..9) owns TMEM lanes 32*(w%4)..+31
+// Precision: the tensor core's FP32 accumulation in TMEM loses accuracy with
+// every MMA it adds (measured: the output-relative error of a 3xTF32 product
+// grows with the K depth accumulated in TMEM, 5e-7 at 16 and 1.9e-6 at 128,
+// independent of cancellation), so the MMAs accumulate only `chunk_stages`
+// stages into one of two TMEM accumulator sets; the accumulator warps add
+// every finished chunk into FP32 registers (round-to-nearest) while the next
+// chunk accumulates in the other set. Accumulator warp w (w = 2..9) owns TMEM lanes 32*(w%4)..+31
 // (tile rows) and columns [64*h, 64*h + 64) of Cr and Ci, h = (w - 2) / 4.
+// Register budget: the ten warps spread over the SM's four register-file
+// partitions (16K registers each) three to a partition at most, so a thread
+// gets at most 168 registers (a few bytes of the epilogue spill).
 template <int V>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_split_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles,
-                          float scale, int a_batched, int b_batched)
+                          float scale, int a_batched, int b_batched, int chunk_stages)
 {
     // Batch b = blockIdx.z: a batched operand is read through a 4-D map
     // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
@@ -250,7 +274,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr bool kBf16 = Cfg::Bf16;
     constexpr int kBK = BlockK<V>();
     constexpr int kStages = Cfg::Stages;
-    constexpr int kChunkStages = Cfg::ChunkStages;
     constexpr int kStageBytes = StageBytes<V>();
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
@@ -263,9 +286,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * kBM;
-    const int n0 = blockIdx.x * kBN;
-    const int nchunks = (ktiles + kChunkStages - 1) / kChunkStages;
+    // Grouped tile order: consecutive CTAs walk kGroupM tile rows down one
+    // tile column before moving to the next column, so the CTAs resident at
+    // one time cover a compact block of C (about 8 x 19 tiles on 152 SMs) and
+    // share their A and B tiles through L2 instead of each tile row
+    // streaming all of B from HBM.
+    const int n_tiles = (N + kBN - 1) / kBN;
+    const int m_tiles = (M + kBM - 1) / kBM;
+    const int span = kGroupM * n_tiles;
+    const int group = (int)blockIdx.x / span;
+    const int first_m = group * kGroupM;
+    const int gm = min(kGroupM, m_tiles - first_m);
+    const int in_group = (int)blockIdx.x - group * span;
+    const int m0 = (first_m + in_group % gm) * kBM;
+    const int n0 = (in_group / gm) * kBN;
+    const int nchunks = (ktiles + chunk_stages - 1) / chunk_stages;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -334,10 +369,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kBf16);
             bool ok = true;
             for (int kt = 0; kt < ktiles && ok; ++kt) {
-                const int chunk = kt / kChunkStages;
+                const int chunk = kt / chunk_stages;
                 const int buf = chunk & 1;
-                const bool chunk_start = (kt % kChunkStages) == 0;
-                const bool chunk_end = (kt % kChunkStages) == kChunkStages - 1 || kt == ktiles - 1;
+                const int in_chunk = kt - chunk * chunk_stages;
+                const bool chunk_start = in_chunk == 0;
+                const bool chunk_end = in_chunk == chunk_stages - 1 || kt == ktiles - 1;
                 if (chunk_start &&
                     !MbarWait(SmemAddr(&acc_empty[buf]), ((uint32_t)(chunk >> 1) & 1u) ^ 1u)) {
                     ok = false;
@@ -558,12 +594,12 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
                                              (int)smem));
         configured_dev = dev;
     }
-    dim3 grid((unsigned)((n + kBN - 1) / kBN), (unsigned)((m + kBM - 1) / kBM),
-              (unsigned)batch);
+    // One CTA per 128 x 128 tile of C in the grouped order, blockIdx.z = batch.
+    dim3 grid((unsigned)(((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM)), 1, (unsigned)batch);
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
-        b_batched);
+        b_batched, ChunkStages(TcCfg<V>::Bf16));
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
@@ -604,7 +640,7 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
     JETGPU_REQUIRE(kpitch >= k && kpitch % SplitPitchAlign(fmt) == 0, "bad k pitch");
     JETGPU_REQUIRE(((uintptr_t)a_planes % 16) == 0 && ((uintptr_t)b_planes % 16) == 0,
                    "planes must be 16-byte aligned");
-    JETGPU_REQUIRE((n + kBN - 1) / kBN <= 0x7fffffffull && (m + kBM - 1) / kBM <= 65535ull,
+    JETGPU_REQUIRE(((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM) <= 0x7fffffffull,
                    "grid too large");
     if (!TcAvailable())
         return SetError(JETGPU_ERR_UNSUPPORTED, "tensor-core path needs an sm_103 device");
@@ -638,6 +674,14 @@ extern "C" int jetgpu_set_tc_variant(int wide)
     jetgpu::ClearError();
     JETGPU_REQUIRE(wide == 0 || wide == 1, "variant must be 0 (N = 128) or 1 (N = 256)");
     jetgpu::g_tc_wide = wide;
+    return JETGPU_OK;
+}
+
+extern "C" int jetgpu_set_tc_chunk_depth(int k_depth)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(k_depth >= 0 && k_depth <= 4096, "chunk depth out of range");
+    jetgpu::g_tc_chunk_k = k_depth;
     return JETGPU_OK;
 }
 

@@ -47,3 +47,12 @@ def test_contract_rejects_tf32_for_complex128():
                                   capi.u64([2]), capi.i32([0]), None, 1, 1, 2, capi.C128,
                                   capi.PREC_TF32X3, capi.ALGO_4M, 0, 0, None, 0, None)
     assert rc == capi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("depth", [-1, 4097])
+def test_chunk_depth_rejects_out_of_range(depth):
+    from jet_gb300 import capi
+
+    assert capi.lib.jetgpu_set_tc_chunk_depth(depth) == capi.ERR_INVALID
+    assert b"chunk depth" in capi.lib.jetgpu_last_error()
+    assert capi.lib.jetgpu_set_tc_chunk_depth(0) == capi.OK

@@ -185,3 +185,30 @@ def test_power_of_two_scales(cuda, tc_variant):
         out = capi.contract(_dev(a, cuda), [m, k], [0, 1], _dev(b, cuda), [k, n], [0, 1], m, n, k,
                             precision=prec, scale_a=20, scale_b=-7).cpu().numpy().reshape(m, n)
         assert _rel(out, want) <= 1e-5
+
+
+def test_tmem_chunk_depth_controls_accumulation_error(cuda):
+    """The K depth accumulated in tensor memory per fold: shorter is more
+    accurate (3xTF32, k = 4096, config-1 data); the default is 16."""
+    from jet_gb300 import capi
+
+    m, n, k = 512, 256, 4096
+    rng = np.random.default_rng(17)
+    a = ((rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))) * np.sqrt(0.5)
+         * 2**-10).astype(np.complex64)
+    b = ((rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))) * np.sqrt(0.5)
+         * 2**-10).astype(np.complex64)
+    want = a.astype(np.complex128) @ b.astype(np.complex128)
+    errs = {}
+    try:
+        for depth in (0, 16, 128):
+            capi.set_tc_chunk_depth(depth)
+            out = capi.contract(_dev(a.reshape(-1), cuda), [m, k], [0, 1],
+                                _dev(b.reshape(-1), cuda), [k, n], [0, 1], m, n, k,
+                                precision=capi.PREC_TF32X3).cpu().numpy().reshape(m, n)
+            errs[depth] = _rel(out, want)
+    finally:
+        capi.set_tc_chunk_depth(0)
+    assert errs[0] == errs[16]
+    assert errs[16] < errs[128]
+    assert errs[16] <= 1e-6, errs

@@ -148,3 +148,51 @@ def test_open_result_indices(jet):
     assert sorted(labels) == sorted(want.indices)
     wt = jo.transpose(want, labels).data
     assert np.linalg.norm(got - wt) <= 1e-5 * np.linalg.norm(wt)
+
+
+def _steps_mnk(net, path):
+    """(m, n, k) of every pairwise step of `path` (ContractTensors label algebra)."""
+    nodes = [(list(lab), list(sh)) for lab, sh, _ in net.tensors]
+    out = []
+    for a, b in path:
+        (la, sa), (lb, sb) = nodes[a], nodes[b]
+        ad, bd = dict(zip(la, sa)), dict(zip(lb, sb))
+        left = [x for x in la if x not in lb]
+        right = [x for x in lb if x not in la]
+        common = [x for x in la if x in lb]
+        m = int(np.prod([ad[x] for x in left])) if left else 1
+        n = int(np.prod([bd[x] for x in right])) if right else 1
+        k = int(np.prod([ad[x] for x in common])) if common else 1
+        out.append((m, n, k))
+        nodes.append((left + right, [ad[x] for x in left] + [bd[x] for x in right]))
+    return out
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_network_amplitude_within_1e5_of_fp64(jet, precision):
+    """A 30-qubit, 10-cycle circuit amplitude (2^34 flops, tensor-core steps
+    under AUTO) sliced over 2 bonds: the complex64 result is within 1e-5 of
+    the complex128 FP64 result of the same path. The tensor core's own
+    accumulation rounds toward zero, and its bias compounds along a network;
+    this bounds it at the amplitude."""
+    from jet_gb300 import circuits
+
+    net = circuits.random_circuit_network(5, 6, 10, seed=3)
+    best = None
+    for s in range(4):
+        p = circuits.greedy_path(net, seed=s, score="gain")
+        f, _ = circuits.path_cost(net, p)
+        if best is None or f < best[0]:
+            best = (f, p)
+    path = best[1]
+    tc_steps = [s for s in _steps_mnk(net, path) if s[0] >= 128 and s[1] >= 64 and s[2] >= 32]
+    assert len(tc_steps) >= 2
+    sliced = circuits.choose_slices(net, path, 2)
+    ref = jet.SlicedContractorC128(_tn(jet, net, "complex128"), path, sliced, 0)
+    ref.set_batch_size(2)
+    want = ref.contract()[0]
+    del ref
+    sc = jet.SlicedContractorC64(_tn(jet, net, "complex64"), path, sliced, precision)
+    sc.set_batch_size(2)
+    got = sc.contract()[0]
+    assert abs(got - want) <= 1e-5 * abs(want), abs(got - want) / abs(want)
