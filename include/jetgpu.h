@@ -99,6 +99,12 @@ int jetgpu_version(void);
  * device. */
 int jetgpu_device_info(int *sm_count, int *cc_major, int *cc_minor);
 
+/* Current device of the calling thread, and selection of it (the device
+ * guard of CudaTensor<T, DEVICE>; reference CudaTensorHelpers.hpp:179-235).
+ * Library streams and pools are per device. */
+int jetgpu_get_device(int *device);
+int jetgpu_set_device(int device);
+
 /*
  * Index permutation, out-of-place.
  *   out[new multi-index] = in[old multi-index], new axis j = old axis perm[j].

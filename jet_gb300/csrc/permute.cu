@@ -165,6 +165,7 @@ struct SplitOut {
     float scale;           // exact power of two
     int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo (TF32)
     int bf16;              // 16-bit BF16 words instead of TF32-in-FP32 words
+    int cols_log2;         // log2(cols) when cols is a power of 2 (bit-permutation path)
 };
 
 __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
@@ -292,9 +293,11 @@ struct SplitStore {
     __device__ __forceinline__ void operator()(uint64_t off, const uint2 *v,
                                                int) const
     {
-        // off is even and cols >= 2 is a power of 2: both elements share a row.
-        uint64_t row = off / so.cols;
-        uint64_t col = off - row * so.cols;
+        // off is even and cols >= 2 is a power of 2: both elements share a row
+        // (shift and mask: a 64-bit division here made the kernel
+        // instruction bound).
+        uint64_t row = off >> so.cols_log2;
+        uint64_t col = off & (so.cols - 1);
         uint64_t base = row * so.pitch + col;
         float2 a = make_float2(__uint_as_float(v[0].x), __uint_as_float(v[0].y));
         float2 b = make_float2(__uint_as_float(v[1].x), __uint_as_float(v[1].y));
@@ -605,6 +608,7 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
     so.scale = ldexpf(1.0f, scale_exp);
     so.neg_im = neg_im;
     so.bf16 = fmt == SplitFormat::kBf16 ? 1 : 0;
+    so.cols_log2 = IsPow2(cols) ? Log2(cols) : -1;
     const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
                          (pitch % 2 == 0) && (plane_stride % 2 == 0);
     static thread_local BitParams bp;

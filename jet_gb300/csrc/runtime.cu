@@ -65,6 +65,24 @@ const char *jetgpu_last_error(void) { return jetgpu::g_last_error.c_str(); }
 
 int jetgpu_version(void) { return JETGPU_ABI_VERSION; }
 
+int jetgpu_get_device(int *device)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(device != nullptr, "null device pointer");
+    JETGPU_CUDA_TRY(cudaGetDevice(device));
+    return JETGPU_OK;
+}
+
+int jetgpu_set_device(int device)
+{
+    jetgpu::ClearError();
+    int count = 0;
+    JETGPU_CUDA_TRY(cudaGetDeviceCount(&count));
+    JETGPU_REQUIRE(device >= 0 && device < count && device < 64, "device out of range");
+    JETGPU_CUDA_TRY(cudaSetDevice(device));
+    return JETGPU_OK;
+}
+
 int jetgpu_device_info(int *sm_count, int *cc_major, int *cc_minor)
 {
     jetgpu::ClearError();

@@ -92,14 +92,46 @@ template <class T> void BindTensor(py::module_ &m)
              py::arg("ptr"));
 
     m.def("conj", [](const tensor_t &t) { return tensor_t::Conj(t); }, py::arg("tensor"));
-    // Permuter<QFlexPermuter<>>::Transpose on host data (the permuter plugin point).
+    // Permuter<Backend>::Transpose on host data (the permuter plugin point):
+    // backend "qflex" = QFlexPermuter<>, "qflex64" = QFlexPermuter<64>,
+    // "default" = DefaultPermuter<>.
     m.def("permuter_transpose",
           [](const std::vector<T> &data, const std::vector<size_t> &shape,
-             const std::vector<std::string> &current, const std::vector<std::string> &target) {
-              Jet::Permuter<Jet::QFlexPermuter<>> p;
-              return p.Transpose(data, shape, current, target);
+             const std::vector<std::string> &current, const std::vector<std::string> &target,
+             const std::string &backend) {
+              if (backend == "qflex")
+                  return Jet::Permuter<Jet::QFlexPermuter<>>().Transpose(data, shape, current,
+                                                                         target);
+              if (backend == "qflex64")
+                  return Jet::Permuter<Jet::QFlexPermuter<64>>().Transpose(data, shape, current,
+                                                                           target);
+              if (backend == "default")
+                  return Jet::Permuter<Jet::DefaultPermuter<>>().Transpose(data, shape, current,
+                                                                           target);
+              throw std::invalid_argument("backend must be qflex, qflex64 or default");
           },
-          py::arg("data"), py::arg("shape"), py::arg("current_order"), py::arg("new_order"));
+          py::arg("data"), py::arg("shape"), py::arg("current_order"), py::arg("new_order"),
+          py::arg("backend") = "qflex");
+    // QFlexPermuter<BLOCKSIZE, MIN_DIMS>::CheckPlan: raises the reference's
+    // error when its plan rejects the transpose (host only, no device work).
+    m.def("qflex_check_plan",
+          [](const std::vector<size_t> &shape, const std::vector<std::string> &current,
+             const std::vector<std::string> &target, size_t blocksize, size_t min_dims) {
+#define JET_QFLEX_CASE(B, M)                                                           \
+    if (blocksize == B && min_dims == M)                                               \
+        return Jet::QFlexPermuter<B, M>::CheckPlan(shape, current, target);
+              JET_QFLEX_CASE(1024, 32)
+              JET_QFLEX_CASE(64, 32)
+              JET_QFLEX_CASE(128, 64)
+              JET_QFLEX_CASE(256, 2)
+              JET_QFLEX_CASE(64, 2)
+              JET_QFLEX_CASE(2048, 1024)
+              JET_QFLEX_CASE(512, 32)
+#undef JET_QFLEX_CASE
+              throw std::invalid_argument("no QFlexPermuter instantiation for these parameters");
+          },
+          py::arg("shape"), py::arg("current_order"), py::arg("new_order"), py::arg("blocksize"),
+          py::arg("min_dims"));
     m.def("add_tensors", [](const tensor_t &a, const tensor_t &b) { return tensor_t::AddTensors(a, b); },
           py::arg("A"), py::arg("B"));
     m.def("contract_tensors",

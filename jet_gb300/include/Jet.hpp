@@ -2,6 +2,9 @@
 #pragma once
 
 #include "jet/Abort.hpp"
+#if __has_include(<cuComplex.h>)
+#include "jet/CudaTensor.hpp"
+#endif
 #include "jet/PathInfo.hpp"
 #include "jet/SlicedContractor.hpp"
 #include "jet/TaskBasedContractor.hpp"

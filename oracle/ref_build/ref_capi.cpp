@@ -189,7 +189,8 @@ int jetref_tensor_transpose(int dtype, size_t rank, const size_t *shape,
 
 // Permuter<Backend>::Transpose of n_data elements, backend 0 = DefaultPermuter<1024>,
 // 1 = QFlexPermuter<1024,32>, 2 = QFlexPermuter<64,32> (the reference test's
-// "insufficient BLOCKSIZE" configuration). complex<float> only.
+// "insufficient BLOCKSIZE" configuration), 3 = <128,64>, 4 = <256,2>,
+// 5 = <64,2>, 6 = <2048,1024>, 7 = <512,32>. complex<float> only.
 int jetref_permuter_transpose(int backend, size_t rank, const size_t *shape,
                               const char *old_labels, const char *new_labels,
                               const void *in, size_t n_data, void *out)
@@ -202,7 +203,22 @@ int jetref_permuter_transpose(int backend, size_t rank, const size_t *shape,
         if (backend == 1)
             return PermuterTranspose<T, Jet::QFlexPermuter<1024, 32>>(
                 rank, shape, old_labels, new_labels, in, n_data, out);
-        return PermuterTranspose<T, Jet::QFlexPermuter<64, 32>>(
+        if (backend == 2)
+            return PermuterTranspose<T, Jet::QFlexPermuter<64, 32>>(
+                rank, shape, old_labels, new_labels, in, n_data, out);
+        if (backend == 3)
+            return PermuterTranspose<T, Jet::QFlexPermuter<128, 64>>(
+                rank, shape, old_labels, new_labels, in, n_data, out);
+        if (backend == 4)
+            return PermuterTranspose<T, Jet::QFlexPermuter<256, 2>>(
+                rank, shape, old_labels, new_labels, in, n_data, out);
+        if (backend == 5)
+            return PermuterTranspose<T, Jet::QFlexPermuter<64, 2>>(
+                rank, shape, old_labels, new_labels, in, n_data, out);
+        if (backend == 6)
+            return PermuterTranspose<T, Jet::QFlexPermuter<2048, 1024>>(
+                rank, shape, old_labels, new_labels, in, n_data, out);
+        return PermuterTranspose<T, Jet::QFlexPermuter<512, 32>>(
             rank, shape, old_labels, new_labels, in, n_data, out);
     }
     catch (const std::exception &e) {

@@ -51,4 +51,6 @@ def golden():
         perm = json.load(f)
     with open(os.path.join(d, "ref_cases.json")) as f:
         cases = json.load(f)
-    return {"permuter": perm, "ref": cases}
+    with open(os.path.join(d, "qflex_plans.json")) as f:
+        qflex = json.load(f)
+    return {"permuter": perm, "ref": cases, "qflex_plans": qflex}

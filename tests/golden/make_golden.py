@@ -10,6 +10,10 @@ Outputs (committed; nothing at test time reads the reference tree):
                             test/Test_Permuter.cpp, parsed from the file as
                             text, each re-checked through the compiled
                             Permuter<DefaultPermuter> and Permuter<QFlexPermuter>.
+  qflex_plans.json       -- accept / reject decisions of the compiled
+                            QFlexPermuter<BLOCKSIZE, MIN_DIMS> plan on seeded
+                            power-of-2 transposes (with the output hash when
+                            accepted), for seven instantiations.
   ref_cases.json         -- seeded random cases run through the compiled
                             reference: Tensor::Transpose (SHA-256 of the
                             output bytes, bit-exact), ContractTensors
@@ -152,8 +156,50 @@ def make_ref_cases():
     return res
 
 
+# QFlexPermuter instantiations of the reference wrapper (oracle/ref_build/ref_capi.cpp).
+QFLEX_BACKENDS = {1: (1024, 32), 2: (64, 32), 3: (128, 64), 4: (256, 2), 5: (64, 2),
+                  6: (2048, 1024), 7: (512, 32)}
+
+
+def make_qflex_plans():
+    """Accept / reject decisions of the reference's QFlexPermuter plan on
+    seeded power-of-2 transposes (6 to 14 binary indices), for every
+    instantiation above: per case the shape, labels, the output's SHA-256
+    (DefaultPermuter; every accepting QFlexPermuter must match it) and, per
+    "BLOCKSIZE,MIN_DIMS", true or the reference's error message."""
+    rng = np.random.default_rng(2024)
+    out = []
+    for case in range(160):
+        nbits = int(rng.integers(6, 15))
+        dims = []
+        left = nbits
+        while left:
+            k = int(rng.integers(1, min(3, left) + 1))
+            dims.append(2 ** k)
+            left -= k
+        rank = len(dims)
+        old = [chr(ord("a") + i) for i in range(rank)]
+        new = [old[i] for i in rng.permutation(rank)]
+        data = cases.tensor_data(7000 + case, [2 ** nbits], np.complex64)
+        want = ref.permuter_transpose(0, data, dims, old, new)
+        decisions = {}
+        for backend, (block, min_dims) in QFLEX_BACKENDS.items():
+            try:
+                got = ref.permuter_transpose(backend, data, dims, old, new)
+                assert np.array_equal(got, want)
+                decisions["%d,%d" % (block, min_dims)] = True
+            except ref.RefError as e:
+                # Keep the message only (the text after "Error in Jet: ").
+                decisions["%d,%d" % (block, min_dims)] = str(e).split("Error in Jet: ")[-1]
+        out.append({"case": case, "seed": 7000 + case, "shape": dims, "old": old, "new": new,
+                    "sha256": sha(want), "decisions": decisions})
+    return out
+
+
 def main():
     assert ref.available(), "build oracle/_ref first: make -C oracle/ref_build"
+    with open(os.path.join(HERE, "qflex_plans.json"), "w") as f:
+        json.dump(make_qflex_plans(), f)
     with open(os.path.join(HERE, "permuter_vectors.json"), "w") as f:
         json.dump(make_permuter_vectors(), f)
     with open(os.path.join(HERE, "ref_cases.json"), "w") as f:
