@@ -433,7 +433,11 @@ SLICED_CONFIGS = {
     "2": (7, 7, 14, (), 12, 2, 2, 48),
     "4": (6, 9, 12, (5,), 6, 16, 4, 48),
     "0": (4, 4, 8, (), 0, 1, 1, 8),
+    # qutrit variant of config 4: 5x5 sites of dimension 3, 8 layers of Haar
+    # unitaries (cycles = layers), 4 sliced bonds -> 81 slices
+    "4q": (5, 5, 8, (), 4, 9, 9, 16),
 }
+QUDIT_DIM = {"4q": 3}
 
 
 def run_sliced(args, rank, world, local_rank):
@@ -450,7 +454,11 @@ def run_sliced(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     rows, cols, cycles, removed, n_sliced, batch, chunks, restarts = SLICED_CONFIGS[args.config]
     t0 = time.perf_counter()
-    net = circuits.random_circuit_network(rows, cols, cycles, seed=SEED, removed=removed)
+    qd = QUDIT_DIM.get(args.config, 2)
+    if qd != 2:
+        net = circuits.qudit_circuit_network(rows, cols, cycles, d=qd, seed=SEED)
+    else:
+        net = circuits.random_circuit_network(rows, cols, cycles, seed=SEED, removed=removed)
     best = None
     for s in range(restarts):
         for temp in (0.0, 0.2):
@@ -516,12 +524,14 @@ def run_sliced(args, rank, world, local_rank):
         "n_gpus": world, "steps": 1, "warmup": 1,
         "ms_per_step": forms["auto"]["s_per_slice"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded circuit)",
-        "config": {"workload": "config %s: %dx%d grid%s, %d cycles, %d sliced bonds, %d slices "
-                               "per batch, greedy path (2^%.1f flops, largest 2^%d)"
+        "config": {"workload": "config %s: %dx%d grid%s%s, %d %s, %d sliced bonds, %d slices "
+                               "per batch, greedy path (2^%.1f flops, largest 2^%.1f)"
                                % (args.config, rows, cols, " minus %d site" % len(removed)
-                                  if removed else "", cycles, n_sliced, batch,
+                                  if removed else "",
+                                  " of qudits (d=%d, Haar unitaries)" % qd if qd != 2 else "",
+                                  cycles, "layers" if qd != 2 else "cycles", n_sliced, batch,
                                   math.log2(full_flops), log2_big),
-                   "slices_total": 2 ** n_sliced},
+                   "slices_total": qd ** n_sliced},
         "forms": forms,
         "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
         "slice_flops_pathinfo": slice_flops, "slice_dependent_flops": dep_flops,
@@ -638,8 +648,8 @@ def main():
     ap.add_argument("--tc-variant", type=int, default=None,
                     help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",
-                    help="1 (default): the pairwise contraction; 0, 2, 4: sliced circuit "
-                         "amplitudes through the sliced executor")
+                    help="1 (default): the pairwise contraction; 0, 2, 4, 4q (qutrits): sliced "
+                         "circuit amplitudes through the sliced executor; 3: gradients")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

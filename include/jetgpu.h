@@ -245,17 +245,19 @@ size_t jetgpu_contract_noalloc_max_scratch(void);
  * Replaces the cblas_cgemm call of TensorHelpers.hpp:47-61.
  *
  * jetgpu_set_tc_variant selects the main-loop shape of the tensor-core
- * product for the calling process: 0 = M 128 x N 128 MMAs over 4 B planes,
- * 1 = M 128 x N 256 MMAs over 6 B planes (stacked [Br; Bi] and [-Bi; Br]
- * operands, half the MMA count); jetgpu_tc_b_planes() reports the B planes
- * the current shape reads.
+ * products for the calling process: 0 = default (M 128 x N 128 MMAs over 4 B
+ * planes, 3 stages of 64-byte rows); 1 = TF32 with M 128 x N 256 MMAs over
+ * 6 B planes (stacked [Br; Bi] and [-Bi; Br] operands, half the MMA count);
+ * 2 = BF16 with 32-byte rows in 6 stages (twice the pipeline depth in the
+ * same shared memory). jetgpu_tc_b_planes() reports the B planes the TF32
+ * product reads.
  */
 int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape,
                       const int32_t *perm, uint64_t rows, uint64_t cols,
                       uint64_t pitch, uint64_t plane_stride, int scale_exp,
                       int n_planes, float *planes, void *stream);
 
-int jetgpu_set_tc_variant(int wide);
+int jetgpu_set_tc_variant(int variant);
 int jetgpu_tc_b_planes(void);
 
 /*

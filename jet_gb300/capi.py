@@ -227,9 +227,10 @@ def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, n_planes=
     return planes
 
 
-def set_tc_variant(wide: int) -> None:
-    """0: N = 128 tensor-core main loop; 1: N = 256 (six B planes)."""
-    check(lib.jetgpu_set_tc_variant(int(wide)))
+def set_tc_variant(variant: int) -> None:
+    """0: default main loops; 1: TF32 with N = 256 MMAs (six B planes);
+    2: BF16 with 32-byte rows in 6 stages."""
+    check(lib.jetgpu_set_tc_variant(int(variant)))
 
 
 def set_tc_chunk_depth(k_depth: int) -> None:

@@ -43,35 +43,41 @@ constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
 constexpr int kGroupM = 8;                    // tile rows per group of the tile order
 
-// Every stage holds boxes of 128 rows x 64 bytes (64-byte swizzle); every
-// MMA consumes 32 bytes of K per row, two per stage. Main-loop variants:
-//  0 TF32 narrow: 16-deep stages, 3 stages of 4 A + 4 B plane boxes; 12 MMAs
-//                 of N = 128 per k step.
-//  1 TF32 wide:   2 stages of 4 A boxes and two B triples [-Bi, Br, Bi]
-//                 (hi, lo); 6 MMAs of N = 256 per k step: Ar [Br; Bi] ->
-//                 [ArBr | ArBi] and Ai [-Bi; Br] -> [-AiBi | AiBr] land on
-//                 (Cr | Ci) in one instruction each.
-//  2 BF16 narrow: variant 0 with 32-deep stages of BF16 planes (kind::f16).
+// Every stage holds boxes of 128 rows x RowBytes (swizzled by RowBytes);
+// every MMA consumes 32 bytes of K per row. Main-loop variants:
+//  0 TF32 narrow: 64-byte rows (16 k), 3 stages of 4 A + 4 B plane boxes;
+//                 12 MMAs of N = 128 per k step.
+//  1 TF32 wide:   64-byte rows, 2 stages of 4 A boxes and two B triples
+//                 [-Bi, Br, Bi] (hi, lo); 6 MMAs of N = 256 per k step:
+//                 Ar [Br; Bi] -> [ArBr | ArBi] and Ai [-Bi; Br] ->
+//                 [-AiBi | AiBr] land on (Cr | Ci) in one instruction each.
+//  2 BF16 narrow: variant 0 on BF16 planes (kind::f16, 32 k per stage).
+//  3 BF16 deep:   32-byte rows (16 k, 32-byte swizzle), 6 stages of 32 KB:
+//                 the same shared memory as variant 2 in twice as many,
+//                 half-size stages.
 // A chunk is the K extent accumulated in TMEM before the FP32 fold, in
 // stages (a kernel argument; see the kernel comment).
 template <int V> struct TcCfg;
 template <> struct TcCfg<0> {
     static constexpr bool Wide = false, Bf16 = false;
-    static constexpr int Stages = 3, Tiles = 8;
+    static constexpr int Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <> struct TcCfg<1> {
     static constexpr bool Wide = true, Bf16 = false;
-    static constexpr int Stages = 2, Tiles = 10;
+    static constexpr int Stages = 2, Tiles = 10, RowBytes = 64;
 };
 template <> struct TcCfg<2> {
     static constexpr bool Wide = false, Bf16 = true;
-    static constexpr int Stages = 3, Tiles = 8;
+    static constexpr int Stages = 3, Tiles = 8, RowBytes = 64;
 };
-constexpr int kRowBytes = 64;
-constexpr int kTileBytes = kBM * kRowBytes;
+template <> struct TcCfg<3> {
+    static constexpr bool Wide = false, Bf16 = true;
+    static constexpr int Stages = 6, Tiles = 8, RowBytes = 32;
+};
+template <int V> constexpr int TileBytes() { return kBM * TcCfg<V>::RowBytes; }
 template <int V> constexpr int ElemBytes() { return TcCfg<V>::Bf16 ? 2 : 4; }
-template <int V> constexpr int BlockK() { return kRowBytes / ElemBytes<V>(); }
-template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * kTileBytes; }
+template <int V> constexpr int BlockK() { return TcCfg<V>::RowBytes / ElemBytes<V>(); }
+template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * TileBytes<V>(); }
 
 // Default K depth accumulated in TMEM per chunk. TF32: 16, one fold per
 // stage. The tensor core's accumulation rounds magnitudes toward zero, so its
@@ -84,9 +90,8 @@ constexpr int kDefaultChunkKTf32 = 16;
 constexpr int kDefaultChunkKBf16 = 128;
 int g_tc_chunk_k = 0; // K depth per TMEM chunk (jetgpu_set_tc_chunk_depth; 0 = default)
 
-inline int ChunkStages(bool bf16)
+inline int ChunkStages(bool bf16, int stage_k)
 {
-    const int stage_k = bf16 ? BlockK<2>() : BlockK<0>();
     int depth = g_tc_chunk_k > 0 ? g_tc_chunk_k : (bf16 ? kDefaultChunkKBf16 : kDefaultChunkKTf32);
     int stages = depth / stage_k;
     return stages < 1 ? 1 : stages;
@@ -166,16 +171,18 @@ __device__ __forceinline__ void TmaLoad4d(uint32_t dst, const CUtensorMap *map,
                  : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 64-byte swizzled rows,
-// 8-row groups 512 bytes apart.
-__device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
+// Shared-memory matrix descriptor: K-major operand, rows of kRow bytes
+// swizzled over kRow bytes (layout code 4 = 64-byte, 6 = 32-byte swizzle),
+// 8-row groups 8 * kRow bytes apart.
+template <int kRow> __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
 {
+    static_assert(kRow == 64 || kRow == 32, "64- or 32-byte rows");
     uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);         // start address
-    d |= (uint64_t)1 << 16;                          // leading byte offset (unused)
-    d |= (uint64_t)((8 * kRowBytes) >> 4) << 32;     // stride byte offset
-    d |= (uint64_t)1 << 46;                          // descriptor version
-    d |= (uint64_t)4 << 61;                          // 64-byte swizzle
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);                 // start address
+    d |= (uint64_t)1 << 16;                                  // leading byte offset (unused)
+    d |= (uint64_t)((8 * kRow) >> 4) << 32;                  // stride byte offset
+    d |= (uint64_t)1 << 46;                                  // descriptor version
+    d |= (uint64_t)(kRow == 64 ? 4 : 6) << 61;               // swizzle mode
     return d;
 }
 
@@ -275,6 +282,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr int kBK = BlockK<V>();
     constexpr int kStages = Cfg::Stages;
     constexpr int kStageBytes = StageBytes<V>();
+    constexpr int kTileBytes = TileBytes<V>();
+    constexpr int kRowBytes = Cfg::RowBytes;
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
@@ -394,15 +403,15 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int kk = 0; kk < kRowBytes / 32; ++kk) {
                         const uint32_t koff = kk * 32; // 32 bytes of K per MMA
-                        const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
-                        const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
-                        const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
-                        const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
+                        const uint64_t arh = SmemDesc<kRowBytes>(base + 0 * kTileBytes + koff);
+                        const uint64_t arl = SmemDesc<kRowBytes>(base + 1 * kTileBytes + koff);
+                        const uint64_t aih = SmemDesc<kRowBytes>(base + 2 * kTileBytes + koff);
+                        const uint64_t ail = SmemDesc<kRowBytes>(base + 3 * kTileBytes + koff);
                         // [-Bi; Br] starts at tile 4, [Br; Bi] at tile 5 (hi); 7, 8 (lo).
-                        const uint64_t b_nr_hi = SmemDesc(base + 4 * kTileBytes + koff);
-                        const uint64_t b_rc_hi = SmemDesc(base + 5 * kTileBytes + koff);
-                        const uint64_t b_nr_lo = SmemDesc(base + 7 * kTileBytes + koff);
-                        const uint64_t b_rc_lo = SmemDesc(base + 8 * kTileBytes + koff);
+                        const uint64_t b_nr_hi = SmemDesc<kRowBytes>(base + 4 * kTileBytes + koff);
+                        const uint64_t b_rc_hi = SmemDesc<kRowBytes>(base + 5 * kTileBytes + koff);
+                        const uint64_t b_nr_lo = SmemDesc<kRowBytes>(base + 7 * kTileBytes + koff);
+                        const uint64_t b_rc_lo = SmemDesc<kRowBytes>(base + 8 * kTileBytes + koff);
                         const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                         // (Cr | Ci) += Ar [Br; Bi]
                         Mma<kBf16>(d_re, arh, b_rc_hi, kIdescW, acc);
@@ -418,14 +427,14 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int kk = 0; kk < kRowBytes / 32; ++kk) {
                     const uint32_t koff = kk * 32; // 32 bytes of K per MMA
-                    const uint64_t arh = SmemDesc(base + 0 * kTileBytes + koff);
-                    const uint64_t arl = SmemDesc(base + 1 * kTileBytes + koff);
-                    const uint64_t aih = SmemDesc(base + 2 * kTileBytes + koff);
-                    const uint64_t ail = SmemDesc(base + 3 * kTileBytes + koff);
-                    const uint64_t brh = SmemDesc(base + 4 * kTileBytes + koff);
-                    const uint64_t brl = SmemDesc(base + 5 * kTileBytes + koff);
-                    const uint64_t bih = SmemDesc(base + 6 * kTileBytes + koff);
-                    const uint64_t bil = SmemDesc(base + 7 * kTileBytes + koff);
+                    const uint64_t arh = SmemDesc<kRowBytes>(base + 0 * kTileBytes + koff);
+                    const uint64_t arl = SmemDesc<kRowBytes>(base + 1 * kTileBytes + koff);
+                    const uint64_t aih = SmemDesc<kRowBytes>(base + 2 * kTileBytes + koff);
+                    const uint64_t ail = SmemDesc<kRowBytes>(base + 3 * kTileBytes + koff);
+                    const uint64_t brh = SmemDesc<kRowBytes>(base + 4 * kTileBytes + koff);
+                    const uint64_t brl = SmemDesc<kRowBytes>(base + 5 * kTileBytes + koff);
+                    const uint64_t bih = SmemDesc<kRowBytes>(base + 6 * kTileBytes + koff);
+                    const uint64_t bil = SmemDesc<kRowBytes>(base + 7 * kTileBytes + koff);
                     const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                     // Cr += Ar Br
                     Mma<kBf16>(d_re, arh, brh, kIdesc, acc);
@@ -538,19 +547,21 @@ int GetEncoder()
     return JETGPU_OK;
 }
 
-// 3-D map over planes: (k, row, plane), box (64 bytes of k) x 128 x 1.
+// 3-D map over planes: (k, row, plane), box (row_bytes of k) x 128 x 1,
+// swizzled over row_bytes (64 or 32).
 int EncodePlanes(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
-                 uint64_t kpitch, bool bf16, int planes)
+                 uint64_t kpitch, bool bf16, int planes, int row_bytes)
 {
     const uint64_t eb = bf16 ? 2 : 4;
     cuuint64_t dims[3] = {k, rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {kpitch * eb, rows * kpitch * eb};
-    cuuint32_t box[3] = {(cuuint32_t)(kRowBytes / eb), kBM, 1};
+    cuuint32_t box[3] = {(cuuint32_t)(row_bytes / eb), kBM, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = g_encode(map,
                           bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                           3, const_cast<void *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return SetError(JETGPU_ERR_CUDA,
@@ -559,19 +570,20 @@ int EncodePlanes(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
 }
 
 // 4-D map over batched planes laid out [plane][batch][rows][kpitch]:
-// (k, row, batch, plane), box (64 bytes of k) x 128 x 1 x 1.
+// (k, row, batch, plane), box (row_bytes of k) x 128 x 1 x 1.
 int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
-                        uint64_t kpitch, uint64_t batch, bool bf16, int planes)
+                        uint64_t kpitch, uint64_t batch, bool bf16, int planes, int row_bytes)
 {
     const uint64_t eb = bf16 ? 2 : 4;
     cuuint64_t dims[4] = {k, rows, batch, (cuuint64_t)planes};
     cuuint64_t strides[3] = {kpitch * eb, rows * kpitch * eb, batch * rows * kpitch * eb};
-    cuuint32_t box[4] = {(cuuint32_t)(kRowBytes / eb), kBM, 1, 1};
+    cuuint32_t box[4] = {(cuuint32_t)(row_bytes / eb), kBM, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = g_encode(map,
                           bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                           4, const_cast<void *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return SetError(JETGPU_ERR_CUDA,
@@ -599,11 +611,13 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
-        b_batched, ChunkStages(TcCfg<V>::Bf16));
+        b_batched, ChunkStages(TcCfg<V>::Bf16, BlockK<V>()));
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
-int g_tc_wide = 0; // main-loop shape of the TF32 product (jetgpu_set_tc_variant)
+// Main-loop variant (jetgpu_set_tc_variant): 0 default, 1 TF32 N = 256,
+// 2 BF16 with 32-byte rows and 6 stages.
+int g_tc_variant = 0;
 
 } // namespace
 
@@ -647,15 +661,21 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
     int rc = GetEncoder();
     if (rc)
         return rc;
-    const bool wide = !bf16 && g_tc_wide != 0;
+    const bool wide = !bf16 && g_tc_variant == 1;
+    const bool deep = bf16 && g_tc_variant == 2;
+    const int row_bytes = deep ? TcCfg<3>::RowBytes : TcCfg<0>::RowBytes;
     CUtensorMap ta, tb;
-    if ((rc = a_batched ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, bf16, 4)
-                        : EncodePlanes(&ta, a_planes, m, k, kpitch, bf16, 4)))
+    if ((rc = a_batched
+                  ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, bf16, 4, row_bytes)
+                  : EncodePlanes(&ta, a_planes, m, k, kpitch, bf16, 4, row_bytes)))
         return rc;
     const int bplanes = wide ? 6 : 4;
-    if ((rc = b_batched ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, bf16, bplanes)
-                        : EncodePlanes(&tb, b_planes, n, k, kpitch, bf16, bplanes)))
+    if ((rc = b_batched
+                  ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, bf16, bplanes, row_bytes)
+                  : EncodePlanes(&tb, b_planes, n, k, kpitch, bf16, bplanes, row_bytes)))
         return rc;
+    if (deep)
+        return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
     if (bf16)
         return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
     return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream)
@@ -663,17 +683,18 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                               stream);
 }
 
-bool TcWide() { return g_tc_wide != 0; }
+bool TcWide() { return g_tc_variant == 1; }
 
 } // namespace jetgpu
 
 extern "C" int jetgpu_tc_b_planes(void) { return jetgpu::TcWide() ? 6 : 4; }
 
-extern "C" int jetgpu_set_tc_variant(int wide)
+extern "C" int jetgpu_set_tc_variant(int variant)
 {
     jetgpu::ClearError();
-    JETGPU_REQUIRE(wide == 0 || wide == 1, "variant must be 0 (N = 128) or 1 (N = 256)");
-    jetgpu::g_tc_wide = wide;
+    JETGPU_REQUIRE(variant >= 0 && variant <= 2,
+                   "variant must be 0 (default), 1 (TF32 N = 256) or 2 (BF16 6-stage)");
+    jetgpu::g_tc_variant = variant;
     return JETGPU_OK;
 }
 

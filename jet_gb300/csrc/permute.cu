@@ -140,21 +140,21 @@ __device__ __forceinline__ float RoundTf32(float x)
     return __uint_as_float((u + 0x1000u) & 0xffffe000u);
 }
 
-// BF16 rounding to nearest, ties to even: add 0x7fff plus the lowest kept
-// bit, then drop the 16 low bits. Returns the BF16 word.
-__device__ __forceinline__ uint32_t Bf16Bits(float x)
+// Two floats to packed BF16 words, round to nearest even (one hardware
+// conversion): `lower` in bits 0-15, `upper` in bits 16-31.
+__device__ __forceinline__ uint32_t PackBf16x2(float lower, float upper)
 {
-    uint32_t u = __float_as_uint(x);
-    if ((u & 0x7f800000u) == 0x7f800000u) // inf stays inf, nan stays (quiet) nan
-        return (u >> 16) | ((u & 0x7fffffu) ? 0x40u : 0u);
-    return (u + 0x7fffu + ((u >> 16) & 1u)) >> 16;
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(upper), "f"(lower));
+    return r;
 }
 
-// hi = RN_bf16(x), lo = RN_bf16(x - hi); x - hi is exact in FP32.
-__device__ __forceinline__ void SplitBf16(float x, uint32_t &hi, uint32_t &lo)
+// BF16 hi/lo splits of two values x0, x1, packed as (x0 low half, x1 high
+// half): hi = RN_bf16(x), lo = RN_bf16(x - hi); x - hi is exact in FP32.
+__device__ __forceinline__ void SplitBf16x2(float x0, float x1, uint32_t &hi, uint32_t &lo)
 {
-    hi = Bf16Bits(x);
-    lo = Bf16Bits(x - __uint_as_float(hi << 16));
+    hi = PackBf16x2(x0, x1);
+    lo = PackBf16x2(x0 - __uint_as_float(hi << 16), x1 - __uint_as_float(hi & 0xffff0000u));
 }
 
 struct SplitOut {
@@ -177,13 +177,12 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
     float re = v.x * so.scale, im = v.y * so.scale;
     if (so.bf16) {
         uint16_t *pl = static_cast<uint16_t *>(so.planes);
-        uint32_t rh, rl, ih, il;
-        SplitBf16(re, rh, rl);
-        SplitBf16(im, ih, il);
-        pl[off] = (uint16_t)rh;
-        pl[off + so.plane_stride] = (uint16_t)rl;
-        pl[off + 2 * so.plane_stride] = (uint16_t)ih;
-        pl[off + 3 * so.plane_stride] = (uint16_t)il;
+        uint32_t h, l; // (re, im) packed
+        SplitBf16x2(re, im, h, l);
+        pl[off] = (uint16_t)(h & 0xffffu);
+        pl[off + so.plane_stride] = (uint16_t)(l & 0xffffu);
+        pl[off + 2 * so.plane_stride] = (uint16_t)(h >> 16);
+        pl[off + 3 * so.plane_stride] = (uint16_t)(l >> 16);
         return;
     }
     float *planes = static_cast<float *>(so.planes);
@@ -306,15 +305,13 @@ struct SplitStore {
         if (so.bf16) {
             // Two BF16 words per plane: one 4-byte store (base is even).
             uint16_t *pl = static_cast<uint16_t *>(so.planes);
-            uint32_t arh, arl, aih, ail, brh, brl, bih, bil;
-            SplitBf16(ar, arh, arl);
-            SplitBf16(ai, aih, ail);
-            SplitBf16(br, brh, brl);
-            SplitBf16(bi, bih, bil);
-            *reinterpret_cast<uint32_t *>(pl + base) = arh | (brh << 16);
-            *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = arl | (brl << 16);
-            *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = aih | (bih << 16);
-            *reinterpret_cast<uint32_t *>(pl + base + 3 * so.plane_stride) = ail | (bil << 16);
+            uint32_t rh, rl, ih, il; // (element a, element b) packed per plane
+            SplitBf16x2(ar, br, rh, rl);
+            SplitBf16x2(ai, bi, ih, il);
+            *reinterpret_cast<uint32_t *>(pl + base) = rh;
+            *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = rl;
+            *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = ih;
+            *reinterpret_cast<uint32_t *>(pl + base + 3 * so.plane_stride) = il;
             return;
         }
         float *planes = static_cast<float *>(so.planes);

@@ -34,12 +34,12 @@ def _case(seed, nl, nc, nr, dtype, batch, a_b, b_b, dev):
 @pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 1),
                                              ("complex64", 3), ("complex128", 0)])
 @pytest.mark.parametrize("shape", [(7, 6, 8), (1, 9, 3), (4, 10, 1), (0, 5, 0), (8, 8, 8)])
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape, variant):
     from jet_gb300 import capi
 
-    if variant and precision != 1:
-        pytest.skip("the main-loop shape only affects the TF32x3 form")
+    if (variant == 1 and precision != 1) or (variant == 2 and precision != 3):
+        pytest.skip("variant 1 shapes the TF32x3 main loop, variant 2 the BF16x3 one")
     capi.set_tc_variant(variant)
 
     batch = 5

@@ -60,6 +60,17 @@ def _product_model(a, b):
         p(arh, arl, bih, bil) + p(aih, ail, brh, brl))
 
 
+@pytest.fixture(params=[0, 2], ids=["rows64", "rows32x6"])
+def bf16_variant(request, cuda):
+    """Runs a test under both BF16 main loops: 3 stages of 64-byte rows, and
+    6 stages of 32-byte rows."""
+    from jet_gb300 import capi
+
+    capi.set_tc_variant(request.param)
+    yield request.param
+    capi.set_tc_variant(0)
+
+
 def _rel(got, want):
     return np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
 
@@ -111,7 +122,7 @@ def test_split_bf16_bit_exact(cuda, shape, perm):
 @pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 128, 64), (200, 136, 100),
                                    (1024, 512, 256), (130, 300, 33), (4096, 256, 1024),
                                    (64, 512, 2048), (384, 256, 4096)])
-def test_bf16x3_random_gemm(cuda, m, n, k):
+def test_bf16x3_random_gemm(cuda, m, n, k, bf16_variant):
     """Config-1 value distribution against complex128 (1e-5) and against the
     exact three-product model (2e-6, the accumulation alone)."""
     from jet_gb300 import capi
@@ -129,7 +140,7 @@ def test_bf16x3_random_gemm(cuda, m, n, k):
     assert capi.take_device_status() == 0
 
 
-def test_bf16x3_stages_equal_contract(cuda):
+def test_bf16x3_stages_equal_contract(cuda, bf16_variant):
     """jetgpu_split_bf16 + jetgpu_gemm_bf16x3 give jetgpu_contract's result
     bit for bit (the contraction is those two stages)."""
     import torch
@@ -188,7 +199,7 @@ def test_bf16x3_exact_values(cuda):
     assert np.all(out == np.complex64(2.25 + 3j))
 
 
-def test_bf16x3_transposed_operands_config1_shape_reduced(cuda):
+def test_bf16x3_transposed_operands_config1_shape_reduced(cuda, bf16_variant):
     """Config-1 structure at reduced size: A rank 21, B rank 19, 10 shared
     labels, both seeded-randomly permuted, against the oracle."""
     from jet_gb300 import capi
