@@ -375,6 +375,9 @@ def run_ours(args, rank, world, local_rank):
     # A per element: read 8 B, write 4 planes x (2 B BF16 | 4 B TF32).
     split_bytes = (16.0 if head == "bf16x3" else 24.0) * m * k
     achieved = flops / (gemm_ms * 1e-3) / 1e12
+    # DRAM bytes (read + write) per launch of the product at this size, from
+    # one ncu capture (profiles/tc_gemm_split_bf16_config1_launches.md).
+    traffic = 7.67e9 if head == "bf16x3" else 14.77e9
     form_names = {"tf32x3": "TF32x3 4M (tcgen05 kind::tf32, hi/lo split, 3 products)",
                   "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)"}
     line = {
@@ -402,7 +405,9 @@ def run_ours(args, rank, world, local_rank):
                      "peak_source": ("%s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak))
                      if head == "bf16x3" else
                      ("TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak)),
-                     "traffic": None},
+                     "traffic": traffic,
+                     "traffic_algorithmic": (16.0 if head == "bf16x3" else 32.0) * (m + n) * k
+                     / 2.0 + 8.0 * m * n},
         "roofline_split": {"bound": "hbm", "kernel": "bitperm_kernel (split store)",
                            "achieved": split_bytes / (split_ms * 1e-3) / 1e9, "peak": hbm_peak,
                            "unit": "GB/s",
