@@ -128,52 +128,71 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def cpu_sample(nthreads=0, s_common=1, reps=3):
-    """The oracle port on the config with s_common shared labels fixed."""
+def _cpu_case(s_common):
+    """Inputs of the config-1 contraction with s_common shared labels fixed
+    (the transposes and the GEMM shrink by the same factor 2^s_common)."""
     import numpy as np
-
-    from oracle import port
 
     w = workload(N_LEFT, N_COMMON - s_common, N_RIGHT)
     rng = np.random.default_rng(SEED)
     na, nb = 2 ** len(w["a_lab"]), 2 ** len(w["b_lab"])
     a = ((rng.standard_normal(na) + 1j * rng.standard_normal(na)) * np.sqrt(0.5) * 2**-10).astype(np.complex64)
     b = ((rng.standard_normal(nb) + 1j * rng.standard_normal(nb)) * np.sqrt(0.5) * 2**-10).astype(np.complex64)
+    return w, a, b
+
+
+def _cpu_step(w, a, b, nthreads=0):
+    from oracle import port
+
+    t0 = time.perf_counter()
     port.contract(a, w["a_shape"], w["a_perm"], b, w["b_shape"], w["b_perm_kn"], w["m"], w["n"],
-                  w["k"], nthreads)  # warm-up
-    times = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        port.contract(a, w["a_shape"], w["a_perm"], b, w["b_shape"], w["b_perm_kn"], w["m"],
-                      w["n"], w["k"], nthreads)
-        times.append(time.perf_counter() - t0)
-    t = statistics.median(times)
+                  w["k"], nthreads)
+    return time.perf_counter() - t0
+
+
+def _cpu_sample_text(s_common, runs, t):
+    return ("config-1 contraction with %d of 13 shared labels fixed (M=2^14, N=2^12, K=2^%d), "
+            "median of %d runs, %.2f s each" % (s_common, N_COMMON - s_common, runs, t))
+
+
+def cpu_sample(nthreads=0, s_common=1, reps=3):
+    """The oracle port on the config with s_common shared labels fixed."""
+    from oracle import port
+
+    w, a, b = _cpu_case(s_common)
+    _cpu_step(w, a, b, nthreads)  # warm-up
+    t = statistics.median(_cpu_step(w, a, b, nthreads) for _ in range(reps))
     flops = 8.0 * w["m"] * w["n"] * w["k"]
     return {"value": flops / t / 1e12, "unit": "TFLOP/s", "cores": port.max_threads(),
-            "kind": "port",
-            "sample": "config-1 contraction with %d of 13 shared labels fixed (M=2^14, N=2^12, "
-                      "K=2^%d), median of %d runs, %.2f s each" % (s_common, N_COMMON - s_common,
-                                                                  reps, t)}
+            "kind": "port", "sample": _cpu_sample_text(s_common, reps, t)}
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU arithmetic for the path (the oracle port: the
+    reference's permute + row-major CBLAS cgemm on all host cores) on a
+    bounded sample of config 1: W warm-up and K timed steps, each step one
+    contraction with 2 of the 13 shared labels fixed."""
     if rank != 0:
         return
-    steps = []
-    info = None
-    for i in range(args.warmup + args.steps):
-        info = cpu_sample(s_common=2, reps=1)
-        if i >= args.warmup:
-            steps.append(info["value"])
-    value = statistics.median(steps)
+    from oracle import port
+
+    s_common = 2
+    w, a, b = _cpu_case(s_common)
+    for _ in range(args.warmup):
+        _cpu_step(w, a, b)
+    times = [_cpu_step(w, a, b) for _ in range(args.steps)]
+    t = statistics.median(times)
+    value = 8.0 * w["m"] * w["n"] * w["k"] / t / 1e12
+    info = {"value": value, "unit": "TFLOP/s", "cores": port.max_threads(), "kind": "port",
+            "sample": _cpu_sample_text(s_common, args.steps, t)}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (fp32)", "data": "synthetic",
             "config": {"workload": "config 1: rank-27 x rank-25 contraction, 13 shared labels "
                                    "(M=2^14, N=2^12, K=2^13), complex64",
                        "sample": info["sample"]},
-            "cpu_baseline": dict(info, value=value),
+            "cpu_baseline": info,
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
