@@ -19,6 +19,7 @@
 
 #include <future>
 #include <memory>
+#include <ostream>
 #include <string>
 #include <thread>
 #include <type_traits>
@@ -226,5 +227,64 @@ template <class TensorType> class TaskBasedContractor {
         reduction_result_ = std::move(acc);
     }
 };
+
+// The task dependency graph in DOT format (reference TaskBasedContractor.hpp:429-452,
+// which prints Taskflow's dump). One node per task, labelled with its name;
+// edges run from the task producing an operand to the task consuming it,
+// from every result store to the reduction, and from every consumer of a
+// tensor to that tensor's deletion task.
+template <class TensorType>
+inline std::ostream &operator<<(std::ostream &out, const TaskBasedContractor<TensorType> &tbc)
+{
+    using Task = typename TaskBasedContractor<TensorType>::Task;
+    const auto &tasks = tbc.GetTasks();
+    const auto &producer = tbc.GetNameToTaskMap();
+    auto quoted = [](const std::string &s) {
+        std::string q = "\"";
+        for (char c : s) {
+            if (c == '"' || c == '\\')
+                q += '\\';
+            q += c;
+        }
+        return q + "\"";
+    };
+    out << "digraph Taskflow {\n";
+    for (size_t i = 0; i < tasks.size(); ++i) {
+        std::string label = tasks[i].name;
+        if (tasks[i].kind == Task::STORE)
+            label = "store " + label;
+        out << "t" << i << " [label=" << quoted(label) << "];\n";
+    }
+    for (size_t i = 0; i < tasks.size(); ++i) {
+        const Task &t = tasks[i];
+        if (t.kind == Task::CONTRACT) {
+            for (const auto *in : {&t.input_1, &t.input_2}) {
+                auto it = producer.find(*in);
+                if (it != producer.end())
+                    out << "t" << it->second << " -> t" << i << ";\n";
+            }
+        }
+        else if (t.kind == Task::STORE) {
+            out << "t" << producer.at(t.name) << " -> t" << i << ";\n";
+        }
+        else if (t.kind == Task::REDUCE) {
+            for (size_t j = 0; j < tasks.size(); ++j)
+                if (tasks[j].kind == Task::STORE)
+                    out << "t" << j << " -> t" << i << ";\n";
+        }
+        else if (t.kind == Task::DELETE) {
+            auto parents = tbc.GetNameToParentsMap().find(t.input_1);
+            if (parents == tbc.GetNameToParentsMap().end())
+                continue;
+            for (const auto &consumer : parents->second) {
+                auto it = producer.find(consumer);
+                if (it != producer.end())
+                    out << "t" << it->second << " -> t" << i << ";\n";
+            }
+        }
+    }
+    out << "}\n";
+    return out;
+}
 
 } // namespace Jet
