@@ -477,6 +477,10 @@ def run_sliced(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     rows, cols, cycles, removed, n_sliced, batch, chunks, restarts = SLICED_CONFIGS[args.config]
+    if args.sliced_batch:
+        batch = args.sliced_batch
+    if args.sliced_chunks:
+        chunks = args.sliced_chunks
     t0 = time.perf_counter()
     qd = QUDIT_DIM.get(args.config, 2)
     if qd != 2:
@@ -499,8 +503,10 @@ def run_sliced(args, rank, world, local_rank):
         tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
     forms = {}
     amps = {}
-    sliced_forms = (("auto", jet.PREC_AUTO), ("bf16x3", jet.PREC_BF16X3),
-                    ("fp32", jet.PREC_FP32))
+    sliced_forms = tuple((f, p) for f, p in (("auto", jet.PREC_AUTO),
+                                             ("bf16x3", jet.PREC_BF16X3),
+                                             ("fp32", jet.PREC_FP32))
+                         if f in args.sliced_forms.split(","))
     for name, prec in sliced_forms:
         sc = jet.SlicedContractorC64(tn, path, sliced, prec)
         sc.set_batch_size(batch)
@@ -522,8 +528,12 @@ def run_sliced(args, rank, world, local_rank):
         slice_flops = sc.slice_flops
         dep_flops = sc.slice_dependent_flops
         del sc
-    rel = abs(amps["auto"] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
-    rel_bf = abs(amps["bf16x3"] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
+    def rel_to_fp32(f):
+        if f not in amps or "fp32" not in amps:
+            return None
+        return abs(amps[f] - amps["fp32"]) / max(abs(amps["fp32"]), 1e-300)
+
+    rel, rel_bf = rel_to_fp32("auto"), rel_to_fp32("bf16x3")
     # One slice in complex128 (FP64 arithmetic on the GPU) as the reference
     # for the per-slice error of both complex64 forms.
     slice_check = None
@@ -543,10 +553,11 @@ def run_sliced(args, rank, world, local_rank):
             v = sc.contract(0, 1)[0]
             slice_check["rel_err_" + name] = abs(v - ref64) / max(abs(ref64), 1e-300)
             del sc
+    head = "auto" if "auto" in forms else next(iter(forms))
     line = {
-        "metric": METRIC, "value": forms["auto"]["slices_per_s"], "unit": "slices/s",
+        "metric": METRIC, "value": forms[head]["slices_per_s"], "unit": "slices/s",
         "n_gpus": world, "steps": 1, "warmup": 1,
-        "ms_per_step": forms["auto"]["s_per_slice"] * 1e3, "higher_is_better": True,
+        "ms_per_step": forms[head]["s_per_slice"] * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded circuit)",
         "config": {"workload": "config %s: %dx%d grid%s%s, %d %s, %d sliced bonds, %d slices "
                                "per batch, greedy path (2^%.1f flops, largest 2^%.1f)"
@@ -557,9 +568,10 @@ def run_sliced(args, rank, world, local_rank):
                                   math.log2(full_flops), log2_big),
                    "slices_total": qd ** n_sliced},
         "forms": forms,
-        "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
+        "tc_vs_plain_speedup": (forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"]
+                                if "auto" in forms and "fp32" in forms else None),
         "slice_flops_pathinfo": slice_flops, "slice_dependent_flops": dep_flops,
-        "amplitude_sample": [amps["auto"].real, amps["auto"].imag],
+        "amplitude_sample": [amps[head].real, amps[head].imag],
         "rel_diff_auto_vs_fp32": rel,
         "rel_diff_bf16x3_vs_fp32": rel_bf,
         "slice_vs_fp64": slice_check,
@@ -667,6 +679,12 @@ def main():
     ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3"],
                     help="split form of the config-1 step (auto: both timed, the headline is "
                          "BF16x3 when its error on the step is within 1e-5, else TF32x3)")
+    ap.add_argument("--sliced-forms", default="auto,bf16x3,fp32",
+                    help="forms timed by the sliced configs (comma list of auto, bf16x3, fp32)")
+    ap.add_argument("--sliced-batch", type=int, default=0,
+                    help="slices per batch of the sliced configs (0: the config's own)")
+    ap.add_argument("--sliced-chunks", type=int, default=0,
+                    help="batches timed by the sliced configs (0: the config's own)")
     ap.add_argument("--tc-chunk", type=int, default=None,
                     help="K depth accumulated in tensor memory per fold (0 = defaults)")
     ap.add_argument("--tc-variant", type=int, default=None,

@@ -101,10 +101,14 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
                        int neg_im, cudaStream_t stream);
 
 // C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
-// operand), C packed as batch x m x n.
+// operand), C packed as batch x m x n. Vector-shaped products split over k
+// into the workspace when it holds MultiplyPlainBatchedWorkspace bytes.
 int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, uint64_t sa,
                          uint64_t sb, uint64_t m, uint64_t n, uint64_t k, int dtype,
-                         int scale_exp, cudaStream_t stream);
+                         int scale_exp, void *workspace, size_t ws_bytes, cudaStream_t stream);
+
+size_t MultiplyPlainBatchedWorkspace(uint64_t batch, uint64_t m, uint64_t n, uint64_t k,
+                                     int dtype);
 
 // Batched TF32x3 product: operand planes laid out [plane][batch][rows][kpitch]
 // when batched (a_batched / b_batched), [plane][rows][kpitch] when shared.

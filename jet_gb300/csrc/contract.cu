@@ -322,6 +322,7 @@ size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const 
         ws += AlignUp(p.ba * m * k * eb);
     if (!IsIdentity(b_rank, b_perm))
         ws += AlignUp(p.bb * k * n * eb);
+    ws += AlignUp(MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype));
     return ws;
 }
 
@@ -401,9 +402,12 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
         if (rc)
             return rc;
         btp = ws;
+        ws += AlignUp(p.bb * k * n * eb);
     }
+    const size_t vec_ws = MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype);
     return MultiplyPlainBatched(at, btp, C, batch, p.ba > 1 ? m * k : 0, p.bb > 1 ? k * n : 0, m,
-                                n, k, dtype, scale_a + scale_b, st);
+                                n, k, dtype, scale_a + scale_b, vec_ws ? ws : nullptr, vec_ws,
+                                st);
 }
 
 } // extern "C"

@@ -163,20 +163,26 @@ template <typename T> struct KahanSum {
     }
 };
 
-// y[m] (+ partial s) = sum_{k in chunk s} A[m, k] x[k]; one warp per row.
+// y[b, m] (+ partial s) = sum_{k in chunk s} A_b[m, k] x_b[k]; one warp per
+// row, batch b = blockIdx.z (operand strides sa, sb; 0 = shared). Partial s
+// of row (b, m) lands at out[(s * batch + b) * M + m].
 template <typename T>
 __global__ void __launch_bounds__(256)
     gemv_rows_kernel(const typename C2<T>::type *__restrict__ A,
                      const typename C2<T>::type *__restrict__ x,
                      typename C2<T>::type *__restrict__ out, int64_t M,
-                     int64_t K, int64_t kchunk, T scale)
+                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb)
 {
     using V = typename C2<T>::type;
     const int lane = threadIdx.x & 31;
     const int64_t m = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
     const int64_t s = blockIdx.y;
+    const int64_t b = blockIdx.z;
     if (m >= M)
         return;
+    A += b * sa;
+    x += b * sb;
+    out += (s * gridDim.z + b) * M;
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
     KahanSum<T> sr, si;
@@ -192,21 +198,27 @@ __global__ void __launch_bounds__(256)
         im += __shfl_xor_sync(0xffffffffu, im, o);
     }
     if (lane == 0)
-        out[s * M + m] = V{re * scale, im * scale};
+        out[m] = V{re * scale, im * scale};
 }
 
-// y[n] (+ partial s) = sum_{k in chunk s} x[k] B[k, n]; one thread per column.
+// y[b, n] (+ partial s) = sum_{k in chunk s} x_b[k] B_b[k, n]; one thread
+// per column, batch b = blockIdx.z (strides sa, sb; 0 = shared). Partial s of
+// column (b, n) lands at out[(s * batch + b) * N + n].
 template <typename T>
 __global__ void __launch_bounds__(256)
     gemv_cols_kernel(const typename C2<T>::type *__restrict__ x,
                      const typename C2<T>::type *__restrict__ B,
                      typename C2<T>::type *__restrict__ out, int64_t N,
-                     int64_t K, int64_t kchunk, T scale)
+                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb)
 {
     using V = typename C2<T>::type;
     const int64_t s = blockIdx.y;
+    const int64_t b = blockIdx.z;
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
+    x += b * sa;
+    B += b * sb;
+    out += (s * gridDim.z + b) * N;
     if (N == 1) {
         // Dot product: the block reduces its k chunk.
         KahanSum<T> sr, si;
@@ -228,7 +240,7 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
         }
         if (threadIdx.x == 0)
-            out[s] = V{sre[0] * scale, sim[0] * scale};
+            out[0] = V{sre[0] * scale, sim[0] * scale};
         return;
     }
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -240,63 +252,7 @@ __global__ void __launch_bounds__(256)
         sr.add(fma(a.x, b.x, -a.y * b.y));
         si.add(fma(a.x, b.y, a.y * b.x));
     }
-    out[s * N + n] = V{sr.s * scale, si.s * scale};
-}
-
-// Batched vector products: row r of batch b (n == 1) or column c of batch b
-// (m == 1); operand strides sa, sb (0 = shared).
-template <typename T>
-__global__ void __launch_bounds__(256)
-    gemv_rows_batched(const typename C2<T>::type *__restrict__ A,
-                      const typename C2<T>::type *__restrict__ x,
-                      typename C2<T>::type *__restrict__ out, int64_t batch, int64_t M,
-                      int64_t K, int64_t sa, int64_t sb, T scale)
-{
-    using V = typename C2<T>::type;
-    const int lane = threadIdx.x & 31;
-    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (row >= batch * M)
-        return;
-    const int64_t b = row / M, m = row - b * M;
-    const V *a = A + b * sa + m * K;
-    const V *v = x + b * sb;
-    KahanSum<T> sr, si;
-    for (int64_t k = lane; k < K; k += 32) {
-        V p = a[k], q = v[k];
-        sr.add(fma(p.x, q.x, -p.y * q.y));
-        si.add(fma(p.x, q.y, p.y * q.x));
-    }
-    T re = sr.s, im = si.s;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        re += __shfl_xor_sync(0xffffffffu, re, o);
-        im += __shfl_xor_sync(0xffffffffu, im, o);
-    }
-    if (lane == 0)
-        out[row] = V{re * scale, im * scale};
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-    gemv_cols_batched(const typename C2<T>::type *__restrict__ x,
-                      const typename C2<T>::type *__restrict__ B,
-                      typename C2<T>::type *__restrict__ out, int64_t batch, int64_t N,
-                      int64_t K, int64_t sa, int64_t sb, T scale)
-{
-    using V = typename C2<T>::type;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= batch * N)
-        return;
-    const int64_t b = idx / N, n = idx - b * N;
-    const V *v = x + b * sa;
-    const V *bb = B + b * sb + n;
-    KahanSum<T> sr, si;
-    for (int64_t k = 0; k < K; ++k) {
-        V p = v[k], q = bb[k * N];
-        sr.add(fma(p.x, q.x, -p.y * q.y));
-        si.add(fma(p.x, q.y, p.y * q.x));
-    }
-    out[idx] = V{sr.s * scale, si.s * scale};
+    out[n] = V{sr.s * scale, si.s * scale};
 }
 
 template <typename T>
@@ -338,18 +294,62 @@ int64_t SplitK(int64_t blocks_per_split, int64_t K)
     return s < 1 ? 1 : s;
 }
 
+// CTAs per batch element of the vector kernels, and the vector length.
+inline void VectorShape(int64_t m, int64_t n, int64_t &blocks, int64_t &len)
+{
+    if (n == 1 && m > 1) {
+        blocks = (m + 7) / 8; // gemv_rows_kernel: 8 rows per CTA
+        len = m;
+    }
+    else {
+        blocks = n == 1 ? 1 : (n + 255) / 256; // gemv_cols_kernel (DOTU: one CTA)
+        len = n;
+    }
+}
+
+// Bytes of partial sums the split-k vector products of `batch` products use
+// (0 for matrix products or when one split suffices).
 template <typename T>
-size_t VectorWorkspace(int64_t m, int64_t n, int64_t k)
+size_t VectorWorkspace(int64_t batch, int64_t m, int64_t n, int64_t k)
 {
     using V = typename C2<T>::type;
-    if (m > 1 && n > 1)
+    if ((m > 1 && n > 1) || batch < 1)
         return 0;
-    int64_t len = n == 1 ? m : n;
-    int64_t blocks = n == 1 ? (m + 7) / 8 : (n == 1 ? 1 : (n + 255) / 256);
-    if (m == 1 && n == 1)
-        blocks = 1;
-    int64_t S = SplitK(blocks, k);
-    return S > 1 ? (size_t)(S * len) * sizeof(V) : 0;
+    int64_t blocks, len;
+    VectorShape(m, n, blocks, len);
+    const int64_t S = SplitK(blocks * batch, k);
+    return S > 1 ? (size_t)(S * batch * len) * sizeof(V) : 0;
+}
+
+// GEMV (n == 1), GEMV^T (m == 1) and DOTU (both) of `batch` products, split
+// over k into partial sums when the caller supplied room for them, reduced
+// in a fixed order (deterministic).
+template <typename T>
+int MultiplyVectorT(const typename C2<T>::type *A, const typename C2<T>::type *B,
+                    typename C2<T>::type *C, int64_t batch, int64_t sa, int64_t sb, int64_t M,
+                    int64_t N, int64_t K, T scale, void *ws, size_t ws_bytes,
+                    cudaStream_t stream)
+{
+    using V = typename C2<T>::type;
+    JETGPU_REQUIRE(batch <= 65535, "batch too large for one launch");
+    const size_t need = VectorWorkspace<T>(batch, M, N, K);
+    const bool split = need > 0 && ws != nullptr && ws_bytes >= need;
+    int64_t blocks, len;
+    VectorShape(M, N, blocks, len);
+    const int64_t S = split ? SplitK(blocks * batch, K) : 1;
+    const int64_t kchunk = (K + S - 1) / S;
+    V *dst = S > 1 ? (V *)ws : C;
+    const dim3 grid((unsigned)blocks, (unsigned)S, (unsigned)batch);
+    if (N == 1 && M > 1)
+        gemv_rows_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, M, K, kchunk, scale, sa, sb);
+    else
+        gemv_cols_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, N, K, kchunk, scale, sa, sb);
+    int rc = CheckLaunch(N == 1 && M > 1 ? "gemv_rows_kernel" : "gemv_cols_kernel");
+    if (rc || S == 1)
+        return rc;
+    reduce_partials<T><<<GridFor((batch * len + 255) / 256, 4), 256, 0, stream>>>(
+        dst, C, batch * len, S);
+    return CheckLaunch("reduce_partials");
 }
 
 template <typename T>
@@ -377,42 +377,13 @@ int MultiplyT(const void *Av, const void *Bv, void *Cv, int64_t M, int64_t N,
         gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, 0, 0);
         return CheckLaunch("gemm_kernel");
     }
-    // Split over k only when the caller supplied room for the partial sums.
-    const size_t need = VectorWorkspace<T>(M, N, K);
-    const bool split = need > 0 && ws != nullptr && ws_bytes >= need;
-    if (N == 1 && M > 1) {
-        int64_t blocks = (M + 7) / 8;
-        int64_t S = split ? SplitK(blocks, K) : 1;
-        int64_t kchunk = (K + S - 1) / S;
-        V *dst = S > 1 ? (V *)ws : C;
-        gemv_rows_kernel<T><<<dim3((unsigned)blocks, (unsigned)S), 256, 0,
-                              stream>>>(A, B, dst, M, K, kchunk, scale);
-        int rc = CheckLaunch("gemv_rows_kernel");
-        if (rc || S == 1)
-            return rc;
-        reduce_partials<T><<<GridFor((M + 255) / 256, 4), 256, 0, stream>>>(
-            dst, C, M, S);
-        return CheckLaunch("reduce_partials");
-    }
-    // M == 1 (GEMV^T, or DOTU when N == 1).
-    int64_t blocks = N == 1 ? 1 : (N + 255) / 256;
-    int64_t S = split ? SplitK(blocks, K) : 1;
-    int64_t kchunk = (K + S - 1) / S;
-    V *dst = S > 1 ? (V *)ws : C;
-    gemv_cols_kernel<T><<<dim3((unsigned)blocks, (unsigned)S), 256, 0,
-                          stream>>>(A, B, dst, N, K, kchunk, scale);
-    int rc = CheckLaunch("gemv_cols_kernel");
-    if (rc || S == 1)
-        return rc;
-    reduce_partials<T><<<GridFor((N + 255) / 256, 4), 256, 0, stream>>>(
-        dst, C, N, S);
-    return CheckLaunch("reduce_partials");
+    return MultiplyVectorT<T>(A, B, C, 1, 0, 0, M, N, K, scale, ws, ws_bytes, stream);
 }
 
 template <typename T>
 int MultiplyBatchedT(const void *Av, const void *Bv, void *Cv, int64_t batch, int64_t sa,
-                     int64_t sb, int64_t M, int64_t N, int64_t K, int scale_exp,
-                     cudaStream_t stream)
+                     int64_t sb, int64_t M, int64_t N, int64_t K, int scale_exp, void *ws,
+                     size_t ws_bytes, cudaStream_t stream)
 {
     using V = typename C2<T>::type;
     const V *A = (const V *)Av;
@@ -433,36 +404,35 @@ int MultiplyBatchedT(const void *Av, const void *Bv, void *Cv, int64_t batch, in
         gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, sa, sb);
         return CheckLaunch("gemm_kernel (batched)");
     }
-    if (N == 1) {
-        const int64_t rows = batch * M;
-        gemv_rows_batched<T><<<(unsigned)((rows + 7) / 8), 256, 0, stream>>>(A, B, C, batch, M, K,
-                                                                            sa, sb, scale);
-        return CheckLaunch("gemv_rows_batched");
-    }
-    const int64_t cols = batch * N;
-    gemv_cols_batched<T><<<(unsigned)((cols + 255) / 256), 256, 0, stream>>>(A, B, C, batch, N,
-                                                                            K, sa, sb, scale);
-    return CheckLaunch("gemv_cols_batched");
+    return MultiplyVectorT<T>(A, B, C, batch, sa, sb, M, N, K, scale, ws, ws_bytes, stream);
 }
 
 } // namespace
 
 int MultiplyPlainBatched(const void *A, const void *B, void *C, uint64_t batch, uint64_t sa,
                          uint64_t sb, uint64_t m, uint64_t n, uint64_t k, int dtype,
-                         int scale_exp, cudaStream_t stream)
+                         int scale_exp, void *workspace, size_t ws_bytes, cudaStream_t stream)
 {
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     if (dtype == JETGPU_C128)
         return MultiplyBatchedT<double>(A, B, C, (int64_t)batch, (int64_t)sa, (int64_t)sb,
-                                        (int64_t)m, (int64_t)n, (int64_t)k, scale_exp, stream);
+                                        (int64_t)m, (int64_t)n, (int64_t)k, scale_exp, workspace,
+                                        ws_bytes, stream);
     return MultiplyBatchedT<float>(A, B, C, (int64_t)batch, (int64_t)sa, (int64_t)sb, (int64_t)m,
-                                   (int64_t)n, (int64_t)k, scale_exp, stream);
+                                   (int64_t)n, (int64_t)k, scale_exp, workspace, ws_bytes,
+                                   stream);
 }
 
 size_t MultiplyPlainWorkspace(uint64_t m, uint64_t n, uint64_t k, int dtype)
 {
-    return dtype == JETGPU_C128 ? VectorWorkspace<double>(m, n, k)
-                                : VectorWorkspace<float>(m, n, k);
+    return MultiplyPlainBatchedWorkspace(1, m, n, k, dtype);
+}
+
+size_t MultiplyPlainBatchedWorkspace(uint64_t batch, uint64_t m, uint64_t n, uint64_t k,
+                                     int dtype)
+{
+    return dtype == JETGPU_C128 ? VectorWorkspace<double>(batch, m, n, k)
+                                : VectorWorkspace<float>(batch, m, n, k);
 }
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
