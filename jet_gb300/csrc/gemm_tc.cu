@@ -247,6 +247,19 @@ __device__ __forceinline__ void TmemLoad16(uint32_t taddr, float (&v)[16])
         v[i] = __uint_as_float(r[i]);
 }
 
+// (a0, a1) += (b0, b1) with one packed instruction; each lane is an IEEE
+// round-to-nearest FP32 add, so the result equals two scalar adds.
+__device__ __forceinline__ void AddF32x2(float &a0, float &a1, float b0, float b1)
+{
+    asm("{\n\t.reg .b64 pa, pb;\n\t"
+        "mov.b64 pa, {%0, %1};\n\t"
+        "mov.b64 pb, {%2, %3};\n\t"
+        "add.rn.f32x2 pa, pa, pb;\n\t"
+        "mov.b64 {%0, %1}, pa;\n\t}"
+        : "+f"(a0), "+f"(a1)
+        : "f"(b0), "f"(b1));
+}
+
 __device__ __forceinline__ void TmemWaitLoad()
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -487,9 +500,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 TmemLoad16(col0 + kBN + c, im);
                 TmemWaitLoad();
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    acc_re[c + j] += re[j];
-                    acc_im[c + j] += im[j];
+                for (int j = 0; j < 16; j += 2) {
+                    AddF32x2(acc_re[c + j], acc_re[c + j + 1], re[j], re[j + 1]);
+                    AddF32x2(acc_im[c + j], acc_im[c + j + 1], im[j], im[j + 1]);
                 }
             }
             FenceBeforeSync();
