@@ -117,10 +117,13 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
                             uint64_t k, uint64_t kpitch, float out_scale, cudaStream_t stream);
 
 // The batched split product for either word format (kpitch in words).
+// `variant`: main-loop variant (jetgpu_set_tc_variant) read once by the
+// caller, so the planes it wrote and the loop that reads them agree; -1 reads
+// the current setting.
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream);
+                           cudaStream_t stream, int variant = -1);
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,
@@ -138,5 +141,6 @@ bool TcAvailable();
 // Main-loop shape of the tensor-core product: wide (N = 256 MMAs) needs six B
 // planes (re hi/lo, im hi/lo, -im hi/lo), narrow four.
 bool TcWide();
+int TcVariant();
 
 } // namespace jetgpu

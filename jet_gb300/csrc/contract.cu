@@ -25,6 +25,7 @@ inline size_t AlignUp(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 // Word format, row pitch and plane counts of the split form.
 struct SplitLayout {
     SplitFormat fmt;
+    int variant;      // main-loop variant, read once
     uint64_t kp;      // row pitch in words
     uint64_t word;    // bytes per word
     int b_planes;     // 4, or 6 for the N = 256 TF32 main loop
@@ -39,7 +40,8 @@ SplitLayout LayoutFor(int precision, uint64_t k)
     const uint64_t al = SplitPitchAlign(l.fmt);
     l.kp = (k + al - 1) / al * al;
     l.word = SplitWordBytes(l.fmt);
-    l.b_planes = (l.fmt == SplitFormat::kTf32 && TcWide()) ? 6 : 4;
+    l.variant = TcVariant();
+    l.b_planes = (l.fmt == SplitFormat::kTf32 && l.variant == 1) ? 6 : 4;
     return l;
 }
 
@@ -178,7 +180,8 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
                                 scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st);
         if (rc)
             return rc;
-        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, 1.0f, l.fmt, st);
+        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, 1.0f, l.fmt, st,
+                                      l.variant);
     }
 
     const size_t eb = ElemBytes(dtype);
@@ -385,7 +388,7 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
         if (rc)
             return rc;
         return GemmSplitPlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, l.kp, 1.0f,
-                                      l.fmt, st);
+                                      l.fmt, st, l.variant);
     }
     const size_t eb = ElemBytes(dtype);
     const void *at = A;

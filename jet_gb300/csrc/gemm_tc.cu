@@ -26,6 +26,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -88,11 +89,14 @@ template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * TileBytes
 // truncation (about 4.5e-6 per product) dominates any accumulation error.
 constexpr int kDefaultChunkKTf32 = 16;
 constexpr int kDefaultChunkKBf16 = 128;
-int g_tc_chunk_k = 0; // K depth per TMEM chunk (jetgpu_set_tc_chunk_depth; 0 = default)
+// K depth per TMEM chunk (jetgpu_set_tc_chunk_depth; 0 = default). Process-wide,
+// read at every launch: atomic so a setter on one thread never tears a read.
+std::atomic<int> g_tc_chunk_k{0};
 
 inline int ChunkStages(bool bf16, int stage_k)
 {
-    int depth = g_tc_chunk_k > 0 ? g_tc_chunk_k : (bf16 ? kDefaultChunkKBf16 : kDefaultChunkKTf32);
+    const int set = g_tc_chunk_k.load(std::memory_order_relaxed);
+    int depth = set > 0 ? set : (bf16 ? kDefaultChunkKBf16 : kDefaultChunkKTf32);
     int stages = depth / stage_k;
     return stages < 1 ? 1 : stages;
 }
@@ -630,7 +634,7 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
 
 // Main-loop variant (jetgpu_set_tc_variant): 0 default, 1 TF32 N = 256,
 // 2 BF16 with 32-byte rows and 6 stages.
-int g_tc_variant = 0;
+std::atomic<int> g_tc_variant{0};
 
 } // namespace
 
@@ -653,7 +657,7 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream)
+                           cudaStream_t stream, int variant)
 {
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
@@ -674,8 +678,10 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
     int rc = GetEncoder();
     if (rc)
         return rc;
-    const bool wide = !bf16 && g_tc_variant == 1;
-    const bool deep = bf16 && g_tc_variant == 2;
+    if (variant < 0)
+        variant = TcVariant();
+    const bool wide = !bf16 && variant == 1;
+    const bool deep = bf16 && variant == 2;
     const int row_bytes = deep ? TcCfg<3>::RowBytes : TcCfg<0>::RowBytes;
     CUtensorMap ta, tb;
     if ((rc = a_batched
@@ -696,7 +702,8 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                               stream);
 }
 
-bool TcWide() { return g_tc_variant == 1; }
+int TcVariant() { return g_tc_variant.load(std::memory_order_relaxed); }
+bool TcWide() { return TcVariant() == 1; }
 
 } // namespace jetgpu
 
@@ -707,7 +714,7 @@ extern "C" int jetgpu_set_tc_variant(int variant)
     jetgpu::ClearError();
     JETGPU_REQUIRE(variant >= 0 && variant <= 2,
                    "variant must be 0 (default), 1 (TF32 N = 256) or 2 (BF16 6-stage)");
-    jetgpu::g_tc_variant = variant;
+    jetgpu::g_tc_variant.store(variant, std::memory_order_relaxed);
     return JETGPU_OK;
 }
 
@@ -715,7 +722,7 @@ extern "C" int jetgpu_set_tc_chunk_depth(int k_depth)
 {
     jetgpu::ClearError();
     JETGPU_REQUIRE(k_depth >= 0 && k_depth <= 4096, "chunk depth out of range");
-    jetgpu::g_tc_chunk_k = k_depth;
+    jetgpu::g_tc_chunk_k.store(k_depth, std::memory_order_relaxed);
     return JETGPU_OK;
 }
 

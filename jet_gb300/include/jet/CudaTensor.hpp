@@ -176,8 +176,17 @@ template <class T = cuComplex, int CUDA_DEVICE = 0> class CudaTensor {
         return axes;
     }
 
-    T *GetData() { return reinterpret_cast<T *>(rm_.GetMutableDeviceData()); }
-    const T *GetData() const { return reinterpret_cast<const T *>(rm_.GetDeviceData()); }
+    // Device data (allocated on first use, under the tensor's device).
+    T *GetData()
+    {
+        CudaTensorHelpers::CudaScopedDevice ctx(CUDA_DEVICE);
+        return reinterpret_cast<T *>(rm_.GetMutableDeviceData());
+    }
+    const T *GetData() const
+    {
+        CudaTensorHelpers::CudaScopedDevice ctx(CUDA_DEVICE);
+        return reinterpret_cast<const T *>(rm_.GetDeviceData());
+    }
 
     void RenameIndex(size_t ind, std::string new_string)
     {
