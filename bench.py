@@ -234,29 +234,40 @@ def run_ours(args, rank, world, local_rank):
 
     def run_form(form):
         """Times `args.steps` steps of split A, split B, split product."""
-        bf = form == "bf16x3"
-        word = torch.int16 if bf else torch.float32
-        bplanes = 4 if bf else capi.tc_b_planes()
+        bf, hf = form == "bf16x3", form == "fp16x3"
+        word = torch.int16 if (bf or hf) else torch.float32
+        bplanes = 4 if (bf or hf) else capi.tc_b_planes()
         pa = torch.empty(4 * m * kp, dtype=word, device=dev)
         pb = torch.empty(bplanes * n * kp, dtype=word, device=dev)
+        e2 = torch.empty(2, dtype=torch.int32, device=dev)  # FP16: max exponents of A, B
 
         def step(events=None):
             if events:
                 events[0].record(stream)
-            if bf:
+            if hf:
+                capi.max_exponent(A, stream=stream, out=e2[0:1])
+                capi.split_fp16(A, w["a_shape"], w["a_perm"], m, k, kp, pa, e2[0:1],
+                                stream=stream)
+            elif bf:
                 capi.split_bf16(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
             else:
                 capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
             if events:
                 events[1].record(stream)
-            if bf:
+            if hf:
+                capi.max_exponent(B, stream=stream, out=e2[1:2])
+                capi.split_fp16(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, e2[1:2],
+                                stream=stream)
+            elif bf:
                 capi.split_bf16(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, stream=stream)
             else:
                 capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb,
                                 n_planes=bplanes, stream=stream)
             if events:
                 events[2].record(stream)
-            if bf:
+            if hf:
+                capi.gemm_fp16x3(pa, pb, m, n, k, kp, C, e2, stream=stream)
+            elif bf:
                 capi.gemm_bf16x3(pa, pb, m, n, k, kp, C, stream=stream)
             else:
                 capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
@@ -295,11 +306,13 @@ def run_ours(args, rank, world, local_rank):
         del pa, pb
         return out
 
-    forms = ["tf32x3", "bf16x3"] if args.form == "auto" else [args.form]
+    forms = ["tf32x3", "bf16x3", "fp16x3"] if args.form == "auto" else [args.form]
     results = {f: run_form(f) for f in forms}
     if args.form == "auto":
-        # The faster form if it meets the 1e-5 bound on this step, else TF32x3.
-        head = "bf16x3" if results["bf16x3"]["rel_err_vs_fp64"] <= 1e-5 else "tf32x3"
+        # The fastest form whose error on this step meets the 1e-5 bound
+        # (TF32x3 if none does).
+        ok = [f for f in forms if results[f]["rel_err_vs_fp64"] <= 1e-5] or ["tf32x3"]
+        head = min(ok, key=lambda f: results[f]["ms_per_step"])
     else:
         head = args.form
     hr = results[head]
@@ -310,7 +323,8 @@ def run_ours(args, rank, world, local_rank):
         return
     ms_step, value, rel_err = hr["ms_per_step"], hr["value"], hr["rel_err_vs_fp64"]
     clocks, wall = hr["clocks"], hr["wall_s_timed"]
-    head_prec = capi.PREC_BF16X3 if head == "bf16x3" else capi.PREC_TF32X3
+    head_prec = {"tf32x3": capi.PREC_TF32X3, "bf16x3": capi.PREC_BF16X3,
+                 "fp16x3": capi.PREC_FP16X3}[head]
 
     # Plain FP32 form of the same step (permute + SIMT complex GEMM), 2 runs.
     ws_need = capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
@@ -388,17 +402,20 @@ def run_ours(args, rank, world, local_rank):
     hbm_peak, bf16_peak, peak_src = measured_peaks()
     # Dense tensor rate of the headline form's operand type: BF16 = measured
     # bf16, TF32 = half of it.
-    tc_peak = bf16_peak if head == "bf16x3" else bf16_peak / 2.0
+    tc_peak = bf16_peak / 2.0 if head == "tf32x3" else bf16_peak
     gemm_ms = hr["stages_ms"]["gemm"]
     split_ms = hr["stages_ms"]["split_a"]
-    # A per element: read 8 B, write 4 planes x (2 B BF16 | 4 B TF32).
-    split_bytes = (16.0 if head == "bf16x3" else 24.0) * m * k
+    # A per element: read 8 B, write 4 planes x (2 B BF16 / FP16 | 4 B TF32);
+    # FP16 also reads A once more for its max exponent.
+    split_bytes = {"tf32x3": 24.0, "bf16x3": 16.0, "fp16x3": 24.0}[head] * m * k
     achieved = flops / (gemm_ms * 1e-3) / 1e12
     # DRAM bytes (read + write) per launch of the product at this size, from
     # one ncu capture (profiles/tc_gemm_split_bf16_config1_launches.md).
-    traffic = 7.67e9 if head == "bf16x3" else 14.77e9
+    traffic = 14.77e9 if head == "tf32x3" else 7.67e9
     form_names = {"tf32x3": "TF32x3 4M (tcgen05 kind::tf32, hi/lo split, 3 products)",
-                  "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)"}
+                  "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)",
+                  "fp16x3": "FP16x3 4M (tcgen05 kind::f16 on FP16 hi/lo of power-of-two "
+                            "scaled operands, 3 products)"}
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -417,17 +434,21 @@ def run_ours(args, rank, world, local_rank):
         "plain_fp32": {"ms_per_step": plain_ms,
                        "value": world * flops / (plain_ms * 1e-3) / 1e12,
                        "rel_err_vs_fp64": plain_err},
-        "roofline": {"bound": "tensor", "kernel": "tc_gemm_split_kernel<%d>" % (2 if head == "bf16x3" else 0),
+        "roofline": {"bound": "tensor",
+                     "kernel": "tc_gemm_split_kernel<%d>" % {"tf32x3": 0, "bf16x3": 2,
+                                                             "fp16x3": 4}[head],
                      "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
                      "frac": achieved / tc_peak,
                      "tensor_pipe_frac": 3 * achieved / tc_peak,
                      "peak_source": ("%s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak))
-                     if head == "bf16x3" else
+                     if head != "tf32x3" else
                      ("TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak)),
                      "traffic": traffic,
-                     "traffic_algorithmic": (16.0 if head == "bf16x3" else 32.0) * (m + n) * k
+                     "traffic_algorithmic": (32.0 if head == "tf32x3" else 16.0) * (m + n) * k
                      / 2.0 + 8.0 * m * n},
-        "roofline_split": {"bound": "hbm", "kernel": "bitperm_kernel (split store)",
+        "roofline_split": {"bound": "hbm",
+                           "kernel": "max_exp_kernel + bitperm_kernel (split store)"
+                           if head == "fp16x3" else "bitperm_kernel (split store)",
                            "achieved": split_bytes / (split_ms * 1e-3) / 1e9, "peak": hbm_peak,
                            "unit": "GB/s",
                            "frac": split_bytes / (split_ms * 1e-3) / 1e9 / hbm_peak,
@@ -438,7 +459,9 @@ def run_ours(args, rank, world, local_rank):
                 "rel_err_vs_fp64": e2e_err,
                 "pipeline": "two device buffer sets; H2D and D2H on copy streams overlap "
                             "the contractions"},
-        "gpu_launches": 3 * args.steps,
+        # per step: 2 splits + 1 product (FP16: + one max-exponent kernel per
+        # operand, each after a 4-byte memset)
+        "gpu_launches": (5 if head == "fp16x3" else 3) * args.steps,
         "wall_s_timed": wall,
         "clocks": clocks,
     }
@@ -468,12 +491,13 @@ def run_sliced(args, rank, world, local_rank):
     """Sliced random-circuit amplitudes through Jet::SlicedContractor: every
     slice of a seeded circuit network along one greedy path, in batched
     launches replayed from one CUDA graph, FP64 slice sum. Reports slices/s
-    and effective TFLOP/s (4 x PathInfo flops per slice) for the AUTO
-    (TF32x3 on large steps) and plain FP32 forms."""
+    and effective TFLOP/s (4 x PathInfo flops per slice) for AUTO (FP16x3 on
+    the large steps; auto_tf32: TF32x3 there), BF16x3 and plain FP32, each
+    with its amplitude error against complex128 under --check-fp64."""
     import torch
 
     import jet_gb300 as jet
-    from jet_gb300 import circuits
+    from jet_gb300 import capi, circuits
 
     torch.cuda.set_device(local_rank)
     rows, cols, cycles, removed, n_sliced, batch, chunks, restarts = SLICED_CONFIGS[args.config]
@@ -503,11 +527,14 @@ def run_sliced(args, rank, world, local_rank):
         tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
     forms = {}
     amps = {}
-    sliced_forms = tuple((f, p) for f, p in (("auto", jet.PREC_AUTO),
-                                             ("bf16x3", jet.PREC_BF16X3),
-                                             ("fp32", jet.PREC_FP32))
-                         if f in args.sliced_forms.split(","))
-    for name, prec in sliced_forms:
+    # (name, precision, split form of AUTO's tensor-core steps)
+    all_forms = (("auto", jet.PREC_AUTO, capi.PREC_FP16X3),
+                 ("auto_tf32", jet.PREC_AUTO, capi.PREC_TF32X3),
+                 ("bf16x3", jet.PREC_BF16X3, None),
+                 ("fp32", jet.PREC_FP32, None))
+    sliced_forms = tuple(f for f in all_forms if f[0] in args.sliced_forms.split(","))
+    for name, prec, auto_form in sliced_forms:
+        capi.set_auto_form(auto_form or capi.PREC_FP16X3)
         sc = jet.SlicedContractorC64(tn, path, sliced, prec)
         sc.set_batch_size(batch)
         n_all = sc.num_slices
@@ -547,7 +574,8 @@ def run_sliced(args, rank, world, local_rank):
         del sc
         slice_check = {"reference": "complex128 FP64 on the GPU, slice 0",
                        "value": [ref64.real, ref64.imag]}
-        for name, prec in sliced_forms:
+        for name, prec, auto_form in sliced_forms:
+            capi.set_auto_form(auto_form or capi.PREC_FP16X3)
             sc = jet.SlicedContractorC64(tn, path, sliced, prec)
             sc.set_batch_size(1)
             v = sc.contract(0, 1)[0]
@@ -676,11 +704,12 @@ def main():
                     help="skip the plain-FP32, end-to-end and CPU legs")
     ap.add_argument("--check-fp64", action="store_true",
                     help="sliced configs: also contract slice 0 in complex128")
-    ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3"],
-                    help="split form of the config-1 step (auto: both timed, the headline is "
-                         "BF16x3 when its error on the step is within 1e-5, else TF32x3)")
-    ap.add_argument("--sliced-forms", default="auto,bf16x3,fp32",
-                    help="forms timed by the sliced configs (comma list of auto, bf16x3, fp32)")
+    ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3", "fp16x3"],
+                    help="split form of the config-1 step (auto: all timed, the headline is "
+                         "the fastest whose error on the step is within 1e-5)")
+    ap.add_argument("--sliced-forms", default="auto,auto_tf32,fp32",
+                    help="forms timed by the sliced configs (comma list of auto (FP16x3 on "
+                         "the tensor-core steps), auto_tf32, bf16x3, fp32)")
     ap.add_argument("--sliced-batch", type=int, default=0,
                     help="slices per batch of the sliced configs (0: the config's own)")
     ap.add_argument("--sliced-chunks", type=int, default=0,

@@ -40,9 +40,13 @@ extern "C" {
 /* Arithmetic forms of a contraction. */
 #define JETGPU_PREC_FP32 0   /* plain: complex FMA in the element type (FP32 or FP64) */
 #define JETGPU_PREC_TF32X3 1 /* tcgen05 kind::tf32, hi/lo split, 3 products, FP32 accumulate */
-#define JETGPU_PREC_AUTO 2   /* TF32x3 where the shape suits the tensor cores, else plain */
+#define JETGPU_PREC_AUTO 2   /* a split form (FP16x3 unless jetgpu_set_auto_form says otherwise)
+                                where the shape suits the tensor cores, else plain */
 #define JETGPU_PREC_BF16X3 3 /* tcgen05 kind::f16 on BF16 hi/lo splits, 3 products, FP32
                                 accumulate: twice the TF32 rate, ~2^-17 truncation per product */
+#define JETGPU_PREC_FP16X3 4 /* tcgen05 kind::f16 on FP16 hi/lo splits of power-of-two scaled
+                                operands, 3 products, FP32 accumulate: twice the TF32 rate,
+                                ~2^-22 truncation per product (TF32x3's) */
 
 /* Complex product algorithms for the tensor-core form. */
 #define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
@@ -146,9 +150,10 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
  * dimensions. Replaces Tensor::ContractTensors (include/jet/Tensor.hpp:708-752)
  * after its label algebra; the label algebra stays on the host.
  *
- * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3 or JETGPU_PREC_BF16X3
- * (complex64 only; shapes with m or n below 2 take the plain form) or
- * JETGPU_PREC_AUTO. algo: JETGPU_ALGO_4M.
+ * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3, JETGPU_PREC_BF16X3 or
+ * JETGPU_PREC_FP16X3 (complex64 only; shapes with m or n below 2 take the
+ * plain form) or JETGPU_PREC_AUTO. algo: JETGPU_ALGO_4M. FP16X3 needs
+ * |scale_a + scale_b| <= 126.
  * scale_a, scale_b: power-of-two exponents applied exactly to A and B before
  * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
  * workspace: caller-owned device scratch of at least
@@ -271,6 +276,13 @@ int jetgpu_tc_b_planes(void);
  */
 int jetgpu_set_tc_chunk_depth(int k_depth);
 
+/*
+ * jetgpu_set_auto_form selects, for the calling process, the split form that
+ * JETGPU_PREC_AUTO uses on the steps it gives to the tensor cores:
+ * JETGPU_PREC_FP16X3 (the default), JETGPU_PREC_TF32X3 or JETGPU_PREC_BF16X3.
+ */
+int jetgpu_set_auto_form(int precision);
+
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                        float out_scale, void *stream);
@@ -296,6 +308,30 @@ int jetgpu_split_bf16(const void *in, int rank, const uint64_t *shape,
 int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                        float out_scale, void *stream);
+
+/*
+ * The stages of the FP16x3 form (JETGPU_PREC_FP16X3), which keeps TF32x3's
+ * precision (11 significant bits per piece) at the FP16 tensor rate. FP16's
+ * range is covered by scaling each operand by 2^s before the split, s = 14 -
+ * e_max clamped to [-120, 120], e_max from jetgpu_max_exponent on the device,
+ * so the operand's largest magnitude lies in [2^14, 2^15).
+ *
+ * jetgpu_split_fp16: as jetgpu_split_bf16 with FP16 words of 2^s x
+ * (hi = RN_fp16(2^s x), lo = RN_fp16(2^s x - hi)); *e_max_dev is read on the
+ * device.
+ *
+ * jetgpu_gemm_fp16x3: C = A * B^T from four FP16 planes of A and of B;
+ * e_max_dev points at two device ints, the max exponents of A and B, whose
+ * scales the epilogue removes; the output is also multiplied by out_scale.
+ */
+int jetgpu_split_fp16(const void *in, int rank, const uint64_t *shape,
+                      const int32_t *perm, uint64_t rows, uint64_t cols,
+                      uint64_t pitch, uint64_t plane_stride, const int *e_max_dev,
+                      uint16_t *planes, void *stream);
+
+int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C,
+                       uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
+                       const int *e_max_dev, float out_scale, void *stream);
 
 /*
  * Element-wise sum C = A + B of equal-size tensors whose data are already in

@@ -8,7 +8,7 @@ factories over the TensorC64/C128, ... classes) and the free functions
 slice runs as a CUDA kernel of libjetgpu.so (sm_103a). Importing the package
 fails when the native libraries are not built: there is no CPU fallback.
 
-Extras: `set_precision` (0 plain FP32, 1 TF32x3 tensor cores, 2 auto, 3 BF16x3) and the
+Extras: `set_precision` (0 plain FP32, 1 TF32x3 tensor cores, 2 auto, 3 BF16x3, 4 FP16x3) and the
 raw C-ABI binding `jet_gb300.capi`.
 """
 from ._jet_bindings import (  # noqa: F401
@@ -34,5 +34,6 @@ PREC_FP32 = 0
 PREC_TF32X3 = 1
 PREC_AUTO = 2
 PREC_BF16X3 = 3
+PREC_FP16X3 = 4
 
 __version__ = version()

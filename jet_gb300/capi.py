@@ -42,6 +42,7 @@ PREC_FP32 = 0
 PREC_TF32X3 = 1
 PREC_AUTO = 2
 PREC_BF16X3 = 3
+PREC_FP16X3 = 4
 
 ALGO_4M = 0
 
@@ -68,6 +69,7 @@ lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   ctypes.c_int, _vp, _vp]
 lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
 lib.jetgpu_set_tc_chunk_depth.argtypes = [ctypes.c_int]
+lib.jetgpu_set_auto_form.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
 lib.jetgpu_split_bf16.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
@@ -75,6 +77,10 @@ lib.jetgpu_split_bf16.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   _vp, _vp]
 lib.jetgpu_gemm_bf16x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_float, _vp]
+lib.jetgpu_split_fp16.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp]
+lib.jetgpu_gemm_fp16x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_uint64, ctypes.c_uint64, _vp, ctypes.c_float, _vp]
 lib.jetgpu_contract_batched_workspace_size.restype = ctypes.c_size_t
 lib.jetgpu_contract_batched_workspace_size.argtypes = [
     ctypes.c_uint64, ctypes.c_int, _u64p, _i32p, ctypes.c_int, ctypes.c_int, _u64p, _i32p,
@@ -233,6 +239,12 @@ def set_tc_variant(variant: int) -> None:
     check(lib.jetgpu_set_tc_variant(int(variant)))
 
 
+def set_auto_form(precision: int) -> None:
+    """Split form of PREC_AUTO's tensor-core steps: PREC_FP16X3 (default),
+    PREC_TF32X3 or PREC_BF16X3."""
+    check(lib.jetgpu_set_auto_form(int(precision)))
+
+
 def set_tc_chunk_depth(k_depth: int) -> None:
     """K depth accumulated in tensor memory per fold (0 = defaults)."""
     check(lib.jetgpu_set_tc_chunk_depth(int(k_depth)))
@@ -258,6 +270,22 @@ def split_bf16(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, stream=No
 def gemm_bf16x3(a_planes, b_planes, m, n, k, kpitch, out, out_scale=1.0, stream=None):
     check(lib.jetgpu_gemm_bf16x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
                                  out_scale, _stream(stream)))
+    return out
+
+
+def split_fp16(x, shape, perm, rows, cols, pitch, planes, e_max, stream=None):
+    """Permute + FP16 hi/lo split of x scaled by 2^(14 - *e_max) (e_max: a
+    device int32 tensor holding the max exponent of x)."""
+    check(lib.jetgpu_split_fp16(_ptr(x), len(shape), u64(shape), i32(perm), rows, cols, pitch,
+                                rows * pitch, _ptr(e_max), _ptr(planes), _stream(stream)))
+    return planes
+
+
+def gemm_fp16x3(a_planes, b_planes, m, n, k, kpitch, out, e_max2, out_scale=1.0, stream=None):
+    """FP16x3 product of split planes; e_max2: device int32[2], the max
+    exponents of A and B."""
+    check(lib.jetgpu_gemm_fp16x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
+                                 _ptr(e_max2), out_scale, _stream(stream)))
     return out
 
 
@@ -306,13 +334,15 @@ def slice_gather(x, shape, axes, value_strides, first_value, n_values, out=None,
     return out
 
 
-def max_exponent(x, stream=None) -> int:
+def max_exponent(x, stream=None, out=None):
+    """Max binary exponent of |re|, |im| over x: an int, or written (without
+    synchronising) into the device int32 tensor `out` when one is given."""
     import torch
 
-    e = torch.empty(1, dtype=torch.int32, device=x.device)
+    e = out if out is not None else torch.empty(1, dtype=torch.int32, device=x.device)
     check(lib.jetgpu_max_exponent(_ptr(x), x.numel(), dtype_code(x.dtype), _ptr(e),
                                   _stream(stream)))
-    return int(e.item())
+    return e if out is not None else int(e.item())
 
 
 def take_device_status() -> int:

@@ -88,17 +88,48 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
                             int scale_exp, cudaStream_t stream, int neg_im = 0);
 
 // Word format of the split planes: TF32 (FP32 words, 13 low mantissa bits
-// zero) or BF16 (16-bit words). pitch and plane_stride count words; a row
-// pitch must span a multiple of 16 bytes (SplitPitchAlign words).
-enum class SplitFormat { kTf32 = 0, kBf16 = 1 };
-inline uint64_t SplitWordBytes(SplitFormat f) { return f == SplitFormat::kBf16 ? 2 : 4; }
-inline uint64_t SplitPitchAlign(SplitFormat f) { return f == SplitFormat::kBf16 ? 8 : 4; }
+// zero), BF16 or FP16 (16-bit words). pitch and plane_stride count words; a
+// row pitch must span a multiple of 16 bytes (SplitPitchAlign words).
+enum class SplitFormat { kTf32 = 0, kBf16 = 1, kFp16 = 2 };
+inline uint64_t SplitWordBytes(SplitFormat f) { return f == SplitFormat::kTf32 ? 4 : 2; }
+inline uint64_t SplitPitchAlign(SplitFormat f) { return f == SplitFormat::kTf32 ? 4 : 8; }
 
-// PermuteSplitTf32Batched for either word format (neg_im with TF32 only).
+// FP16 split: an operand whose largest magnitude has binary exponent e_max
+// (jetgpu_max_exponent; -1000 when all zero) is multiplied by 2^s before the
+// split, s = 14 - e_max clamped to [-120, 120], so its largest value lies in
+// [2^14, 2^15) (below the FP16 maximum 65504, hi and lo normal down to
+// 2^-15 of it). The product's epilogue multiplies by 2^-(s_A + s_B).
+__host__ __device__ inline int Fp16ScaleExp(int e_max)
+{
+    const int s = 14 - e_max;
+    return s < -120 ? -120 : (s > 120 ? 120 : s);
+}
+
+// 2^e as a float, e in [-126, 127] (exact).
+__host__ __device__ inline float Pow2f(int e)
+{
+    union {
+        uint32_t u;
+        float f;
+    } v;
+    v.u = (uint32_t)(e + 127) << 23;
+    return v.f;
+}
+
+// PermuteSplitTf32Batched for any word format (neg_im with TF32 only). For
+// FP16, `e_max_dev` points at the operand's max exponent on the device and
+// sets the scale (Fp16ScaleExp); scale_exp is then ignored.
 int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
                        const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
                        uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
-                       int neg_im, cudaStream_t stream);
+                       int neg_im, cudaStream_t stream, const int *e_max_dev = nullptr);
+
+// Device max exponent of `size` complex elements into *e_dev (stream-ordered).
+int MaxExponent(const void *x, uint64_t size, int dtype, int *e_dev, cudaStream_t stream);
+
+// Max exponents of two operands into e[0], e[1] in one fill and one launch.
+int MaxExponent2(const void *x0, uint64_t n0, const void *x1, uint64_t n1, int dtype, int *e,
+                 cudaStream_t stream, int operands = 2);
 
 // C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
 // operand), C packed as batch x m x n. Vector-shaped products split over k
@@ -120,10 +151,13 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 // `variant`: main-loop variant (jetgpu_set_tc_variant) read once by the
 // caller, so the planes it wrote and the loop that reads them agree; -1 reads
 // the current setting.
+// For FP16, `e_max_dev` points at the two operands' max exponents (A, B) and
+// the epilogue undoes their scales.
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream, int variant = -1);
+                           cudaStream_t stream, int variant = -1,
+                           const int *e_max_dev = nullptr);
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,

@@ -8,9 +8,13 @@
 // Plain form:  At = permute(A), Bt = permute(B) into the workspace (skipped
 //              when already ordered), then the SIMT complex product.
 // Split form: A is permuted straight into hi/lo planes (M x K; TF32 words for
-//              TF32x3, BF16 words for BF16x3), B into planes of its
+//              TF32x3, BF16 words for BF16x3, FP16 words of the operand
+//              scaled by a power of two for FP16x3), B into planes of its
 //              (right ++ common) order (N x K, K-major), then the tcgen05
-//              product writes C.
+//              product writes C. FP16x3 first writes each operand's max
+//              exponent into the workspace; the splits and the product's
+//              epilogue read the scales from there (no host round trip).
+#include <atomic>
 #include <vector>
 
 #include "common.cuh"
@@ -31,12 +35,33 @@ struct SplitLayout {
     int b_planes;     // 4, or 6 for the N = 256 TF32 main loop
     size_t a_bytes(uint64_t rows) const { return AlignUp(4 * rows * kp * word); }
     size_t b_bytes(uint64_t rows) const { return AlignUp(b_planes * rows * kp * word); }
+    // FP16: two ints (max exponents of A and B) after the planes.
+    size_t exp_bytes() const { return fmt == SplitFormat::kFp16 ? kAlign : 0; }
 };
 
-SplitLayout LayoutFor(int precision, uint64_t k)
+// The split form JETGPU_PREC_AUTO uses on tensor-core steps
+// (jetgpu_set_auto_form). FP16x3 by default: TF32x3's precision at twice its
+// rate (measured on sliced 49- and 53-qubit circuit amplitudes: 5.7e-6 and
+// 7.4e-6 from FP64, against TF32x3's 6.7e-6 and 7.0e-6, at 1.55x and 1.74x
+// the slices/s).
+std::atomic<int> g_auto_form{JETGPU_PREC_FP16X3};
+
+// AUTO gives FP16x3 steps of at least this many complex multiply-adds
+// (m n k, summed over a batch); below it, where the operands' max-exponent
+// pass costs more than the faster product saves, TF32x3 (same precision).
+constexpr double kAutoFp16MinWork = 1073741824.0; // 2^30
+
+SplitLayout LayoutFor(int precision, uint64_t k, double work)
 {
+    if (precision == JETGPU_PREC_AUTO) {
+        precision = g_auto_form.load(std::memory_order_relaxed);
+        if (precision == JETGPU_PREC_FP16X3 && work < kAutoFp16MinWork)
+            precision = JETGPU_PREC_TF32X3;
+    }
     SplitLayout l;
-    l.fmt = precision == JETGPU_PREC_BF16X3 ? SplitFormat::kBf16 : SplitFormat::kTf32;
+    l.fmt = precision == JETGPU_PREC_BF16X3   ? SplitFormat::kBf16
+            : precision == JETGPU_PREC_FP16X3 ? SplitFormat::kFp16
+                                              : SplitFormat::kTf32;
     const uint64_t al = SplitPitchAlign(l.fmt);
     l.kp = (k + al - 1) / al * al;
     l.word = SplitWordBytes(l.fmt);
@@ -115,8 +140,9 @@ size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
                                       int precision)
 {
     if (UseTensorCores(m, n, k, dtype, precision)) {
-        const SplitLayout l = LayoutFor(precision, k);
-        return l.a_bytes(m) + AlignUp((l.fmt == SplitFormat::kBf16 ? 4 : 6) * n * l.kp * l.word);
+        const SplitLayout l = LayoutFor(precision, k, (double)m * n * k);
+        return l.a_bytes(m) + AlignUp((l.fmt == SplitFormat::kTf32 ? 6 : 4) * n * l.kp * l.word) +
+               l.exp_bytes();
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -137,11 +163,11 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
 {
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
-    JETGPU_REQUIRE(precision == JETGPU_PREC_FP32 || precision == JETGPU_PREC_TF32X3 ||
-                       precision == JETGPU_PREC_AUTO || precision == JETGPU_PREC_BF16X3,
+    JETGPU_REQUIRE(precision >= JETGPU_PREC_FP32 && precision <= JETGPU_PREC_FP16X3,
                    "bad precision");
     JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
-    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3) &&
+    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
+         precision == JETGPU_PREC_FP16X3) &&
         dtype != JETGPU_C64)
         return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
     int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
@@ -164,24 +190,39 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
     uint8_t *ws = static_cast<uint8_t *>(workspace);
 
     if (k > 0 && UseTensorCores(m, n, k, dtype, precision)) {
-        const SplitLayout l = LayoutFor(precision, k);
+        const SplitLayout l = LayoutFor(precision, k, (double)m * n * k);
         uint8_t *pa = ws;
         uint8_t *pb = ws + l.a_bytes(m);
+        int *e_dev = nullptr;
+        float out_scale = 1.0f;
+        if (l.fmt == SplitFormat::kFp16) {
+            // Each operand's max exponent sets its FP16 scale; the user's
+            // exact scales move to the epilogue.
+            JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
+                           "scale_a + scale_b out of range for FP16x3");
+            e_dev = reinterpret_cast<int *>(
+                pb + AlignUp((size_t)l.b_planes * n * l.kp * l.word));
+            if ((rc = MaxExponent2(A, m * k, B, k * n, dtype, e_dev, st)))
+                return rc;
+            out_scale = Pow2f(scale_a + scale_b);
+            scale_a = scale_b = 0;
+        }
         // B is wanted as (right ++ common): rotate its (common ++ right) order.
         const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
         std::vector<int32_t> bt(b_rank);
         for (int j = 0; j < b_rank; ++j)
             bt[j] = b_perm[(j + nc) % b_rank];
         rc = PermuteSplitPlanes(A, pa, 1, a_rank, a_shape, a_perm, m, k, l.kp, m * l.kp, scale_a,
-                                l.fmt, 0, st);
+                                l.fmt, 0, st, e_dev);
         if (rc)
             return rc;
         rc = PermuteSplitPlanes(B, pb, 1, b_rank, b_shape, bt.data(), n, k, l.kp, n * l.kp,
-                                scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st);
+                                scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
+                                e_dev ? e_dev + 1 : nullptr);
         if (rc)
             return rc;
-        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, 1.0f, l.fmt, st,
-                                      l.variant);
+        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, out_scale, l.fmt, st,
+                                      l.variant, e_dev);
     }
 
     const size_t eb = ElemBytes(dtype);
@@ -245,6 +286,43 @@ int jetgpu_split_bf16(const void *in, int rank, const uint64_t *shape, const int
     JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
     return PermuteSplitPlanes(in, planes, 1, rank, shape, perm, rows, cols, pitch, plane_stride,
                               scale_exp, SplitFormat::kBf16, 0, AsStream(stream));
+}
+
+int jetgpu_set_auto_form(int precision)
+{
+    ClearError();
+    JETGPU_REQUIRE(precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
+                       precision == JETGPU_PREC_FP16X3,
+                   "the AUTO form must be TF32X3, BF16X3 or FP16X3");
+    g_auto_form.store(precision, std::memory_order_relaxed);
+    return JETGPU_OK;
+}
+
+int jetgpu_split_fp16(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
+                      uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                      const int *e_max_dev, uint16_t *planes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(pitch >= cols && pitch % 8 == 0, "pitch must be >= cols and a multiple of 8");
+    JETGPU_REQUIRE(plane_stride >= rows * pitch, "plane stride too small");
+    JETGPU_REQUIRE(e_max_dev != nullptr, "null exponent pointer");
+    if (rows * cols == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
+    return PermuteSplitPlanes(in, planes, 1, rank, shape, perm, rows, cols, pitch, plane_stride,
+                              0, SplitFormat::kFp16, 0, AsStream(stream), e_max_dev);
+}
+
+int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C, uint64_t m,
+                       uint64_t n, uint64_t k, uint64_t kpitch, const int *e_max_dev,
+                       float out_scale, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr &&
+                       e_max_dev != nullptr,
+                   "null pointer");
+    return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
+                                  SplitFormat::kFp16, AsStream(stream), -1, e_max_dev);
 }
 
 int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C, uint64_t m,
@@ -315,9 +393,10 @@ size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const 
                                               b_perm, batch * m, n, k, dtype, precision);
     }
     if (p.tc) {
-        const SplitLayout l = LayoutFor(precision, k);
+        const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k);
         return l.a_bytes(p.ba * m) +
-               AlignUp((l.fmt == SplitFormat::kBf16 ? 4 : 6) * p.bb * n * l.kp * l.word);
+               AlignUp((l.fmt == SplitFormat::kTf32 ? 6 : 4) * p.bb * n * l.kp * l.word) +
+               l.exp_bytes();
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -372,23 +451,36 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
     cudaStream_t st = AsStream(stream);
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc) {
-        const SplitLayout l = LayoutFor(precision, k);
+        const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k);
         uint8_t *pa = ws;
         uint8_t *pb = ws + l.a_bytes(p.ba * m);
+        int *e_dev = nullptr;
+        float out_scale = 1.0f;
+        if (l.fmt == SplitFormat::kFp16) {
+            JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
+                           "scale_a + scale_b out of range for FP16x3");
+            e_dev = reinterpret_cast<int *>(
+                pb + AlignUp((size_t)l.b_planes * p.bb * n * l.kp * l.word));
+            if ((rc = MaxExponent2(A, p.ba * m * k, B, p.bb * k * n, dtype, e_dev, st)))
+                return rc;
+            out_scale = Pow2f(scale_a + scale_b);
+            scale_a = scale_b = 0;
+        }
         const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
         std::vector<int32_t> bt(b_rank);
         for (int j = 0; j < b_rank; ++j)
             bt[j] = b_perm[(j + nc) % b_rank];
         rc = PermuteSplitPlanes(A, pa, p.ba, a_rank, a_shape, a_perm, m, k, l.kp,
-                                p.ba * m * l.kp, scale_a, l.fmt, 0, st);
+                                p.ba * m * l.kp, scale_a, l.fmt, 0, st, e_dev);
         if (rc)
             return rc;
         rc = PermuteSplitPlanes(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, l.kp,
-                                p.bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st);
+                                p.bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
+                                e_dev ? e_dev + 1 : nullptr);
         if (rc)
             return rc;
-        return GemmSplitPlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, l.kp, 1.0f,
-                                      l.fmt, st, l.variant);
+        return GemmSplitPlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, l.kp,
+                                      out_scale, l.fmt, st, l.variant, e_dev);
     }
     const size_t eb = ElemBytes(dtype);
     const void *at = A;

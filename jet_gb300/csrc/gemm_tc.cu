@@ -53,30 +53,37 @@ constexpr int kGroupM = 8;                    // tile rows per group of the tile
 //                 Ar [Br; Bi] -> [ArBr | ArBi] and Ai [-Bi; Br] ->
 //                 [-AiBi | AiBr] land on (Cr | Ci) in one instruction each.
 //  2 BF16 narrow: variant 0 on BF16 planes (kind::f16, 32 k per stage).
+//  4 FP16 narrow: variant 2 on FP16 planes of power-of-two scaled operands.
 //  3 BF16 deep:   32-byte rows (16 k, 32-byte swizzle), 6 stages of 32 KB:
 //                 the same shared memory as variant 2 in twice as many,
 //                 half-size stages.
 // A chunk is the K extent accumulated in TMEM before the FP32 fold, in
 // stages (a kernel argument; see the kernel comment).
 template <int V> struct TcCfg;
+// Operand formats: 0 TF32 (kind::tf32), 1 BF16, 2 FP16 (both kind::f16).
+constexpr int kFmtTf32 = 0, kFmtBf16 = 1, kFmtFp16 = 2;
 template <> struct TcCfg<0> {
-    static constexpr bool Wide = false, Bf16 = false;
-    static constexpr int Stages = 3, Tiles = 8, RowBytes = 64;
+    static constexpr bool Wide = false;
+    static constexpr int Fmt = kFmtTf32, Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <> struct TcCfg<1> {
-    static constexpr bool Wide = true, Bf16 = false;
-    static constexpr int Stages = 2, Tiles = 10, RowBytes = 64;
+    static constexpr bool Wide = true;
+    static constexpr int Fmt = kFmtTf32, Stages = 2, Tiles = 10, RowBytes = 64;
 };
 template <> struct TcCfg<2> {
-    static constexpr bool Wide = false, Bf16 = true;
-    static constexpr int Stages = 3, Tiles = 8, RowBytes = 64;
+    static constexpr bool Wide = false;
+    static constexpr int Fmt = kFmtBf16, Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <> struct TcCfg<3> {
-    static constexpr bool Wide = false, Bf16 = true;
-    static constexpr int Stages = 6, Tiles = 8, RowBytes = 32;
+    static constexpr bool Wide = false;
+    static constexpr int Fmt = kFmtBf16, Stages = 6, Tiles = 8, RowBytes = 32;
+};
+template <> struct TcCfg<4> {
+    static constexpr bool Wide = false;
+    static constexpr int Fmt = kFmtFp16, Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <int V> constexpr int TileBytes() { return kBM * TcCfg<V>::RowBytes; }
-template <int V> constexpr int ElemBytes() { return TcCfg<V>::Bf16 ? 2 : 4; }
+template <int V> constexpr int ElemBytes() { return TcCfg<V>::Fmt == kFmtTf32 ? 4 : 2; }
 template <int V> constexpr int BlockK() { return TcCfg<V>::RowBytes / ElemBytes<V>(); }
 template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * TileBytes<V>(); }
 
@@ -87,16 +94,22 @@ template <int V> constexpr int StageBytes() { return TcCfg<V>::Tiles * TileBytes
 // errors 7.0e-6 / 1.0e-5 / 1.2e-5 / 1.9e-5 against FP64, at 1.10 / 1.04 /
 // 1.01 / 1.00 times the depth-128 product time. BF16: 128, since its split
 // truncation (about 4.5e-6 per product) dominates any accumulation error.
+// FP16: 32, one stage (the same number of accumulations per chunk as TF32 at
+// 16: two MMA k steps).
 constexpr int kDefaultChunkKTf32 = 16;
 constexpr int kDefaultChunkKBf16 = 128;
+constexpr int kDefaultChunkKFp16 = 32;
 // K depth per TMEM chunk (jetgpu_set_tc_chunk_depth; 0 = default). Process-wide,
 // read at every launch: atomic so a setter on one thread never tears a read.
 std::atomic<int> g_tc_chunk_k{0};
 
-inline int ChunkStages(bool bf16, int stage_k)
+inline int ChunkStages(int fmt, int stage_k)
 {
     const int set = g_tc_chunk_k.load(std::memory_order_relaxed);
-    int depth = set > 0 ? set : (bf16 ? kDefaultChunkKBf16 : kDefaultChunkKTf32);
+    int depth = set > 0 ? set
+                        : fmt == kFmtBf16 ? kDefaultChunkKBf16
+                                          : fmt == kFmtFp16 ? kDefaultChunkKFp16
+                                                            : kDefaultChunkKTf32;
     int stages = depth / stage_k;
     return stages < 1 ? 1 : stages;
 }
@@ -191,19 +204,20 @@ template <int kRow> __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr)
 }
 
 // Instruction descriptor: D = F32, both operands K-major, M x N; operand
-// format 2 = TF32 (kind::tf32), 1 = BF16 (kind::f16). A and B share it.
-__host__ __device__ constexpr uint32_t InstrDesc(int m, int n, bool neg_a, bool bf16)
+// format code 2 = TF32 (kind::tf32), 1 = BF16, 0 = FP16 (kind::f16). A and B
+// share it.
+__host__ __device__ constexpr uint32_t InstrDesc(int m, int n, bool neg_a, int fmt)
 {
-    return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) |
-           ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(m >> 4) << 24);
+    const uint32_t code = fmt == kFmtTf32 ? 2u : fmt == kFmtBf16 ? 1u : 0u;
+    return (1u << 4) | (code << 7) | (code << 10) | ((neg_a ? 1u : 0u) << 13) |
+           ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-template <bool kBf16>
+template <bool kHalf>
 __device__ __forceinline__ void Mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
                                     uint32_t accumulate)
 {
-    if constexpr (kBf16)
+    if constexpr (kHalf)
         asm volatile("{\n\t.reg .pred p;\n\t"
                      "setp.ne.b32 p, %4, 0;\n\t"
                      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
@@ -287,7 +301,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_split_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles,
-                          float scale, int a_batched, int b_batched, int chunk_stages)
+                          float scale, int a_batched, int b_batched, int chunk_stages,
+                          const int *__restrict__ scale_exps)
 {
     // Batch b = blockIdx.z: a batched operand is read through a 4-D map
     // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
@@ -295,7 +310,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     C += (size_t)bz * M * N;
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
-    constexpr bool kBf16 = Cfg::Bf16;
+    constexpr int kFmt = Cfg::Fmt;
+    constexpr bool kHalf = kFmt != kFmtTf32;
     constexpr int kBK = BlockK<V>();
     constexpr int kStages = Cfg::Stages;
     constexpr int kStageBytes = StageBytes<V>();
@@ -391,8 +407,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer.
-            constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false, kBf16);
-            constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kBf16);
+            constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false, kFmt);
+            constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kFmt);
             bool ok = true;
             for (int kt = 0; kt < ktiles && ok; ++kt) {
                 const int chunk = kt / chunk_stages;
@@ -416,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t d_im = d_re + kBN;
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
                 if constexpr (kWide) {
-                    constexpr uint32_t kIdescW = InstrDesc(kBM, 2 * kBN, false, kBf16);
+                    constexpr uint32_t kIdescW = InstrDesc(kBM, 2 * kBN, false, kFmt);
 #pragma unroll
                     for (int kk = 0; kk < kRowBytes / 32; ++kk) {
                         const uint32_t koff = kk * 32; // 32 bytes of K per MMA
@@ -431,13 +447,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                         const uint64_t b_rc_lo = SmemDesc<kRowBytes>(base + 8 * kTileBytes + koff);
                         const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                         // (Cr | Ci) += Ar [Br; Bi]
-                        Mma<kBf16>(d_re, arh, b_rc_hi, kIdescW, acc);
-                        Mma<kBf16>(d_re, arh, b_rc_lo, kIdescW, 1u);
-                        Mma<kBf16>(d_re, arl, b_rc_hi, kIdescW, 1u);
+                        Mma<kHalf>(d_re, arh, b_rc_hi, kIdescW, acc);
+                        Mma<kHalf>(d_re, arh, b_rc_lo, kIdescW, 1u);
+                        Mma<kHalf>(d_re, arl, b_rc_hi, kIdescW, 1u);
                         // (Cr | Ci) += Ai [-Bi; Br]
-                        Mma<kBf16>(d_re, aih, b_nr_hi, kIdescW, 1u);
-                        Mma<kBf16>(d_re, aih, b_nr_lo, kIdescW, 1u);
-                        Mma<kBf16>(d_re, ail, b_nr_hi, kIdescW, 1u);
+                        Mma<kHalf>(d_re, aih, b_nr_hi, kIdescW, 1u);
+                        Mma<kHalf>(d_re, aih, b_nr_lo, kIdescW, 1u);
+                        Mma<kHalf>(d_re, ail, b_nr_hi, kIdescW, 1u);
                     }
                 }
                 else
@@ -454,21 +470,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint64_t bil = SmemDesc<kRowBytes>(base + 7 * kTileBytes + koff);
                     const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
                     // Cr += Ar Br
-                    Mma<kBf16>(d_re, arh, brh, kIdesc, acc);
-                    Mma<kBf16>(d_re, arh, brl, kIdesc, 1u);
-                    Mma<kBf16>(d_re, arl, brh, kIdesc, 1u);
+                    Mma<kHalf>(d_re, arh, brh, kIdesc, acc);
+                    Mma<kHalf>(d_re, arh, brl, kIdesc, 1u);
+                    Mma<kHalf>(d_re, arl, brh, kIdesc, 1u);
                     // Cr -= Ai Bi
-                    Mma<kBf16>(d_re, aih, bih, kIdescNeg, 1u);
-                    Mma<kBf16>(d_re, aih, bil, kIdescNeg, 1u);
-                    Mma<kBf16>(d_re, ail, bih, kIdescNeg, 1u);
+                    Mma<kHalf>(d_re, aih, bih, kIdescNeg, 1u);
+                    Mma<kHalf>(d_re, aih, bil, kIdescNeg, 1u);
+                    Mma<kHalf>(d_re, ail, bih, kIdescNeg, 1u);
                     // Ci += Ar Bi
-                    Mma<kBf16>(d_im, arh, bih, kIdesc, acc);
-                    Mma<kBf16>(d_im, arh, bil, kIdesc, 1u);
-                    Mma<kBf16>(d_im, arl, bih, kIdesc, 1u);
+                    Mma<kHalf>(d_im, arh, bih, kIdesc, acc);
+                    Mma<kHalf>(d_im, arh, bil, kIdesc, 1u);
+                    Mma<kHalf>(d_im, arl, bih, kIdesc, 1u);
                     // Ci += Ai Br
-                    Mma<kBf16>(d_im, aih, brh, kIdesc, 1u);
-                    Mma<kBf16>(d_im, aih, brl, kIdesc, 1u);
-                    Mma<kBf16>(d_im, ail, brh, kIdesc, 1u);
+                    Mma<kHalf>(d_im, aih, brh, kIdesc, 1u);
+                    Mma<kHalf>(d_im, aih, brl, kIdesc, 1u);
+                    Mma<kHalf>(d_im, ail, brh, kIdesc, 1u);
                 }
                 MmaCommit(SmemAddr(&empty_bar[s]));
                 if (chunk_end)
@@ -515,6 +531,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
                                  SmemAddr(&acc_empty[buf]))
                              : "memory");
+        }
+        if (scale_exps != nullptr) {
+            // Undo the operands' power-of-two FP16 scales: two exact
+            // multiplies keep each factor inside the float range.
+            const int e = -(Fp16ScaleExp(scale_exps[0]) + Fp16ScaleExp(scale_exps[1]));
+            const float f1 = Pow2f(e / 2), f2 = Pow2f(e - e / 2);
+#pragma unroll
+            for (int j = 0; j < 64; ++j) {
+                acc_re[j] = acc_re[j] * f1 * f2;
+                acc_im[j] = acc_im[j] * f1 * f2;
+            }
         }
         const int row = m0 + quad * 32 + lane;
         if (ok && row < M) {
@@ -567,15 +594,15 @@ int GetEncoder()
 // 3-D map over planes: (k, row, plane), box (row_bytes of k) x 128 x 1,
 // swizzled over row_bytes (64 or 32).
 int EncodePlanes(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
-                 uint64_t kpitch, bool bf16, int planes, int row_bytes)
+                 uint64_t kpitch, bool half, int planes, int row_bytes)
 {
-    const uint64_t eb = bf16 ? 2 : 4;
+    const uint64_t eb = half ? 2 : 4;
     cuuint64_t dims[3] = {k, rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {kpitch * eb, rows * kpitch * eb};
     cuuint32_t box[3] = {(cuuint32_t)(row_bytes / eb), kBM, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = g_encode(map,
-                          bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          half ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                           3, const_cast<void *>(base), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE,
                           row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
@@ -589,15 +616,15 @@ int EncodePlanes(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
 // 4-D map over batched planes laid out [plane][batch][rows][kpitch]:
 // (k, row, batch, plane), box (row_bytes of k) x 128 x 1 x 1.
 int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint64_t k,
-                        uint64_t kpitch, uint64_t batch, bool bf16, int planes, int row_bytes)
+                        uint64_t kpitch, uint64_t batch, bool half, int planes, int row_bytes)
 {
-    const uint64_t eb = bf16 ? 2 : 4;
+    const uint64_t eb = half ? 2 : 4;
     cuuint64_t dims[4] = {k, rows, batch, (cuuint64_t)planes};
     cuuint64_t strides[3] = {kpitch * eb, rows * kpitch * eb, batch * rows * kpitch * eb};
     cuuint32_t box[4] = {(cuuint32_t)(row_bytes / eb), kBM, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = g_encode(map,
-                          bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          half ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                           4, const_cast<void *>(base), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE,
                           row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
@@ -611,7 +638,7 @@ int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint6
 template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
-             cudaStream_t stream)
+             cudaStream_t stream, const int *e_max_dev = nullptr)
 {
     const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + 1024;
     static thread_local int configured_dev = -1;
@@ -628,7 +655,7 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
-        b_batched, ChunkStages(TcCfg<V>::Bf16, BlockK<V>()));
+        b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev);
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
@@ -657,7 +684,7 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream, int variant)
+                           cudaStream_t stream, int variant, const int *e_max_dev)
 {
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
@@ -665,6 +692,9 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         b_batched = 0;
     }
     const bool bf16 = fmt == SplitFormat::kBf16;
+    const bool fp16 = fmt == SplitFormat::kFp16;
+    const bool half = bf16 || fp16;
+    JETGPU_REQUIRE(!fp16 || e_max_dev != nullptr, "FP16 planes need their max exponents");
     JETGPU_REQUIRE(m > 0 && n > 0 && k > 0, "empty product");
     JETGPU_REQUIRE(m < (1ull << 31) && n < (1ull << 31) && k < (1ull << 31),
                    "dimension too large");
@@ -680,19 +710,22 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (variant < 0)
         variant = TcVariant();
-    const bool wide = !bf16 && variant == 1;
+    const bool wide = !half && variant == 1;
     const bool deep = bf16 && variant == 2;
     const int row_bytes = deep ? TcCfg<3>::RowBytes : TcCfg<0>::RowBytes;
     CUtensorMap ta, tb;
     if ((rc = a_batched
-                  ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, bf16, 4, row_bytes)
-                  : EncodePlanes(&ta, a_planes, m, k, kpitch, bf16, 4, row_bytes)))
+                  ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, half, 4, row_bytes)
+                  : EncodePlanes(&ta, a_planes, m, k, kpitch, half, 4, row_bytes)))
         return rc;
     const int bplanes = wide ? 6 : 4;
     if ((rc = b_batched
-                  ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, bf16, bplanes, row_bytes)
-                  : EncodePlanes(&tb, b_planes, n, k, kpitch, bf16, bplanes, row_bytes)))
+                  ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, half, bplanes, row_bytes)
+                  : EncodePlanes(&tb, b_planes, n, k, kpitch, half, bplanes, row_bytes)))
         return rc;
+    if (fp16)
+        return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           e_max_dev);
     if (deep)
         return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
     if (bf16)

@@ -157,6 +157,33 @@ __device__ __forceinline__ void SplitBf16x2(float x0, float x1, uint32_t &hi, ui
     lo = PackBf16x2(x0 - __uint_as_float(hi << 16), x1 - __uint_as_float(hi & 0xffff0000u));
 }
 
+// Two floats to packed FP16 words, round to nearest even, and back.
+__device__ __forceinline__ uint32_t PackF16x2(float lower, float upper)
+{
+    uint32_t r;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(upper), "f"(lower));
+    return r;
+}
+
+__device__ __forceinline__ void UnpackF16x2(uint32_t r, float &lower, float &upper)
+{
+    asm("{\n\t.reg .b16 l, h;\n\t"
+        "mov.b32 {l, h}, %2;\n\t"
+        "cvt.f32.f16 %0, l;\n\t"
+        "cvt.f32.f16 %1, h;\n\t}"
+        : "=f"(lower), "=f"(upper)
+        : "r"(r));
+}
+
+// FP16 hi/lo splits of two (already scaled) values, packed like SplitBf16x2.
+__device__ __forceinline__ void SplitF16x2(float x0, float x1, uint32_t &hi, uint32_t &lo)
+{
+    hi = PackF16x2(x0, x1);
+    float h0, h1;
+    UnpackF16x2(hi, h0, h1);
+    lo = PackF16x2(x0 - h0, x1 - h1);
+}
+
 struct SplitOut {
     void *planes;          // 4 planes, or 6 with the negated imaginary pair
     uint64_t plane_stride; // words between planes
@@ -165,8 +192,24 @@ struct SplitOut {
     float scale;           // exact power of two
     int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo (TF32)
     int bf16;              // 16-bit BF16 words instead of TF32-in-FP32 words
+    int fp16;              // 16-bit FP16 words of the operand scaled by its FP16 scale
+    const int *e_max_dev;  // FP16: the operand's max exponent (sets the scale)
     int cols_log2;         // log2(cols) when cols is a power of 2 (bit-permutation path)
 };
+
+__device__ __forceinline__ float SplitScale(const SplitOut &so)
+{
+    return so.fp16 ? Pow2f(Fp16ScaleExp(*so.e_max_dev)) : so.scale;
+}
+
+__device__ __forceinline__ void Split16x2(const SplitOut &so, float x0, float x1, uint32_t &hi,
+                                          uint32_t &lo)
+{
+    if (so.fp16)
+        SplitF16x2(x0, x1, hi, lo);
+    else
+        SplitBf16x2(x0, x1, hi, lo);
+}
 
 __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
                                            float2 v)
@@ -174,11 +217,12 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
     uint64_t row = o / so.cols;
     uint64_t col = o - row * so.cols;
     uint64_t off = row * so.pitch + col;
-    float re = v.x * so.scale, im = v.y * so.scale;
-    if (so.bf16) {
+    const float sc = SplitScale(so);
+    float re = v.x * sc, im = v.y * sc;
+    if (so.bf16 || so.fp16) {
         uint16_t *pl = static_cast<uint16_t *>(so.planes);
         uint32_t h, l; // (re, im) packed
-        SplitBf16x2(re, im, h, l);
+        Split16x2(so, re, im, h, l);
         pl[off] = (uint16_t)(h & 0xffffu);
         pl[off + so.plane_stride] = (uint16_t)(l & 0xffffu);
         pl[off + 2 * so.plane_stride] = (uint16_t)(h >> 16);
@@ -300,14 +344,15 @@ struct SplitStore {
         uint64_t base = row * so.pitch + col;
         float2 a = make_float2(__uint_as_float(v[0].x), __uint_as_float(v[0].y));
         float2 b = make_float2(__uint_as_float(v[1].x), __uint_as_float(v[1].y));
-        float ar = a.x * so.scale, ai = a.y * so.scale;
-        float br = b.x * so.scale, bi = b.y * so.scale;
-        if (so.bf16) {
-            // Two BF16 words per plane: one 4-byte store (base is even).
+        const float sc = SplitScale(so);
+        float ar = a.x * sc, ai = a.y * sc;
+        float br = b.x * sc, bi = b.y * sc;
+        if (so.bf16 || so.fp16) {
+            // Two 16-bit words per plane: one 4-byte store (base is even).
             uint16_t *pl = static_cast<uint16_t *>(so.planes);
             uint32_t rh, rl, ih, il; // (element a, element b) packed per plane
-            SplitBf16x2(ar, br, rh, rl);
-            SplitBf16x2(ai, bi, ih, il);
+            Split16x2(so, ar, br, rh, rl);
+            Split16x2(so, ai, bi, ih, il);
             *reinterpret_cast<uint32_t *>(pl + base) = rh;
             *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = rl;
             *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = ih;
@@ -584,9 +629,11 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
 int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
                        const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
                        uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
-                       int neg_im, cudaStream_t stream)
+                       int neg_im, cudaStream_t stream, const int *e_max_dev)
 {
-    JETGPU_REQUIRE(!(neg_im && fmt == SplitFormat::kBf16), "negated planes are TF32 only");
+    JETGPU_REQUIRE(!(neg_im && fmt != SplitFormat::kTf32), "negated planes are TF32 only");
+    JETGPU_REQUIRE(fmt != SplitFormat::kFp16 || e_max_dev != nullptr,
+                   "FP16 planes need the operand's max exponent");
     Simplified s;
     int rc = Simplify(rank, shape, perm, s);
     if (rc)
@@ -605,6 +652,8 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
     so.scale = ldexpf(1.0f, scale_exp);
     so.neg_im = neg_im;
     so.bf16 = fmt == SplitFormat::kBf16 ? 1 : 0;
+    so.fp16 = fmt == SplitFormat::kFp16 ? 1 : 0;
+    so.e_max_dev = e_max_dev;
     so.cols_log2 = IsPow2(cols) ? Log2(cols) : -1;
     const bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)planes % 16 == 0) &&
                          (pitch % 2 == 0) && (plane_stride % 2 == 0);

@@ -128,9 +128,15 @@ __global__ void init_exp_kernel(int *e) { *e = -1000; }
 
 __global__ void counter_add_kernel(uint64_t *c, uint64_t delta) { *c += delta; }
 
+// Max exponent of operand blockIdx.y (x0 or x1) into e[blockIdx.y]; e must
+// start below -1000 (the 0x80 byte fill), so all-zero operands give -1000.
 template <typename V, typename U>
-__global__ void max_exp_kernel(const V *__restrict__ x, uint64_t n, int *e)
+__global__ void max_exp_kernel(const V *__restrict__ x0, uint64_t n0, const V *__restrict__ x1,
+                               uint64_t n1, int *e)
 {
+    const V *__restrict__ x = blockIdx.y ? x1 : x0;
+    const uint64_t n = blockIdx.y ? n1 : n0;
+    e += blockIdx.y;
     U best = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -328,21 +334,43 @@ int jetgpu_max_exponent(const void *x, uint64_t size, int dtype, int *exp_dev,
                         void *stream)
 {
     ClearError();
-    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
-    JETGPU_REQUIRE(exp_dev != nullptr, "null exponent pointer");
-    cudaStream_t st = AsStream(stream);
-    init_exp_kernel<<<1, 1, 0, st>>>(exp_dev);
-    if (size == 0)
-        return CheckLaunch("init_exp_kernel");
-    JETGPU_REQUIRE(x != nullptr, "null input");
-    unsigned grid = GridFor((size + kThreads - 1) / kThreads, 8);
-    if (dtype == JETGPU_C64)
-        max_exp_kernel<float2, uint32_t><<<grid, kThreads, 0, st>>>(
-            (const float2 *)x, size, exp_dev);
-    else
-        max_exp_kernel<double2, unsigned long long><<<grid, kThreads, 0, st>>>(
-            (const double2 *)x, size, exp_dev);
-    return CheckLaunch("max_exp_kernel");
+    return MaxExponent(x, size, dtype, exp_dev, AsStream(stream));
 }
 
 } // extern "C"
+
+namespace jetgpu {
+
+int MaxExponent(const void *x, uint64_t size, int dtype, int *exp_dev, cudaStream_t st)
+{
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(exp_dev != nullptr, "null exponent pointer");
+    if (size == 0) {
+        init_exp_kernel<<<1, 1, 0, st>>>(exp_dev);
+        return CheckLaunch("init_exp_kernel");
+    }
+    return MaxExponent2(x, size, x, 0, dtype, exp_dev, st, 1);
+}
+
+// Both operands' max exponents (e[0] of x0, e[1] of x1) with one fill and one
+// launch; `operands` = 1 computes e[0] only. Empty operands leave their word
+// at the fill value (below any exponent).
+int MaxExponent2(const void *x0, uint64_t n0, const void *x1, uint64_t n1, int dtype, int *e,
+                 cudaStream_t st, int operands)
+{
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(e != nullptr, "null exponent pointer");
+    JETGPU_REQUIRE((n0 == 0 || x0 != nullptr) && (n1 == 0 || x1 != nullptr), "null input");
+    JETGPU_CUDA_TRY(cudaMemsetAsync(e, 0x80, sizeof(int) * operands, st));
+    const uint64_t n = n0 > n1 ? n0 : n1;
+    const dim3 grid(GridFor((n + kThreads - 1) / kThreads, 8), (unsigned)operands);
+    if (dtype == JETGPU_C64)
+        max_exp_kernel<float2, uint32_t><<<grid, kThreads, 0, st>>>(
+            (const float2 *)x0, n0, (const float2 *)x1, n1, e);
+    else
+        max_exp_kernel<double2, unsigned long long><<<grid, kThreads, 0, st>>>(
+            (const double2 *)x0, n0, (const double2 *)x1, n1, e);
+    return CheckLaunch("max_exp_kernel");
+}
+
+} // namespace jetgpu

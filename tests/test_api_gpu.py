@@ -180,9 +180,9 @@ def test_sliced_networks_share_tasks_and_reduce(jet):
 def test_config0_amplitude(jet, precision):
     """4x4 grid, 8 cycles: TensorNetwork::Contract(path) on the GPU against the
     complex128 oracle and the reference's own CPU result (golden). Whole
-    networks use plain FP32 or AUTO (TF32x3 on the large steps only): forcing
-    TF32x3 onto ~200 steps of 2x2 gates compounds its ~2^-22 per-product
-    rounding past 1e-5."""
+    networks use plain FP32 or AUTO (a split form on the large steps only):
+    forcing a split form onto ~200 steps of 2x2 gates compounds the tensor
+    core's biased accumulation past 1e-5."""
     import json
     import os
 

@@ -32,7 +32,8 @@ def _case(seed, nl, nc, nr, dtype, batch, a_b, b_b, dev):
 
 @pytest.mark.parametrize("a_b,b_b", [(1, 0), (0, 1), (1, 1)])
 @pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 1),
-                                             ("complex64", 3), ("complex128", 0)])
+                                             ("complex64", 3), ("complex64", 4),
+                                             ("complex128", 0)])
 @pytest.mark.parametrize("shape", [(7, 6, 8), (1, 9, 3), (4, 10, 1), (0, 5, 0), (8, 8, 8),
                                    (6, 14, 0), (0, 16, 3), (0, 18, 0)])
 @pytest.mark.parametrize("variant", [0, 1, 2])
