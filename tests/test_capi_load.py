@@ -56,3 +56,47 @@ def test_chunk_depth_rejects_out_of_range(depth):
     assert capi.lib.jetgpu_set_tc_chunk_depth(depth) == capi.ERR_INVALID
     assert b"chunk depth" in capi.lib.jetgpu_last_error()
     assert capi.lib.jetgpu_set_tc_chunk_depth(0) == capi.OK
+
+
+@pytest.mark.parametrize("form,ok", [(1, True), (3, True), (4, True), (0, False), (2, False),
+                                     (5, False)])
+def test_auto_form_accepts_split_forms_only(form, ok):
+    from jet_gb300 import capi
+
+    rc = capi.lib.jetgpu_set_auto_form(form)
+    try:
+        if ok:
+            assert rc == capi.OK
+        else:
+            assert rc == capi.ERR_INVALID
+            assert b"AUTO form" in capi.lib.jetgpu_last_error()
+    finally:
+        capi.lib.jetgpu_set_auto_form(capi.PREC_FP16X3)
+
+
+def test_split_forms_need_complex64_and_fp16_scale_range():
+    """Host-side checks of jetgpu_contract before any device work: the split
+    forms reject complex128, FP16x3 rejects |scale_a + scale_b| > 126."""
+    from jet_gb300 import capi
+
+    sh = capi.u64([256, 256])
+    pm = capi.i32([0, 1])
+    for prec in (capi.PREC_TF32X3, capi.PREC_BF16X3, capi.PREC_FP16X3):
+        rc = capi.lib.jetgpu_contract(None, 2, sh, pm, None, 2, sh, pm, None, 256, 256, 256,
+                                      capi.C128, prec, capi.ALGO_4M, 0, 0, None, 0, None)
+        assert rc == capi.ERR_UNSUPPORTED
+        assert b"complex64" in capi.lib.jetgpu_last_error()
+    rc = capi.lib.jetgpu_contract(None, 2, sh, pm, None, 2, sh, pm, None, 256, 256, 256,
+                                  capi.C64, 9, capi.ALGO_4M, 0, 0, None, 0, None)
+    assert rc == capi.ERR_INVALID and b"precision" in capi.lib.jetgpu_last_error()
+
+
+def test_fp16_stage_entry_points_need_exponents():
+    from jet_gb300 import capi
+
+    sh = capi.u64([16, 8])
+    pm = capi.i32([0, 1])
+    rc = capi.lib.jetgpu_split_fp16(None, 2, sh, pm, 16, 8, 8, 128, None, None, None)
+    assert rc == capi.ERR_INVALID and b"exponent" in capi.lib.jetgpu_last_error()
+    rc = capi.lib.jetgpu_gemm_fp16x3(None, None, None, 128, 128, 64, 64, None, 1.0, None)
+    assert rc == capi.ERR_INVALID and b"null" in capi.lib.jetgpu_last_error()
