@@ -119,6 +119,47 @@ int Validate(int rank, const uint64_t *shape, const int32_t *perm, uint64_t lead
     return JETGPU_OK;
 }
 
+// The split form of one contraction or of a batch of them: operand planes
+// (and, for FP16, the operands' max exponents) in `ws`, then the tcgen05
+// product. ba / bb: tensors of A / B (batch or 1, shared operands are 1).
+int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank,
+                 const uint64_t *a_shape, const int32_t *a_perm, uint64_t ba, const void *B,
+                 int b_rank, const uint64_t *b_shape, const int32_t *b_perm, uint64_t bb,
+                 void *C, uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a,
+                 int scale_b, uint8_t *ws, cudaStream_t st)
+{
+    int rc;
+    uint8_t *pa = ws;
+    uint8_t *pb = ws + l.a_bytes(ba * m);
+    int *e_dev = nullptr;
+    float out_scale = 1.0f;
+    if (l.fmt == SplitFormat::kFp16) {
+        // Each operand's max exponent sets its FP16 scale; the user's exact
+        // scales move to the epilogue.
+        JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
+                       "scale_a + scale_b out of range for FP16x3");
+        e_dev = reinterpret_cast<int *>(pb + AlignUp((size_t)l.b_planes * bb * n * l.kp * l.word));
+        if ((rc = MaxExponent2(A, ba * m * k, B, bb * k * n, dtype, e_dev, st)))
+            return rc;
+        out_scale = Pow2f(scale_a + scale_b);
+        scale_a = scale_b = 0;
+    }
+    // B is wanted as (right ++ common): rotate its (common ++ right) order.
+    const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
+    std::vector<int32_t> bt(b_rank);
+    for (int j = 0; j < b_rank; ++j)
+        bt[j] = b_perm[(j + nc) % b_rank];
+    if ((rc = PermuteSplitPlanes(A, pa, ba, a_rank, a_shape, a_perm, m, k, l.kp, ba * m * l.kp,
+                                 scale_a, l.fmt, 0, st, e_dev)))
+        return rc;
+    if ((rc = PermuteSplitPlanes(B, pb, bb, b_rank, b_shape, bt.data(), n, k, l.kp,
+                                 bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
+                                 e_dev ? e_dev + 1 : nullptr)))
+        return rc;
+    return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
+                                  l.fmt, st, l.variant, e_dev);
+}
+
 } // namespace
 } // namespace jetgpu
 
@@ -189,41 +230,10 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
     cudaStream_t st = AsStream(stream);
     uint8_t *ws = static_cast<uint8_t *>(workspace);
 
-    if (k > 0 && UseTensorCores(m, n, k, dtype, precision)) {
-        const SplitLayout l = LayoutFor(precision, k, (double)m * n * k);
-        uint8_t *pa = ws;
-        uint8_t *pb = ws + l.a_bytes(m);
-        int *e_dev = nullptr;
-        float out_scale = 1.0f;
-        if (l.fmt == SplitFormat::kFp16) {
-            // Each operand's max exponent sets its FP16 scale; the user's
-            // exact scales move to the epilogue.
-            JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
-                           "scale_a + scale_b out of range for FP16x3");
-            e_dev = reinterpret_cast<int *>(
-                pb + AlignUp((size_t)l.b_planes * n * l.kp * l.word));
-            if ((rc = MaxExponent2(A, m * k, B, k * n, dtype, e_dev, st)))
-                return rc;
-            out_scale = Pow2f(scale_a + scale_b);
-            scale_a = scale_b = 0;
-        }
-        // B is wanted as (right ++ common): rotate its (common ++ right) order.
-        const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
-        std::vector<int32_t> bt(b_rank);
-        for (int j = 0; j < b_rank; ++j)
-            bt[j] = b_perm[(j + nc) % b_rank];
-        rc = PermuteSplitPlanes(A, pa, 1, a_rank, a_shape, a_perm, m, k, l.kp, m * l.kp, scale_a,
-                                l.fmt, 0, st, e_dev);
-        if (rc)
-            return rc;
-        rc = PermuteSplitPlanes(B, pb, 1, b_rank, b_shape, bt.data(), n, k, l.kp, n * l.kp,
-                                scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
-                                e_dev ? e_dev + 1 : nullptr);
-        if (rc)
-            return rc;
-        return GemmSplitPlanarBatched(pa, 0, pb, 0, C, 1, m, n, k, l.kp, out_scale, l.fmt, st,
-                                      l.variant, e_dev);
-    }
+    if (k > 0 && UseTensorCores(m, n, k, dtype, precision))
+        return SplitProduct(LayoutFor(precision, k, (double)m * n * k), 1, A, a_rank, a_shape,
+                            a_perm, 1, B, b_rank, b_shape, b_perm, 1, C, m, n, k, dtype, scale_a,
+                            scale_b, ws, st);
 
     const size_t eb = ElemBytes(dtype);
     const void *at = A;
@@ -450,38 +460,10 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
                         "workspace too small: need " + std::to_string(need) + " bytes");
     cudaStream_t st = AsStream(stream);
     uint8_t *ws = static_cast<uint8_t *>(workspace);
-    if (k > 0 && p.tc) {
-        const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k);
-        uint8_t *pa = ws;
-        uint8_t *pb = ws + l.a_bytes(p.ba * m);
-        int *e_dev = nullptr;
-        float out_scale = 1.0f;
-        if (l.fmt == SplitFormat::kFp16) {
-            JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
-                           "scale_a + scale_b out of range for FP16x3");
-            e_dev = reinterpret_cast<int *>(
-                pb + AlignUp((size_t)l.b_planes * p.bb * n * l.kp * l.word));
-            if ((rc = MaxExponent2(A, p.ba * m * k, B, p.bb * k * n, dtype, e_dev, st)))
-                return rc;
-            out_scale = Pow2f(scale_a + scale_b);
-            scale_a = scale_b = 0;
-        }
-        const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
-        std::vector<int32_t> bt(b_rank);
-        for (int j = 0; j < b_rank; ++j)
-            bt[j] = b_perm[(j + nc) % b_rank];
-        rc = PermuteSplitPlanes(A, pa, p.ba, a_rank, a_shape, a_perm, m, k, l.kp,
-                                p.ba * m * l.kp, scale_a, l.fmt, 0, st, e_dev);
-        if (rc)
-            return rc;
-        rc = PermuteSplitPlanes(B, pb, p.bb, b_rank, b_shape, bt.data(), n, k, l.kp,
-                                p.bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
-                                e_dev ? e_dev + 1 : nullptr);
-        if (rc)
-            return rc;
-        return GemmSplitPlanarBatched(pa, p.ba > 1, pb, p.bb > 1, C, batch, m, n, k, l.kp,
-                                      out_scale, l.fmt, st, l.variant, e_dev);
-    }
+    if (k > 0 && p.tc)
+        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k), batch, A, a_rank,
+                            a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm, p.bb, C, m, n, k,
+                            dtype, scale_a, scale_b, ws, st);
     const size_t eb = ElemBytes(dtype);
     const void *at = A;
     const void *btp = B;
