@@ -394,6 +394,16 @@ int jetgpu_counter_add(uint64_t *counter_dev, uint64_t delta, void *stream);
 int jetgpu_take_device_status(int *status);
 
 /*
+ * Exercises the failure path of the bounded device waits without faulting:
+ * launches one kernel whose thread waits on an mbarrier that nothing
+ * completes; the wait gives up after limit_us microseconds (1 us .. 1 s; or
+ * 2^24 polls), records JETGPU_ERR_TIMEOUT in the status word that
+ * jetgpu_take_device_status reads, and the kernel exits normally, so the
+ * context stays usable. No reference counterpart (failure detection test).
+ */
+int jetgpu_probe_bounded_wait(unsigned int limit_us, void *stream);
+
+/*
  * Largest binary exponent e with 2^e <= max |x_i| over the real and imaginary
  * parts of `size` complex elements, written to the device int *exp_dev
  * (stream-ordered, no host synchronisation). -1000 when every element is

@@ -97,6 +97,7 @@ lib.jetgpu_slice_gather.argtypes = [_vp, ctypes.c_int, _u64p, ctypes.c_int, _i32
                                     ctypes.c_uint64, ctypes.c_uint64, _vp, ctypes.c_int, _vp]
 lib.jetgpu_max_exponent.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, _vp]
 lib.jetgpu_take_device_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
+lib.jetgpu_probe_bounded_wait.argtypes = [ctypes.c_uint, _vp]
 lib.jetgpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
 
 

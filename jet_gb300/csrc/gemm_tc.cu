@@ -152,8 +152,11 @@ __device__ __forceinline__ bool MbarTryWait(uint32_t bar, uint32_t parity)
     return done != 0;
 }
 
-// Bounded wait for the phase of parity `parity`; false on timeout.
-__device__ __forceinline__ bool MbarWait(uint32_t bar, uint32_t parity)
+// Bounded wait for the phase of parity `parity`: gives up after limit_ns of
+// %globaltimer or max_iters polls, whichever comes first, records
+// JETGPU_ERR_TIMEOUT in the device status word and returns false.
+__device__ __forceinline__ bool MbarWaitFor(uint32_t bar, uint32_t parity,
+                                            unsigned long long limit_ns, uint32_t max_iters)
 {
     if (MbarTryWait(bar, parity))
         return true;
@@ -161,11 +164,16 @@ __device__ __forceinline__ bool MbarWait(uint32_t bar, uint32_t parity)
     for (uint32_t i = 1;; ++i) {
         if (MbarTryWait(bar, parity))
             return true;
-        if ((i & 255u) == 0 && GlobalTimer() - t0 > kWaitNs) {
+        if (i >= max_iters || ((i & 255u) == 0 && GlobalTimer() - t0 > limit_ns)) {
             atomicExch(&g_tc_status, JETGPU_ERR_TIMEOUT);
             return false;
         }
     }
+}
+
+__device__ __forceinline__ bool MbarWait(uint32_t bar, uint32_t parity)
+{
+    return MbarWaitFor(bar, parity, kWaitNs, 0xffffffffu);
 }
 
 __device__ __forceinline__ void TmaLoad3d(uint32_t dst, const CUtensorMap *map,
@@ -573,6 +581,22 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// The failure path of the bounded waits, exercised without a fault: one
+// thread waits on an mbarrier that nothing arrives on (phase 0 never
+// completes), gives up after limit_ns (or 2^24 polls) and records the timeout.
+__global__ void bounded_wait_probe_kernel(unsigned long long limit_ns)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        MbarInit(SmemAddr(&bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        MbarWaitFor(SmemAddr(&bar), 0, limit_ns, 1u << 24);
+    __syncthreads();
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
 
@@ -757,6 +781,15 @@ extern "C" int jetgpu_set_tc_chunk_depth(int k_depth)
     JETGPU_REQUIRE(k_depth >= 0 && k_depth <= 4096, "chunk depth out of range");
     jetgpu::g_tc_chunk_k.store(k_depth, std::memory_order_relaxed);
     return JETGPU_OK;
+}
+
+extern "C" int jetgpu_probe_bounded_wait(unsigned int limit_us, void *stream)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(limit_us >= 1 && limit_us <= 1000000, "limit must be 1 us .. 1 s");
+    jetgpu::bounded_wait_probe_kernel<<<1, 32, 0, jetgpu::AsStream(stream)>>>(
+        (unsigned long long)limit_us * 1000ull);
+    return jetgpu::CheckLaunch("bounded_wait_probe_kernel");
 }
 
 extern "C" int jetgpu_take_device_status(int *status)
