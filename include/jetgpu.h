@@ -32,6 +32,7 @@ extern "C" {
 #define JETGPU_ERR_UNSUPPORTED 3 /* valid request this build cannot serve */
 #define JETGPU_ERR_WORKSPACE 4   /* workspace missing or too small */
 #define JETGPU_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define JETGPU_ERR_MEMORY 6      /* the device memory pool limit (jetgpu_set_pool_limit) */
 
 /* Element types. */
 #define JETGPU_C64 0  /* std::complex<float>  */
@@ -69,6 +70,21 @@ int jetgpu_free(void *ptr);
 
 /* Releases every cached (free) block to the device. */
 int jetgpu_release_cached(void);
+
+/*
+ * Caps the bytes jetgpu_malloc may hold at once (0: no cap, the default).
+ * An allocation that would pass the cap fails with JETGPU_ERR_MEMORY before
+ * any CUDA call, so running out of device memory can be injected on the host
+ * (the C++ API turns it into a Jet::Exception). jetgpu_pool_bytes_in_use
+ * reports the bytes jetgpu_malloc currently holds.
+ */
+int jetgpu_set_pool_limit(size_t bytes);
+size_t jetgpu_pool_bytes_in_use(void);
+
+/* NVTX ranges (nsys / ncu timelines) for host code above the C-ABI; the
+ * library's own entry points mark themselves. No cost without a tool. */
+void jetgpu_range_push(const char *name);
+void jetgpu_range_pop(void);
 
 /* Bytes currently handed out by / held in the caching allocator. */
 int jetgpu_memory_stats(size_t *in_use, size_t *cached, size_t *peak_in_use);

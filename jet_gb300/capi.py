@@ -34,6 +34,7 @@ ERR_CUDA = 2
 ERR_UNSUPPORTED = 3
 ERR_WORKSPACE = 4
 ERR_TIMEOUT = 5
+ERR_MEMORY = 6
 
 C64 = 0
 C128 = 1
@@ -99,6 +100,15 @@ lib.jetgpu_max_exponent.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, _vp
 lib.jetgpu_take_device_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
 lib.jetgpu_probe_bounded_wait.argtypes = [ctypes.c_uint, _vp]
 lib.jetgpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+lib.jetgpu_malloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(_vp)]
+lib.jetgpu_free.argtypes = [_vp]
+lib.jetgpu_set_pool_limit.argtypes = [ctypes.c_size_t]
+lib.jetgpu_pool_bytes_in_use.restype = ctypes.c_size_t
+lib.jetgpu_pool_bytes_in_use.argtypes = []
+lib.jetgpu_range_push.argtypes = [ctypes.c_char_p]
+lib.jetgpu_range_push.restype = None
+lib.jetgpu_range_pop.argtypes = []
+lib.jetgpu_range_pop.restype = None
 
 
 class JetGpuError(RuntimeError):
@@ -344,6 +354,42 @@ def max_exponent(x, stream=None, out=None):
     check(lib.jetgpu_max_exponent(_ptr(x), x.numel(), dtype_code(x.dtype), _ptr(e),
                                   _stream(stream)))
     return e if out is not None else int(e.item())
+
+
+def set_pool_limit(nbytes: int) -> None:
+    """Caps the device bytes the library allocator may hold at once (0: no
+    cap). Allocations past the cap fail with ERR_MEMORY before any CUDA call."""
+    check(lib.jetgpu_set_pool_limit(int(nbytes)))
+
+
+def pool_bytes_in_use() -> int:
+    return int(lib.jetgpu_pool_bytes_in_use())
+
+
+def malloc(nbytes: int) -> int:
+    """Raw device allocation from the library allocator (an address)."""
+    p = _vp()
+    check(lib.jetgpu_malloc(int(nbytes), ctypes.byref(p)))
+    return p.value or 0
+
+
+def free(ptr: int) -> None:
+    check(lib.jetgpu_free(_vp(ptr)))
+
+
+class nvtx_range:
+    """NVTX range over a `with` block (visible to nsys / ncu)."""
+
+    def __init__(self, name: str):
+        self.name = name.encode()
+
+    def __enter__(self):
+        lib.jetgpu_range_push(self.name)
+        return self
+
+    def __exit__(self, *exc):
+        lib.jetgpu_range_pop()
+        return False
 
 
 def take_device_status() -> int:

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -19,6 +20,14 @@ inline cudaStream_t AsStream(void *s) { return reinterpret_cast<cudaStream_t>(s)
 
 // Checks the launch that was just enqueued.
 int CheckLaunch(const char *what);
+
+// An NVTX range for the scope (seen by nsys / ncu; no cost without a tool).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 #define JETGPU_CUDA_TRY(expr)                                                  \
     do {                                                                       \

@@ -170,6 +170,7 @@ extern "C" {
 int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m, uint64_t n,
                     uint64_t k, int dtype, void *stream)
 {
+    NvtxRange range("jetgpu_multiply");
     ClearError();
     return MultiplyPlain(A, B, C, m, n, k, dtype, 0, nullptr, 0, AsStream(stream));
 }
@@ -202,6 +203,7 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
                     int algo, int scale_a, int scale_b, void *workspace,
                     size_t workspace_bytes, void *stream)
 {
+    NvtxRange range("jetgpu_contract");
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     JETGPU_REQUIRE(precision >= JETGPU_PREC_FP32 && precision <= JETGPU_PREC_FP16X3,
@@ -425,6 +427,7 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
                             int algo, int scale_a, int scale_b, void *workspace,
                             size_t workspace_bytes, void *stream)
 {
+    NvtxRange range("jetgpu_contract_batched");
     ClearError();
     JETGPU_REQUIRE(batch >= 1, "batch must be at least 1");
     if (batch == 1 || (!a_batched && !b_batched)) {

@@ -675,6 +675,7 @@ extern "C" {
 int jetgpu_permute(const void *in, void *out, int rank, const uint64_t *shape,
                    const int32_t *perm, int dtype, void *stream)
 {
+    jetgpu::NvtxRange range("jetgpu_permute");
     jetgpu::ClearError();
     return jetgpu::PermuteImpl(in, out, 1, rank, shape, perm, dtype,
                                jetgpu::AsStream(stream));
@@ -684,6 +685,7 @@ int jetgpu_permute_batched(const void *in, void *out, uint64_t batch, int rank,
                            const uint64_t *shape, const int32_t *perm,
                            int dtype, void *stream)
 {
+    jetgpu::NvtxRange range("jetgpu_permute_batched");
     jetgpu::ClearError();
     return jetgpu::PermuteImpl(in, out, batch, rank, shape, perm, dtype,
                                jetgpu::AsStream(stream));

@@ -220,6 +220,7 @@ int jetgpu_conj(const void *in, void *out, uint64_t size, int dtype, void *strea
 int jetgpu_slice_sum_f64(const void *results, uint64_t n_slices, uint64_t size,
                          int dtype, void *out, int accumulate, void *stream)
 {
+    NvtxRange range("jetgpu_slice_sum_f64");
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     if (size == 0)

@@ -1,6 +1,7 @@
 // Error reporting and device queries of the jetgpu C-ABI.
 #include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "common.cuh"
 
@@ -109,6 +110,12 @@ int jetgpu_device_info(int *sm_count, int *cc_major, int *cc_minor)
 // freed blocks stay cached for reuse instead of returning to the driver.
 // ---------------------------------------------------------------------------
 namespace jetgpu {
+// jetgpu_malloc accounting for jetgpu_set_pool_limit.
+std::mutex g_pool_mutex;
+size_t g_pool_limit = 0;
+size_t g_pool_in_use = 0;
+std::unordered_map<void *, size_t> g_pool_sizes;
+
 namespace {
 std::mutex g_stream_mutex;
 cudaStream_t g_streams[64] = {nullptr};
@@ -157,8 +164,21 @@ int jetgpu_malloc(size_t bytes, void **ptr)
     *ptr = nullptr;
     if (bytes == 0)
         return JETGPU_OK;
+    const size_t rounded = (bytes + 255) / 256 * 256;
+    {
+        std::lock_guard<std::mutex> lock(jetgpu::g_pool_mutex);
+        if (jetgpu::g_pool_limit != 0 && jetgpu::g_pool_in_use + rounded > jetgpu::g_pool_limit)
+            return jetgpu::SetError(JETGPU_ERR_MEMORY,
+                                    "device memory limit of " +
+                                        std::to_string(jetgpu::g_pool_limit) + " bytes reached (" +
+                                        std::to_string(jetgpu::g_pool_in_use) + " in use, " +
+                                        std::to_string(rounded) + " requested)");
+    }
     cudaStream_t s = jetgpu::LibraryStream();
-    JETGPU_CUDA_TRY(cudaMallocAsync(ptr, (bytes + 255) / 256 * 256, s));
+    JETGPU_CUDA_TRY(cudaMallocAsync(ptr, rounded, s));
+    std::lock_guard<std::mutex> lock(jetgpu::g_pool_mutex);
+    jetgpu::g_pool_sizes[*ptr] = rounded;
+    jetgpu::g_pool_in_use += rounded;
     return JETGPU_OK;
 }
 
@@ -168,8 +188,32 @@ int jetgpu_free(void *ptr)
     if (ptr == nullptr)
         return JETGPU_OK;
     JETGPU_CUDA_TRY(cudaFreeAsync(ptr, jetgpu::LibraryStream()));
+    std::lock_guard<std::mutex> lock(jetgpu::g_pool_mutex);
+    auto it = jetgpu::g_pool_sizes.find(ptr);
+    if (it != jetgpu::g_pool_sizes.end()) {
+        jetgpu::g_pool_in_use -= it->second;
+        jetgpu::g_pool_sizes.erase(it);
+    }
     return JETGPU_OK;
 }
+
+int jetgpu_set_pool_limit(size_t bytes)
+{
+    jetgpu::ClearError();
+    std::lock_guard<std::mutex> lock(jetgpu::g_pool_mutex);
+    jetgpu::g_pool_limit = bytes;
+    return JETGPU_OK;
+}
+
+size_t jetgpu_pool_bytes_in_use(void)
+{
+    std::lock_guard<std::mutex> lock(jetgpu::g_pool_mutex);
+    return jetgpu::g_pool_in_use;
+}
+
+void jetgpu_range_push(const char *name) { nvtxRangePushA(name ? name : "jetgpu"); }
+
+void jetgpu_range_pop(void) { nvtxRangePop(); }
 
 int jetgpu_release_cached(void)
 {

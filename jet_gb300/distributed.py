@@ -6,7 +6,7 @@ networks (TaskBasedContractor.hpp:162-248, AddReductionTask :258-280).
 """
 from __future__ import annotations
 
-from typing import Sequence, Tuple
+from typing import Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -41,10 +41,23 @@ def reduce_partials(partial: Sequence[complex], group=None) -> np.ndarray:
     return v[:, 0] + 1j * v[:, 1]
 
 
-def contract_sharded(sliced_contractor, rank: int, world: int, group=None) -> np.ndarray:
-    """Contracts this rank's share of the slices and returns the total."""
+def contract_sharded(sliced_contractor, rank: int, world: int, group=None,
+                     checkpoint: Optional[str] = None, **checkpoint_args) -> np.ndarray:
+    """Contracts this rank's share of the slices and returns the total.
+
+    With `checkpoint`, each rank keeps its own resumable partial sum in
+    "<checkpoint>.rank<r>-of-<world>" (jet_gb300.checkpoint.contract_resumable;
+    `checkpoint_args` go to it), so a restarted job redoes no finished chunk."""
     first, count = shard_range(sliced_contractor.num_slices, sliced_contractor.batch_size,
                                rank, world)
-    part = sliced_contractor.contract(first, count) if count else [0j] * int(
-        np.prod(sliced_contractor.result_shape or [1]))
+    if not count:
+        part = [0j] * int(np.prod(sliced_contractor.result_shape or [1]))
+    elif checkpoint is not None:
+        from .checkpoint import contract_resumable
+
+        path = "%s.rank%d-of-%d" % (checkpoint, rank, world)
+        part = contract_resumable(sliced_contractor, path, first, count,
+                                  **checkpoint_args).reshape(-1)
+    else:
+        part = sliced_contractor.contract(first, count)
     return reduce_partials(part, group)

@@ -114,6 +114,7 @@ template <class T = std::complex<float>> class SlicedContractor {
             count = num_slices_ - first;
         JET_ABORT_IF(first + count > num_slices_, "Slice range out of bounds.");
         JET_ABORT_IF(count % batch_ != 0, "Slice count must be a multiple of the batch size.");
+        Gpu::Range range("Jet::SlicedContractor::Contract");
         if (!planned_)
             Plan();
         void *st = Gpu::Stream();

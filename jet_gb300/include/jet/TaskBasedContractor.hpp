@@ -148,6 +148,7 @@ template <class TensorType> class TaskBasedContractor {
 
     void Run()
     {
+        Gpu::Range range("Jet::TaskBasedContractor::Contract");
         // Index of the last contraction task consuming each name: its
         // deletion may run right after that task is enqueued.
         std::unordered_map<std::string, size_t> last_use;

@@ -55,6 +55,16 @@ inline void *Stream() { return jetgpu_default_stream(); }
 
 inline void Synchronize() { Check(jetgpu_stream_synchronize(Stream()), "synchronize"); }
 
+// A named NVTX range over the scope (jetgpu_range_push / jetgpu_range_pop):
+// the host loops show up in a timeline around the library's own ranges.
+class Range {
+  public:
+    explicit Range(const char *name) { jetgpu_range_push(name); }
+    ~Range() { jetgpu_range_pop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
+
 // Move-only owner of a device allocation from the library allocator.
 class DeviceBuffer {
   public:

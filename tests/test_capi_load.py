@@ -100,3 +100,36 @@ def test_fp16_stage_entry_points_need_exponents():
     assert rc == capi.ERR_INVALID and b"exponent" in capi.lib.jetgpu_last_error()
     rc = capi.lib.jetgpu_gemm_fp16x3(None, None, None, 128, 128, 64, 64, None, 1.0, None)
     assert rc == capi.ERR_INVALID and b"null" in capi.lib.jetgpu_last_error()
+
+
+def test_pool_limit_fails_allocations_on_the_host():
+    """A capped pool turns an allocation past the cap into ERR_MEMORY before
+    any CUDA call (host-side injection of device memory exhaustion)."""
+    from jet_gb300 import capi
+
+    assert capi.pool_bytes_in_use() == 0
+    capi.set_pool_limit(1)
+    try:
+        p = ctypes.c_void_p(0)
+        rc = capi.lib.jetgpu_malloc(1024, ctypes.byref(p))
+        assert rc == capi.ERR_MEMORY
+        assert p.value is None
+        msg = capi.lib.jetgpu_last_error().decode()
+        assert "device memory limit of 1 bytes reached" in msg
+        assert "1024 requested" in msg
+        # A zero-byte request needs no memory and passes.
+        assert capi.lib.jetgpu_malloc(0, ctypes.byref(p)) == capi.OK
+        with pytest.raises(capi.JetGpuError) as e:
+            capi.malloc(4096)
+        assert e.value.code == capi.ERR_MEMORY
+    finally:
+        capi.set_pool_limit(0)
+    assert capi.pool_bytes_in_use() == 0
+
+
+def test_nvtx_ranges_nest_without_a_tool():
+    from jet_gb300 import capi
+
+    with capi.nvtx_range("outer"):
+        with capi.nvtx_range("inner"):
+            pass

@@ -11,7 +11,12 @@ construction, conversions to and from Jet::Tensor (labels reversed), rename,
 reshape, column-major slicing and transposes, contractions (exact small
 cases, random tensors against Jet::Tensor, planned contraction into a
 preallocated output in either label order, complex128), additions, and a
-TaskBasedContractor network over CudaTensor."""
+TaskBasedContractor network over CudaTensor.
+
+pool_limit_test.cpp (GPU): device memory exhaustion injected through a capped
+library pool raises Jet::Exception from Tensor::ContractTensors,
+TaskBasedContractor and SlicedContractor, and each recovers once the cap is
+lifted."""
 import os
 import shutil
 import subprocess
@@ -43,6 +48,21 @@ def test_cuda_tensor_header_compiles(tmp_path):
 def test_cuda_tensor_behaviour(tmp_path, cuda):
     exe = str(tmp_path / "cuda_tensor_test")
     _compile(exe)
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0 and "ALL OK" in res.stdout, res.stdout[-4000:] + res.stderr[-2000:]
+
+
+def test_pool_limit_program_compiles(tmp_path):
+    _compile(str(tmp_path / "pool_limit_test"), "pool_limit_test.cpp")
+
+
+@pytest.mark.gpu
+def test_pool_limit_raises_jet_exception_and_recovers(tmp_path, cuda):
+    """Device memory exhaustion injected on the host (a capped pool): the
+    contraction raises Jet::Exception, the cap lifted it succeeds with the
+    uncapped result, and the failed attempts hold no device memory."""
+    exe = str(tmp_path / "pool_limit_test")
+    _compile(exe, "pool_limit_test.cpp")
     res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert res.returncode == 0 and "ALL OK" in res.stdout, res.stdout[-4000:] + res.stderr[-2000:]
 
