@@ -492,7 +492,8 @@ def run_sliced(args, rank, world, local_rank):
     slice of a seeded circuit network along one greedy path, in batched
     launches replayed from one CUDA graph, FP64 slice sum. Reports slices/s
     and effective TFLOP/s (4 x PathInfo flops per slice) for AUTO (FP16x3 on
-    the large steps; auto_tf32: TF32x3 there), BF16x3 and plain FP32, each
+    the large steps; auto_tf32: TF32x3 there), TUNED (the autotuner's fastest
+    form per step, tuned on the warm-up chunk), BF16x3 and plain FP32, each
     with its amplitude error against complex128 under --check-fp64."""
     import torch
 
@@ -529,6 +530,7 @@ def run_sliced(args, rank, world, local_rank):
     amps = {}
     # (name, precision, split form of AUTO's tensor-core steps)
     all_forms = (("auto", jet.PREC_AUTO, capi.PREC_FP16X3),
+                 ("tuned", jet.PREC_TUNED, capi.PREC_FP16X3),
                  ("auto_tf32", jet.PREC_AUTO, capi.PREC_TF32X3),
                  ("bf16x3", jet.PREC_BF16X3, None),
                  ("fp32", jet.PREC_FP32, None))
@@ -555,10 +557,18 @@ def run_sliced(args, rank, world, local_rank):
             sc.contract(start, count)
             reps.append(time.perf_counter() - t1)
         dt = statistics.median(reps)
+        tuned = None
+        if prec == jet.PREC_TUNED:
+            table = capi.autotune_table()
+            tuned = {"entries": len(table)}
+            for e in table:
+                tuned[e["choice"]] = tuned.get(e["choice"], 0) + 1
         forms[name] = {"slices_per_s": count / dt, "s_per_slice": dt / count,
                        "eff_tflops": 4.0 * sc.slice_dependent_flops * count / dt / 1e12,
                        "slices_timed": count, "runs": len(reps),
                        "arena_gb": sc.arena_bytes / 1e9}
+        if tuned is not None:
+            forms[name]["autotune"] = tuned
         amps[name] = amp
         slice_flops = sc.slice_flops
         dep_flops = sc.slice_dependent_flops
@@ -715,7 +725,7 @@ def main():
     ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3", "fp16x3"],
                     help="split form of the config-1 step (auto: all timed, the headline is "
                          "the fastest whose error on the step is within 1e-5)")
-    ap.add_argument("--sliced-forms", default="auto,auto_tf32,fp32",
+    ap.add_argument("--sliced-forms", default="auto,tuned,auto_tf32,fp32",
                     help="forms timed by the sliced configs (comma list of auto (FP16x3 on "
                          "the tensor-core steps), auto_tf32, bf16x3, fp32)")
     ap.add_argument("--sliced-batch", type=int, default=0,

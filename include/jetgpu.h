@@ -48,6 +48,9 @@ extern "C" {
 #define JETGPU_PREC_FP16X3 4 /* tcgen05 kind::f16 on FP16 hi/lo splits of power-of-two scaled
                                 operands, 3 products, FP32 accumulate: twice the TF32 rate,
                                 ~2^-22 truncation per product (TF32x3's) */
+#define JETGPU_PREC_TUNED 5  /* per contraction key, the fastest of FP32, TF32X3 (either main
+                                loop) and FP16X3, timed on first use (jetgpu_autotune_*);
+                                AUTO for small steps and for keys first met during capture */
 
 /* Complex product algorithms for the tensor-core form. */
 #define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
@@ -168,7 +171,7 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
  *
  * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3, JETGPU_PREC_BF16X3 or
  * JETGPU_PREC_FP16X3 (complex64 only; shapes with m or n below 2 take the
- * plain form) or JETGPU_PREC_AUTO. algo: JETGPU_ALGO_4M. FP16X3 needs
+ * plain form), JETGPU_PREC_AUTO or JETGPU_PREC_TUNED. algo: JETGPU_ALGO_4M. FP16X3 needs
  * |scale_a + scale_b| <= 126.
  * scale_a, scale_b: power-of-two exponents applied exactly to A and B before
  * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
@@ -298,6 +301,24 @@ int jetgpu_set_tc_chunk_depth(int k_depth);
  * JETGPU_PREC_FP16X3 (the default), JETGPU_PREC_TF32X3 or JETGPU_PREC_BF16X3.
  */
 int jetgpu_set_auto_form(int precision);
+
+/*
+ * The autotuner behind JETGPU_PREC_TUNED (no counterpart in the reference,
+ * which has one BLAS form). The first contraction with a given key (device,
+ * batch, batched operands, m, n, k, dtype, both shapes and permutations)
+ * times each candidate form on the caller's stream after one untimed run and
+ * keeps the fastest; later ones with that key run it directly, also inside a
+ * stream capture. Steps whose m n k times the batch is below `mnk` (default
+ * 2^20) take AUTO's rule. jetgpu_autotune_entry reports entry `index` (in the
+ * order they were made): batch, m, n, k, the chosen precision and main-loop
+ * variant, and the measured ms per contraction of the candidates FP32,
+ * TF32X3 (variant 0), TF32X3 (variant 1), FP16X3 (-1: not timed).
+ */
+int jetgpu_set_autotune_min_work(uint64_t mnk);
+size_t jetgpu_autotune_count(void);
+int jetgpu_autotune_entry(size_t index, uint64_t *batch_m_n_k, int *precision, int *variant,
+                          float *times_ms);
+int jetgpu_autotune_clear(void);
 
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,

@@ -35,5 +35,6 @@ PREC_TF32X3 = 1
 PREC_AUTO = 2
 PREC_BF16X3 = 3
 PREC_FP16X3 = 4
+PREC_TUNED = 5
 
 __version__ = version()

@@ -44,6 +44,7 @@ PREC_TF32X3 = 1
 PREC_AUTO = 2
 PREC_BF16X3 = 3
 PREC_FP16X3 = 4
+PREC_TUNED = 5
 
 ALGO_4M = 0
 
@@ -100,6 +101,12 @@ lib.jetgpu_max_exponent.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, _vp
 lib.jetgpu_take_device_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
 lib.jetgpu_probe_bounded_wait.argtypes = [ctypes.c_uint, _vp]
 lib.jetgpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+lib.jetgpu_set_autotune_min_work.argtypes = [ctypes.c_uint64]
+lib.jetgpu_autotune_count.restype = ctypes.c_size_t
+lib.jetgpu_autotune_count.argtypes = []
+lib.jetgpu_autotune_entry.argtypes = [ctypes.c_size_t, _u64p, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_float)]
 lib.jetgpu_malloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(_vp)]
 lib.jetgpu_free.argtypes = [_vp]
 lib.jetgpu_set_pool_limit.argtypes = [ctypes.c_size_t]
@@ -354,6 +361,37 @@ def max_exponent(x, stream=None, out=None):
     check(lib.jetgpu_max_exponent(_ptr(x), x.numel(), dtype_code(x.dtype), _ptr(e),
                                   _stream(stream)))
     return e if out is not None else int(e.item())
+
+
+AUTOTUNE_CANDIDATES = ("fp32", "tf32x3", "tf32x3_wide", "fp16x3")
+
+
+def set_autotune_min_work(mnk: int) -> None:
+    """PREC_TUNED tunes contractions whose m n k times the batch is at least
+    `mnk` (default 2^20); smaller ones take AUTO's rule."""
+    check(lib.jetgpu_set_autotune_min_work(int(mnk)))
+
+
+def autotune_clear() -> None:
+    check(lib.jetgpu_autotune_clear())
+
+
+def autotune_table():
+    """The autotuner's entries: batch, m, n, k, the chosen form and the
+    measured ms per contraction of each candidate (None: not timed)."""
+    out = []
+    for i in range(int(lib.jetgpu_autotune_count())):
+        bmnk = (ctypes.c_uint64 * 4)()
+        prec, var = ctypes.c_int(0), ctypes.c_int(0)
+        times = (ctypes.c_float * 4)()
+        check(lib.jetgpu_autotune_entry(i, bmnk, ctypes.byref(prec), ctypes.byref(var), times))
+        choice = {PREC_FP32: "fp32", PREC_FP16X3: "fp16x3"}.get(
+            prec.value, "tf32x3_wide" if var.value == 1 else "tf32x3")
+        out.append({"batch": bmnk[0], "m": bmnk[1], "n": bmnk[2], "k": bmnk[3],
+                    "choice": choice,
+                    "ms": {c: (float(t) if t >= 0 else None)
+                           for c, t in zip(AUTOTUNE_CANDIDATES, times)}})
+    return out
 
 
 def set_pool_limit(nbytes: int) -> None:

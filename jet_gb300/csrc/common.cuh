@@ -168,6 +168,30 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                            cudaStream_t stream, int variant = -1,
                            const int *e_max_dev = nullptr);
 
+// Workspace bytes of a (batched) contraction in `precision` (JETGPU_PREC_TUNED:
+// the largest of its candidates' and AUTO's).
+size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
+                         const int32_t *a_perm, int a_batched, int b_rank,
+                         const uint64_t *b_shape, const int32_t *b_perm, int b_batched, uint64_t m,
+                         uint64_t n, uint64_t k, int dtype, int precision);
+
+// A checked (batched) contraction in one form: precision FP32, TF32X3,
+// BF16X3, FP16X3 or AUTO; `variant` the tensor-core main loop (-1: the
+// jetgpu_set_tc_variant setting).
+int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                 const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                 const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
+                 uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st);
+
+// JETGPU_PREC_TUNED: the form the autotuner measured fastest for this
+// contraction's key, timing the candidates on first use (autotune.cu).
+int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
+                  uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a, int scale_b,
+                  void *workspace, cudaStream_t st);
+
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,
                   void *workspace, size_t ws_bytes, cudaStream_t stream);

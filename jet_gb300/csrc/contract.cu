@@ -51,7 +51,7 @@ std::atomic<int> g_auto_form{JETGPU_PREC_FP16X3};
 // pass costs more than the faster product saves, TF32x3 (same precision).
 constexpr double kAutoFp16MinWork = 1073741824.0; // 2^30
 
-SplitLayout LayoutFor(int precision, uint64_t k, double work)
+SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1)
 {
     if (precision == JETGPU_PREC_AUTO) {
         precision = g_auto_form.load(std::memory_order_relaxed);
@@ -65,7 +65,7 @@ SplitLayout LayoutFor(int precision, uint64_t k, double work)
     const uint64_t al = SplitPitchAlign(l.fmt);
     l.kp = (k + al - 1) / al * al;
     l.word = SplitWordBytes(l.fmt);
-    l.variant = TcVariant();
+    l.variant = variant >= 0 ? variant : TcVariant();
     l.b_planes = (l.fmt == SplitFormat::kTf32 && l.variant == 1) ? 6 : 4;
     return l;
 }
@@ -175,92 +175,6 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m, uint64_t 
     return MultiplyPlain(A, B, C, m, n, k, dtype, 0, nullptr, 0, AsStream(stream));
 }
 
-size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
-                                      const int32_t *a_perm, int b_rank,
-                                      const uint64_t *b_shape, const int32_t *b_perm,
-                                      uint64_t m, uint64_t n, uint64_t k, int dtype,
-                                      int precision)
-{
-    if (UseTensorCores(m, n, k, dtype, precision)) {
-        const SplitLayout l = LayoutFor(precision, k, (double)m * n * k);
-        return l.a_bytes(m) + AlignUp((l.fmt == SplitFormat::kTf32 ? 6 : 4) * n * l.kp * l.word) +
-               l.exp_bytes();
-    }
-    const size_t eb = ElemBytes(dtype);
-    size_t ws = 0;
-    if (!IsIdentity(a_rank, a_perm))
-        ws += AlignUp(m * k * eb);
-    if (!IsIdentity(b_rank, b_perm))
-        ws += AlignUp(k * n * eb);
-    ws += AlignUp(MultiplyPlainWorkspace(m, n, k, dtype));
-    return ws;
-}
-
-int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
-                    const int32_t *a_perm, const void *B, int b_rank,
-                    const uint64_t *b_shape, const int32_t *b_perm, void *C,
-                    uint64_t m, uint64_t n, uint64_t k, int dtype, int precision,
-                    int algo, int scale_a, int scale_b, void *workspace,
-                    size_t workspace_bytes, void *stream)
-{
-    NvtxRange range("jetgpu_contract");
-    ClearError();
-    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
-    JETGPU_REQUIRE(precision >= JETGPU_PREC_FP32 && precision <= JETGPU_PREC_FP16X3,
-                   "bad precision");
-    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
-    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
-         precision == JETGPU_PREC_FP16X3) &&
-        dtype != JETGPU_C64)
-        return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
-    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
-    if (rc)
-        return rc;
-    rc = Validate(b_rank, b_shape, b_perm, k, n, "B");
-    if (rc)
-        return rc;
-    if (m * n == 0)
-        return JETGPU_OK;
-    JETGPU_REQUIRE(C != nullptr, "null output");
-    JETGPU_REQUIRE(k == 0 || (A != nullptr && B != nullptr), "null operand");
-    const size_t need = jetgpu_contract_workspace_size(a_rank, a_shape, a_perm, b_rank,
-                                                       b_shape, b_perm, m, n, k, dtype,
-                                                       precision);
-    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
-        return SetError(JETGPU_ERR_WORKSPACE,
-                        "workspace too small: need " + std::to_string(need) + " bytes");
-    cudaStream_t st = AsStream(stream);
-    uint8_t *ws = static_cast<uint8_t *>(workspace);
-
-    if (k > 0 && UseTensorCores(m, n, k, dtype, precision))
-        return SplitProduct(LayoutFor(precision, k, (double)m * n * k), 1, A, a_rank, a_shape,
-                            a_perm, 1, B, b_rank, b_shape, b_perm, 1, C, m, n, k, dtype, scale_a,
-                            scale_b, ws, st);
-
-    const size_t eb = ElemBytes(dtype);
-    const void *at = A;
-    const void *btp = B;
-    if (k > 0 && !IsIdentity(a_rank, a_perm)) {
-        rc = PermuteImpl(A, ws, 1, a_rank, a_shape, a_perm, dtype, st);
-        if (rc)
-            return rc;
-        at = ws;
-        ws += AlignUp(m * k * eb);
-    }
-    if (k > 0 && !IsIdentity(b_rank, b_perm)) {
-        rc = PermuteImpl(B, ws, 1, b_rank, b_shape, b_perm, dtype, st);
-        if (rc)
-            return rc;
-        btp = ws;
-        ws += AlignUp(k * n * eb);
-    }
-    const size_t vec_ws = MultiplyPlainWorkspace(m, n, k, dtype);
-    return MultiplyPlain(at, btp, C, m, n, k, dtype, scale_a + scale_b, ws, vec_ws, st);
-}
-
-} // extern "C"
-
-extern "C" {
 
 int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
                       uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
@@ -382,29 +296,25 @@ void FoldShape(int rank, const uint64_t *shape, const int32_t *perm, uint64_t ba
         pm.push_back(perm[j] + 1);
 }
 
-} // namespace
-} // namespace jetgpu
-
-extern "C" {
-
-size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const uint64_t *a_shape,
-                                              const int32_t *a_perm, int a_batched, int b_rank,
-                                              const uint64_t *b_shape, const int32_t *b_perm,
-                                              int b_batched, uint64_t m, uint64_t n, uint64_t k,
-                                              int dtype, int precision)
+// Workspace of one form (precision FP32, TF32X3, BF16X3, FP16X3 or AUTO).
+size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_perm,
+                     int a_batched, int b_rank, const uint64_t *b_shape, const int32_t *b_perm,
+                     int b_batched, uint64_t m, uint64_t n, uint64_t k, int dtype, int precision)
 {
+    if (batch <= 1 || (!a_batched && !b_batched)) {
+        batch = 1;
+        a_batched = b_batched = 0;
+    }
     const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
-    if (batch <= 1 || (!a_batched && !b_batched))
-        return jetgpu_contract_workspace_size(a_rank, a_shape, a_perm, b_rank, b_shape, b_perm, m,
-                                              n, k, dtype, precision);
     if (p.fold) {
         std::vector<uint64_t> s;
         std::vector<int32_t> pm;
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
-        return jetgpu_contract_workspace_size(a_rank + 1, s.data(), pm.data(), b_rank, b_shape,
-                                              b_perm, batch * m, n, k, dtype, precision);
+        return FormWorkspace(1, a_rank + 1, s.data(), pm.data(), 0, b_rank, b_shape, b_perm, 0,
+                             batch * m, n, k, dtype, precision);
     }
     if (p.tc) {
+        // Sized for six TF32 B planes whatever the main-loop variant.
         const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k);
         return l.a_bytes(p.ba * m) +
                AlignUp((l.fmt == SplitFormat::kTf32 ? 6 : 4) * p.bb * n * l.kp * l.word) +
@@ -416,8 +326,178 @@ size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const 
         ws += AlignUp(p.ba * m * k * eb);
     if (!IsIdentity(b_rank, b_perm))
         ws += AlignUp(p.bb * k * n * eb);
-    ws += AlignUp(MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype));
+    ws += AlignUp(batch == 1 ? MultiplyPlainWorkspace(m, n, k, dtype)
+                             : MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype));
     return ws;
+}
+
+} // namespace
+
+size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
+                         const int32_t *a_perm, int a_batched, int b_rank,
+                         const uint64_t *b_shape, const int32_t *b_perm, int b_batched, uint64_t m,
+                         uint64_t n, uint64_t k, int dtype, int precision)
+{
+    if (precision != JETGPU_PREC_TUNED)
+        return FormWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm,
+                             b_batched, m, n, k, dtype, precision);
+    // Any candidate of the tuner, and AUTO (untuned steps).
+    size_t ws = 0;
+    for (int prec : {JETGPU_PREC_FP32, JETGPU_PREC_AUTO, JETGPU_PREC_TF32X3, JETGPU_PREC_FP16X3}) {
+        if (dtype != JETGPU_C64 && prec != JETGPU_PREC_FP32)
+            continue;
+        const size_t w = FormWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape,
+                                       b_perm, b_batched, m, n, k, dtype, prec);
+        ws = w > ws ? w : ws;
+    }
+    return ws;
+}
+
+int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                 const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                 const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
+                 uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st)
+{
+    if (batch <= 1 || (!a_batched && !b_batched)) {
+        batch = 1;
+        a_batched = b_batched = 0;
+    }
+    const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
+    if (p.fold) {
+        std::vector<uint64_t> s;
+        std::vector<int32_t> pm;
+        FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
+        return ContractForm(1, A, a_rank + 1, s.data(), pm.data(), 0, B, b_rank, b_shape, b_perm,
+                            0, C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
+                            workspace, st);
+    }
+    uint8_t *ws = static_cast<uint8_t *>(workspace);
+    if (k > 0 && p.tc)
+        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant), batch, A,
+                            a_rank, a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm, p.bb, C, m,
+                            n, k, dtype, scale_a, scale_b, ws, st);
+    int rc;
+    const size_t eb = ElemBytes(dtype);
+    const void *at = A;
+    const void *btp = B;
+    if (k > 0 && !IsIdentity(a_rank, a_perm)) {
+        if ((rc = PermuteImpl(A, ws, p.ba, a_rank, a_shape, a_perm, dtype, st)))
+            return rc;
+        at = ws;
+        ws += AlignUp(p.ba * m * k * eb);
+    }
+    if (k > 0 && !IsIdentity(b_rank, b_perm)) {
+        if ((rc = PermuteImpl(B, ws, p.bb, b_rank, b_shape, b_perm, dtype, st)))
+            return rc;
+        btp = ws;
+        ws += AlignUp(p.bb * k * n * eb);
+    }
+    if (batch == 1) {
+        const size_t vec_ws = MultiplyPlainWorkspace(m, n, k, dtype);
+        return MultiplyPlain(at, btp, C, m, n, k, dtype, scale_a + scale_b, ws, vec_ws, st);
+    }
+    const size_t vec_ws = MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype);
+    return MultiplyPlainBatched(at, btp, C, batch, p.ba > 1 ? m * k : 0, p.bb > 1 ? k * n : 0, m,
+                                n, k, dtype, scale_a + scale_b, vec_ws ? ws : nullptr, vec_ws, st);
+}
+
+namespace {
+
+// Argument checks shared by both entry points; JETGPU_OK when the product
+// has work to do, a status otherwise (*empty set when m n = 0).
+int CheckContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
+                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int algo,
+                  void *workspace, size_t workspace_bytes, bool *empty)
+{
+    *empty = false;
+    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
+    JETGPU_REQUIRE(precision >= JETGPU_PREC_FP32 && precision <= JETGPU_PREC_TUNED,
+                   "bad precision");
+    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
+    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
+         precision == JETGPU_PREC_FP16X3) &&
+        dtype != JETGPU_C64)
+        return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
+    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
+    if (rc)
+        return rc;
+    if ((rc = Validate(b_rank, b_shape, b_perm, k, n, "B")))
+        return rc;
+    if (m * n == 0) {
+        *empty = true;
+        return JETGPU_OK;
+    }
+    JETGPU_REQUIRE(C != nullptr, "null output");
+    JETGPU_REQUIRE(k == 0 || (A != nullptr && B != nullptr), "null operand");
+    const size_t need = ContractWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank,
+                                          b_shape, b_perm, b_batched, m, n, k, dtype, precision);
+    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
+        return SetError(JETGPU_ERR_WORKSPACE,
+                        "workspace too small: need " + std::to_string(need) + " bytes");
+    return JETGPU_OK;
+}
+
+int Contract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+             const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+             const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C, uint64_t m,
+             uint64_t n, uint64_t k, int dtype, int precision, int algo, int scale_a, int scale_b,
+             void *workspace, size_t workspace_bytes, cudaStream_t st)
+{
+    bool empty = false;
+    int rc = CheckContract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
+                           b_perm, b_batched, C, m, n, k, dtype, precision, algo, workspace,
+                           workspace_bytes, &empty);
+    if (rc || empty)
+        return rc;
+    if (precision == JETGPU_PREC_TUNED)
+        return ContractTuned(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
+                             b_perm, b_batched, C, m, n, k, dtype, scale_a, scale_b, workspace,
+                             st);
+    return ContractForm(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
+                        b_batched, C, m, n, k, dtype, precision, -1, scale_a, scale_b, workspace,
+                        st);
+}
+
+} // namespace
+} // namespace jetgpu
+
+extern "C" {
+
+size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
+                                      const int32_t *a_perm, int b_rank,
+                                      const uint64_t *b_shape, const int32_t *b_perm,
+                                      uint64_t m, uint64_t n, uint64_t k, int dtype,
+                                      int precision)
+{
+    return ContractWorkspace(1, a_rank, a_shape, a_perm, 0, b_rank, b_shape, b_perm, 0, m, n, k,
+                             dtype, precision);
+}
+
+int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
+                    const int32_t *a_perm, const void *B, int b_rank,
+                    const uint64_t *b_shape, const int32_t *b_perm, void *C,
+                    uint64_t m, uint64_t n, uint64_t k, int dtype, int precision,
+                    int algo, int scale_a, int scale_b, void *workspace,
+                    size_t workspace_bytes, void *stream)
+{
+    NvtxRange range("jetgpu_contract");
+    ClearError();
+    return Contract(1, A, a_rank, a_shape, a_perm, 0, B, b_rank, b_shape, b_perm, 0, C, m, n, k,
+                    dtype, precision, algo, scale_a, scale_b, workspace, workspace_bytes,
+                    AsStream(stream));
+}
+
+size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const uint64_t *a_shape,
+                                              const int32_t *a_perm, int a_batched, int b_rank,
+                                              const uint64_t *b_shape, const int32_t *b_perm,
+                                              int b_batched, uint64_t m, uint64_t n, uint64_t k,
+                                              int dtype, int precision)
+{
+    return ContractWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm,
+                             b_batched, m, n, k, dtype, precision);
 }
 
 int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
@@ -430,64 +510,11 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
     NvtxRange range("jetgpu_contract_batched");
     ClearError();
     JETGPU_REQUIRE(batch >= 1, "batch must be at least 1");
-    if (batch == 1 || (!a_batched && !b_batched)) {
-        JETGPU_REQUIRE(batch == 1, "a batch needs at least one batched operand");
-        return jetgpu_contract(A, a_rank, a_shape, a_perm, B, b_rank, b_shape, b_perm, C, m, n, k,
-                               dtype, precision, algo, scale_a, scale_b, workspace,
-                               workspace_bytes, stream);
-    }
-    const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
-    if (p.fold) {
-        std::vector<uint64_t> s;
-        std::vector<int32_t> pm;
-        FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
-        return jetgpu_contract(A, a_rank + 1, s.data(), pm.data(), B, b_rank, b_shape, b_perm, C,
-                               batch * m, n, k, dtype, precision, algo, scale_a, scale_b,
-                               workspace, workspace_bytes, stream);
-    }
-    JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
-    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
-    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
-    if (rc)
-        return rc;
-    rc = Validate(b_rank, b_shape, b_perm, k, n, "B");
-    if (rc)
-        return rc;
-    if (m * n == 0)
-        return JETGPU_OK;
-    const size_t need = jetgpu_contract_batched_workspace_size(
-        batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm, b_batched, m, n, k,
-        dtype, precision);
-    if (need > 0 && (workspace == nullptr || workspace_bytes < need))
-        return SetError(JETGPU_ERR_WORKSPACE,
-                        "workspace too small: need " + std::to_string(need) + " bytes");
-    cudaStream_t st = AsStream(stream);
-    uint8_t *ws = static_cast<uint8_t *>(workspace);
-    if (k > 0 && p.tc)
-        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k), batch, A, a_rank,
-                            a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm, p.bb, C, m, n, k,
-                            dtype, scale_a, scale_b, ws, st);
-    const size_t eb = ElemBytes(dtype);
-    const void *at = A;
-    const void *btp = B;
-    if (k > 0 && !IsIdentity(a_rank, a_perm)) {
-        rc = PermuteImpl(A, ws, p.ba, a_rank, a_shape, a_perm, dtype, st);
-        if (rc)
-            return rc;
-        at = ws;
-        ws += AlignUp(p.ba * m * k * eb);
-    }
-    if (k > 0 && !IsIdentity(b_rank, b_perm)) {
-        rc = PermuteImpl(B, ws, p.bb, b_rank, b_shape, b_perm, dtype, st);
-        if (rc)
-            return rc;
-        btp = ws;
-        ws += AlignUp(p.bb * k * n * eb);
-    }
-    const size_t vec_ws = MultiplyPlainBatchedWorkspace(batch, m, n, k, dtype);
-    return MultiplyPlainBatched(at, btp, C, batch, p.ba > 1 ? m * k : 0, p.bb > 1 ? k * n : 0, m,
-                                n, k, dtype, scale_a + scale_b, vec_ws ? ws : nullptr, vec_ws,
-                                st);
+    JETGPU_REQUIRE(batch == 1 || a_batched || b_batched,
+                   "a batch needs at least one batched operand");
+    return Contract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
+                    b_batched, C, m, n, k, dtype, precision, algo, scale_a, scale_b, workspace,
+                    workspace_bytes, AsStream(stream));
 }
 
 } // extern "C"

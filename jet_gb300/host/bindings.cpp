@@ -289,7 +289,8 @@ PYBIND11_MODULE(_jet_bindings, m)
     BindSliced<std::complex<double>>(m);
     m.def("version", [] { return std::string("0.2.3-gb300"); });
     m.def("set_precision", &Jet::Gpu::SetPrecision, py::arg("precision"),
-          "ContractTensors arithmetic for complex64: 0 plain FP32, 1 TF32x3, 2 auto, 3 BF16x3.");
+          "ContractTensors arithmetic for complex64: 0 plain FP32, 1 TF32x3, 2 auto, 3 BF16x3, "
+          "4 FP16x3, 5 tuned (the autotuner's fastest per shape).");
     m.def("get_precision", &Jet::Gpu::GetPrecision);
     py::register_exception<Jet::Exception>(m, "JetException", PyExc_RuntimeError);
 }

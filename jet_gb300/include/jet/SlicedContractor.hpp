@@ -548,10 +548,13 @@ template <class T = std::complex<float>> class SlicedContractor {
                        "operand reorder");
             b = tmp_b_.get();
         }
+        // Steps that run once gain nothing from tuning: AUTO's rule.
+        const int prec =
+            (!s.chunk && precision_ == JETGPU_PREC_TUNED) ? JETGPU_PREC_AUTO : precision_;
         Gpu::Check(jetgpu_contract_batched(
                        s.batch, a, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(),
                        s.batched, b, (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(),
-                       s.batched, Buffer(s.out), s.m, s.n, s.k, dt, precision_, JETGPU_ALGO_4M,
+                       s.batched, Buffer(s.out), s.m, s.n, s.k, dt, prec, JETGPU_ALGO_4M,
                        0, 0, ws_.get(), ws_.size(), st),
                    "batched contraction");
     }

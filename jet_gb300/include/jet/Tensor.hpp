@@ -12,7 +12,8 @@
 // the reference exactly, so results carry the same index order.
 //
 // Arithmetic form of ContractTensors (complex64): Gpu::SetPrecision(
-// JETGPU_PREC_FP32 | JETGPU_PREC_TF32X3 | JETGPU_PREC_AUTO | JETGPU_PREC_BF16X3);
+// JETGPU_PREC_FP32 | JETGPU_PREC_TF32X3 | JETGPU_PREC_AUTO | JETGPU_PREC_BF16X3 |
+// JETGPU_PREC_FP16X3 | JETGPU_PREC_TUNED);
 // default FP32, the arithmetic class of the reference's cgemm. complex128
 // always uses FP64.
 #pragma once

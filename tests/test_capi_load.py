@@ -133,3 +133,22 @@ def test_nvtx_ranges_nest_without_a_tool():
     with capi.nvtx_range("outer"):
         with capi.nvtx_range("inner"):
             pass
+
+
+def test_tuned_precision_accepted_and_workspace_covers_every_form():
+    """TUNED is a valid precision code; its workspace is at least that of each
+    form it may pick (host arithmetic only)."""
+    from jet_gb300 import capi
+
+    shape, perm = [2] * 12, list(range(12))
+    sizes = {p: capi.contract_workspace_size(shape, perm[::-1], shape, perm, 64, 64, 64,
+                                             capi.C64, p)
+             for p in (capi.PREC_FP32, capi.PREC_AUTO, capi.PREC_TF32X3, capi.PREC_FP16X3,
+                       capi.PREC_TUNED)}
+    assert sizes[capi.PREC_TUNED] == max(sizes.values())
+    rc = capi.lib.jetgpu_contract(None, 12, capi.u64(shape), capi.i32(perm), None, 12,
+                                  capi.u64(shape), capi.i32(perm), None, 64, 64, 64, capi.C64,
+                                  6, capi.ALGO_4M, 0, 0, None, 0, None)
+    assert rc == capi.ERR_INVALID and b"bad precision" in capi.lib.jetgpu_last_error()
+    assert capi.lib.jetgpu_autotune_count() == 0
+    assert capi.lib.jetgpu_autotune_entry(0, None, None, None, None) == capi.ERR_INVALID
