@@ -535,6 +535,7 @@ def run_sliced(args, rank, world, local_rank):
                  ("bf16x3", jet.PREC_BF16X3, None),
                  ("fp32", jet.PREC_FP32, None))
     sliced_forms = tuple(f for f in all_forms if f[0] in args.sliced_forms.split(","))
+    profiles = {}
     for name, prec, auto_form in sliced_forms:
         capi.set_auto_form(auto_form or capi.PREC_FP16X3)
         sc = jet.SlicedContractorC64(tn, path, sliced, prec)
@@ -557,12 +558,17 @@ def run_sliced(args, rank, world, local_rank):
             sc.contract(start, count)
             reps.append(time.perf_counter() - t1)
         dt = statistics.median(reps)
+        if args.profile_chunk and rank == 0:
+            profiles[name] = sc.profile_chunk(start)
         tuned = None
         if prec == jet.PREC_TUNED:
             table = capi.autotune_table()
             tuned = {"entries": len(table)}
             for e in table:
                 tuned[e["choice"]] = tuned.get(e["choice"], 0) + 1
+            if args.autotune_dump and rank == 0:
+                with open(args.autotune_dump, "w") as f:
+                    json.dump(table, f, indent=1)
         forms[name] = {"slices_per_s": count / dt, "s_per_slice": dt / count,
                        "eff_tflops": 4.0 * sc.slice_dependent_flops * count / dt / 1e12,
                        "slices_timed": count, "runs": len(reps),
@@ -573,6 +579,10 @@ def run_sliced(args, rank, world, local_rank):
         slice_flops = sc.slice_flops
         dep_flops = sc.slice_dependent_flops
         del sc
+    if profiles:
+        with open(args.profile_chunk, "w") as f:
+            json.dump(profiles, f, indent=1)
+
     def rel_to_fp32(f):
         if f not in amps or "fp32" not in amps:
             return None
@@ -620,6 +630,7 @@ def run_sliced(args, rank, world, local_rank):
         "amplitude_sample": [amps[head].real, amps[head].imag],
         "rel_diff_auto_vs_fp32": rel,
         "rel_diff_bf16x3_vs_fp32": rel_bf,
+        "rel_diff_tuned_vs_fp32": rel_to_fp32("tuned"),
         "slice_vs_fp64": slice_check,
         "plan_seconds": plan_s,
     }
@@ -720,6 +731,12 @@ def main():
                     help="profiling case: rank-25 x rank-25 (M = N = 2^12, K = 2^13)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="skip the plain-FP32, end-to-end and CPU legs")
+    ap.add_argument("--autotune-dump", default=None,
+                    help="sliced configs: write the autotuner's table (per-step candidate "
+                         "times) of the tuned form to this JSON file")
+    ap.add_argument("--profile-chunk", default=None,
+                    help="sliced configs: write each form's per-step device times of one chunk "
+                         "(SlicedContractor.profile_chunk) to this JSON file")
     ap.add_argument("--check-fp64", action="store_true",
                     help="sliced configs: also contract slice 0 in complex128")
     ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3", "fp16x3"],

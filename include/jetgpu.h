@@ -112,6 +112,13 @@ int jetgpu_graph_end(void *stream, void **graph_exec);
 int jetgpu_graph_launch(void *graph_exec, void *stream);
 int jetgpu_graph_destroy(void *graph_exec);
 
+/* CUDA events for timing host loops above the boundary: create, record on a
+ * stream, elapsed ms between two recorded events (waits for `end`), destroy. */
+int jetgpu_event_create(void **event);
+int jetgpu_event_record(void *event, void *stream);
+int jetgpu_event_elapsed_ms(void *start, void *end, float *ms);
+int jetgpu_event_destroy(void *event);
+
 /* Message of the last failing call made by this host thread ("" if none). */
 const char *jetgpu_last_error(void);
 

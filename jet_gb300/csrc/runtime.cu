@@ -315,4 +315,39 @@ int jetgpu_graph_destroy(void *graph_exec)
     return JETGPU_OK;
 }
 
+int jetgpu_event_create(void **event)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(event != nullptr, "null output pointer");
+    cudaEvent_t e = nullptr;
+    JETGPU_CUDA_TRY(cudaEventCreate(&e));
+    *event = (void *)e;
+    return JETGPU_OK;
+}
+
+int jetgpu_event_record(void *event, void *stream)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(event != nullptr, "null event");
+    JETGPU_CUDA_TRY(cudaEventRecord((cudaEvent_t)event, jetgpu::AsStream(stream)));
+    return JETGPU_OK;
+}
+
+int jetgpu_event_elapsed_ms(void *start, void *end, float *ms)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(start != nullptr && end != nullptr && ms != nullptr, "null pointer");
+    JETGPU_CUDA_TRY(cudaEventSynchronize((cudaEvent_t)end));
+    JETGPU_CUDA_TRY(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end));
+    return JETGPU_OK;
+}
+
+int jetgpu_event_destroy(void *event)
+{
+    jetgpu::ClearError();
+    if (event)
+        JETGPU_CUDA_TRY(cudaEventDestroy((cudaEvent_t)event));
+    return JETGPU_OK;
+}
+
 } // extern "C"

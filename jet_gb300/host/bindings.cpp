@@ -236,6 +236,29 @@ template <class T> void BindSliced(py::module_ &m)
                  return s.Contract(first, c);
              },
              py::arg("first") = 0, py::arg("count") = py::none())
+        .def("profile_chunk",
+             [](sc_t &s, size_t first) {
+                 std::vector<typename sc_t::ChunkProfileEntry> prof;
+                 {
+                     py::gil_scoped_release release;
+                     prof = s.ProfileChunk(first);
+                 }
+                 py::list out;
+                 for (const auto &e : prof) {
+                     py::dict d;
+                     d["kind"] = e.kind;
+                     d["step"] = e.step;
+                     d["batch"] = e.batch;
+                     d["m"] = e.m;
+                     d["n"] = e.n;
+                     d["k"] = e.k;
+                     d["ms"] = e.ms;
+                     out.append(d);
+                 }
+                 return out;
+             },
+             py::arg("first") = 0,
+             "Device ms of every gather, reorder, contraction and the slice sum of one chunk.")
         .def_property_readonly("batch_size", &sc_t::GetBatchSize)
         .def_property_readonly("num_slices", &sc_t::GetNumSlices)
         .def_property_readonly("result_indices", &sc_t::GetResultIndices)

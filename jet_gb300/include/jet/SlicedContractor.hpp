@@ -140,6 +140,41 @@ template <class T = std::complex<float>> class SlicedContractor {
         return out;
     }
 
+    // One entry of ProfileChunk: a slice gather ("gather"), an operand
+    // reorder ("reorder"), a path step ("contract"), the result reorder
+    // ("result reorder") or the FP64 slice sum ("slice sum").
+    struct ChunkProfileEntry {
+        std::string kind;
+        int step; // index into the path (-1 when not a step)
+        uint64_t batch, m, n, k;
+        double ms;
+    };
+
+    // Runs one chunk (slices [first, first + batch size)) eagerly with a CUDA
+    // event after every gather, reorder, contraction and the slice sum, and
+    // returns each one's device time: a per-step profile of what the captured
+    // graph replays. The accumulator holds that chunk's sum afterwards.
+    std::vector<ChunkProfileEntry> ProfileChunk(size_t first = 0)
+    {
+        JET_ABORT_IF(first % batch_ != 0 || first + batch_ > num_slices_,
+                     "Chunk start must be a multiple of the batch size inside the slice range.");
+        JET_ABORT_IF(sliced_.empty(), "A network without sliced indices has no chunk.");
+        Gpu::Range range("Jet::SlicedContractor::ProfileChunk");
+        if (!planned_)
+            Plan();
+        void *st = Gpu::Stream();
+        RunPrefix(st);
+        Gpu::Check(jetgpu_memset_zero(acc_.get(), result_size_ * 16, st), "zero accumulator");
+        const uint64_t first64 = first;
+        Gpu::Check(jetgpu_memcpy(counter_.get(), &first64, 8, 0, st), "slice counter");
+        Profile prof(st);
+        RecordChunk(st, &prof);
+        const std::vector<double> ms = prof.timer.Finish();
+        for (size_t i = 0; i < prof.entries.size(); ++i)
+            prof.entries[i].ms = ms[i];
+        return prof.entries;
+    }
+
     // Labels and shape of the result (the "$b" axis, if any, included).
     const std::vector<std::string> &GetResultIndices() const { return result_labels_; }
     const std::vector<size_t> &GetResultShape() const { return result_dims_; }
@@ -186,6 +221,16 @@ template <class T = std::complex<float>> class SlicedContractor {
         std::vector<uint64_t> a_pre_shape, b_pre_shape;
         std::vector<int32_t> a_pre_perm, b_pre_perm;
         size_t ws = 0;
+    };
+    struct Profile {
+        explicit Profile(void *st) : timer(st) {}
+        Gpu::StreamTimer timer;
+        std::vector<ChunkProfileEntry> entries;
+        void Mark(const char *kind, int step, uint64_t b, uint64_t m, uint64_t n, uint64_t k)
+        {
+            timer.Mark();
+            entries.push_back(ChunkProfileEntry{kind, step, b, m, n, k, 0.0});
+        }
     };
     struct Loader { // a "$s" leaf gathered per chunk
         int leaf;
@@ -531,9 +576,10 @@ template <class T = std::complex<float>> class SlicedContractor {
         prefix_done_ = true;
     }
 
-    void Launch(const Step &s, void *st)
+    void Launch(const Step &s, void *st, Profile *prof = nullptr)
     {
         const int dt = Gpu::DtypeCode<T>();
+        const int idx = (int)(&s - steps_.data());
         const void *a = Buffer(s.a);
         const void *b = Buffer(s.b);
         if (!s.a_pre_perm.empty()) {
@@ -541,12 +587,16 @@ template <class T = std::complex<float>> class SlicedContractor {
                                       s.a_pre_shape.data(), s.a_pre_perm.data(), dt, st),
                        "operand reorder");
             a = tmp_a_.get();
+            if (prof)
+                prof->Mark("reorder", idx, s.batch, s.m, s.k, 0);
         }
         if (!s.b_pre_perm.empty()) {
             Gpu::Check(jetgpu_permute(b, tmp_b_.get(), (int)s.b_pre_shape.size(),
                                       s.b_pre_shape.data(), s.b_pre_perm.data(), dt, st),
                        "operand reorder");
             b = tmp_b_.get();
+            if (prof)
+                prof->Mark("reorder", idx, s.batch, s.k, s.n, 0);
         }
         // Steps that run once gain nothing from tuning: AUTO's rule.
         const int prec =
@@ -557,6 +607,8 @@ template <class T = std::complex<float>> class SlicedContractor {
                        s.batched, Buffer(s.out), s.m, s.n, s.k, dt, prec, JETGPU_ALGO_4M,
                        0, 0, ws_.get(), ws_.size(), st),
                    "batched contraction");
+        if (prof)
+            prof->Mark("contract", idx, s.batch, s.m, s.n, s.k);
     }
 
     void Capture(void *st)
@@ -578,10 +630,10 @@ template <class T = std::complex<float>> class SlicedContractor {
 
     // Enqueues one chunk: gather the "$s" leaves, run the "$s" steps, add the
     // chunk's slices into the FP64 accumulator, advance the slice counter.
-    void RecordChunk(void *st)
+    void RecordChunk(void *st, Profile *prof = nullptr)
     {
         const int dt = Gpu::DtypeCode<T>();
-        for (const Loader &ld : loaders_)
+        for (const Loader &ld : loaders_) {
             Gpu::Check(jetgpu_slice_gather_at(leaves_[ld.leaf].GetDeviceData(),
                                               (int)ld.shape.size(), ld.shape.data(),
                                               (int)ld.axes.size(), ld.axes.data(),
@@ -589,18 +641,25 @@ template <class T = std::complex<float>> class SlicedContractor {
                                               static_cast<const uint64_t *>(counter_.get()),
                                               batch_, Buffer(ld.leaf), dt, st),
                        "slice gather");
+            if (prof)
+                prof->Mark("gather", -1, batch_, 0, 0, 0);
+        }
         for (const Step &s : steps_)
             if (s.chunk)
-                Launch(s, st);
+                Launch(s, st, prof);
         const void *fin = Buffer(final_id_);
         if (final_perm_needed_) {
             Gpu::Check(jetgpu_permute(fin, final_tmp_.get(), (int)final_shape_.size(),
                                       final_shape_.data(), final_perm_.data(), dt, st),
                        "result reorder");
             fin = final_tmp_.get();
+            if (prof)
+                prof->Mark("result reorder", -1, batch_, 0, 0, 0);
         }
         Gpu::Check(jetgpu_slice_sum_f64(fin, batch_, result_size_, dt, acc_.get(), 1, st),
                    "slice sum");
+        if (prof)
+            prof->Mark("slice sum", -1, batch_, 0, 0, 0);
         Gpu::Check(jetgpu_counter_add(static_cast<uint64_t *>(counter_.get()), batch_, st),
                    "counter");
     }

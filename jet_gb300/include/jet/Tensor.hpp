@@ -66,6 +66,43 @@ class Range {
     Range &operator=(const Range &) = delete;
 };
 
+// Device time of consecutive stretches of work on a stream: each Mark()
+// records a CUDA event; Finish() waits and returns the ms between each mark
+// and the one before (the first against construction).
+class StreamTimer {
+  public:
+    explicit StreamTimer(void *stream) : stream_(stream) { Push(); }
+    ~StreamTimer()
+    {
+        for (void *e : events_)
+            jetgpu_event_destroy(e);
+    }
+    StreamTimer(const StreamTimer &) = delete;
+    StreamTimer &operator=(const StreamTimer &) = delete;
+    void Mark() { Push(); }
+    std::vector<double> Finish()
+    {
+        std::vector<double> ms;
+        for (size_t i = 1; i < events_.size(); ++i) {
+            float t = 0;
+            Check(jetgpu_event_elapsed_ms(events_[i - 1], events_[i], &t), "event time");
+            ms.push_back(t);
+        }
+        return ms;
+    }
+
+  private:
+    void Push()
+    {
+        void *e = nullptr;
+        Check(jetgpu_event_create(&e), "event create");
+        events_.push_back(e);
+        Check(jetgpu_event_record(e, stream_), "event record");
+    }
+    void *stream_;
+    std::vector<void *> events_;
+};
+
 // Move-only owner of a device allocation from the library allocator.
 class DeviceBuffer {
   public:

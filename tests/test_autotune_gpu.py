@@ -43,7 +43,7 @@ def _want(capi, a, a_shape, a_perm, b, b_shape, b_perm, m, n, k):
     return at @ bt
 
 
-@pytest.mark.parametrize("lm,lk,ln", [(10, 10, 10), (12, 8, 6), (6, 12, 10), (9, 7, 1)])
+@pytest.mark.parametrize("lm,lk,ln", [(10, 10, 10), (12, 8, 6), (6, 12, 10), (12, 9, 0)])
 def test_tuned_matches_fp64_and_tunes_once(tuner, cuda, lm, lk, ln):
     capi = tuner
     a, sa, pa, b, sb, pb = _operands(cuda, lm, lk, ln, seed=lm * 100 + lk * 10 + ln)

@@ -196,3 +196,29 @@ def test_network_amplitude_within_1e5_of_fp64(jet, precision):
     sc.set_batch_size(2)
     got = sc.contract()[0]
     assert abs(got - want) <= 1e-5 * abs(want), abs(got - want) / abs(want)
+
+
+def test_profile_chunk_times_every_launch(jet):
+    """profile_chunk: one entry per slice gather, operand reorder, path step
+    and the slice sum of a chunk, each with a device time; the chunk's sum is
+    left in the accumulator and later contractions are unaffected."""
+    from jet_gb300 import circuits
+
+    net = circuits.random_circuit_network(4, 4, 8, seed=21, dtype=np.dtype("complex64"))
+    path = circuits.find_path(net, restarts=2, seed=21)
+    sliced = circuits.choose_slices(net, path, 4)
+    sc = jet.SlicedContractorC64(_tn(jet, net, "complex64"), path, sliced, 2)
+    sc.set_batch_size(4)
+    want = sc.contract()[0]
+    prof = sc.profile_chunk(4)
+    kinds = [e["kind"] for e in prof]
+    assert kinds.count("slice sum") == 1 and kinds[-1] == "slice sum"
+    assert kinds.count("gather") >= 1 and kinds.count("contract") >= 1
+    assert set(kinds) <= {"gather", "reorder", "contract", "result reorder", "slice sum"}
+    assert all(e["ms"] >= 0 for e in prof)
+    steps = [e["step"] for e in prof if e["kind"] == "contract"]
+    assert steps == sorted(steps) and len(set(steps)) == len(steps)
+    assert all(0 <= s < len(path) for s in steps)
+    with pytest.raises(Exception, match="multiple of the batch size"):
+        sc.profile_chunk(2)
+    assert sc.contract()[0] == want
