@@ -163,96 +163,109 @@ template <typename T> struct KahanSum {
     }
 };
 
-// y[b, m] (+ partial s) = sum_{k in chunk s} A_b[m, k] x_b[k]; one warp per
-// row, batch b = blockIdx.z (operand strides sa, sb; 0 = shared). Partial s
-// of row (b, m) lands at out[(s * batch + b) * M + m].
+// y[b, m] (+ partial s) = sum_{k in chunk s} A_b[m, k] x_b[k]. A CTA of 8
+// warps covers `rows` rows (8, 4, 2 or 1) with 8 / rows warps per row, which
+// interleave the row's k chunk, so few rows still keep every warp streaming.
+// Batch b = blockIdx.z (operand strides sa, sb; 0 = shared). Partial s of row
+// (b, m) lands at out[(s * batch + b) * M + m].
 template <typename T>
 __global__ void __launch_bounds__(256)
     gemv_rows_kernel(const typename C2<T>::type *__restrict__ A,
                      const typename C2<T>::type *__restrict__ x,
                      typename C2<T>::type *__restrict__ out, int64_t M,
-                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb)
+                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb, int rows)
 {
     using V = typename C2<T>::type;
     const int lane = threadIdx.x & 31;
-    const int64_t m = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int warp = threadIdx.x >> 5;
+    const int wpr = 8 / rows; // warps per row
+    const int part = warp % wpr;
+    const int64_t m = (int64_t)blockIdx.x * rows + warp / wpr;
     const int64_t s = blockIdx.y;
     const int64_t b = blockIdx.z;
-    if (m >= M)
-        return;
     A += b * sa;
     x += b * sb;
     out += (s * gridDim.z + b) * M;
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
     KahanSum<T> sr, si;
-    for (int64_t k = k_begin + lane; k < k_end; k += 32) {
-        V a = A[m * K + k], b = x[k];
-        sr.add(fma(a.x, b.x, -a.y * b.y));
-        si.add(fma(a.x, b.y, a.y * b.x));
-    }
+    if (m < M)
+        for (int64_t k = k_begin + part * 32 + lane; k < k_end; k += wpr * 32) {
+            V a = A[m * K + k], b = x[k];
+            sr.add(fma(a.x, b.x, -a.y * b.y));
+            si.add(fma(a.x, b.y, a.y * b.x));
+        }
     T re = sr.s, im = si.s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
         im += __shfl_xor_sync(0xffffffffu, im, o);
     }
-    if (lane == 0)
+    __shared__ T wre[8], wim[8];
+    if (lane == 0) {
+        wre[warp] = re;
+        wim[warp] = im;
+    }
+    __syncthreads();
+    if (lane == 0 && part == 0 && m < M) {
+        for (int w = 1; w < wpr; ++w) { // fixed order: deterministic
+            re += wre[warp + w];
+            im += wim[warp + w];
+        }
         out[m] = V{re * scale, im * scale};
+    }
 }
 
-// y[b, n] (+ partial s) = sum_{k in chunk s} x_b[k] B_b[k, n]; one thread
-// per column, batch b = blockIdx.z (strides sa, sb; 0 = shared). Partial s of
-// column (b, n) lands at out[(s * batch + b) * N + n].
+// y[b, n] (+ partial s) = sum_{k in chunk s} x_b[k] B_b[k, n]. A CTA of 256
+// threads covers `cols` columns (a power of two up to 256) with 256 / cols
+// threads per column, which interleave the k chunk: thread t takes column
+// t % cols and rows k = t / cols (mod 256 / cols), so consecutive threads read
+// consecutive elements of B's rows. `cols` = 1 is the dot product. Batch b =
+// blockIdx.z (strides sa, sb; 0 = shared). Partial s of column (b, n) lands at
+// out[(s * batch + b) * N + n].
 template <typename T>
 __global__ void __launch_bounds__(256)
     gemv_cols_kernel(const typename C2<T>::type *__restrict__ x,
                      const typename C2<T>::type *__restrict__ B,
                      typename C2<T>::type *__restrict__ out, int64_t N,
-                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb)
+                     int64_t K, int64_t kchunk, T scale, int64_t sa, int64_t sb, int cols)
 {
     using V = typename C2<T>::type;
     const int64_t s = blockIdx.y;
     const int64_t b = blockIdx.z;
+    const int tk_count = 256 / cols;
+    const int tn = threadIdx.x % cols;
+    const int tk = threadIdx.x / cols;
+    const int64_t n = (int64_t)blockIdx.x * cols + tn;
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
     x += b * sa;
     B += b * sb;
     out += (s * gridDim.z + b) * N;
-    if (N == 1) {
-        // Dot product: the block reduces its k chunk.
-        KahanSum<T> sr, si;
-        for (int64_t k = k_begin + threadIdx.x; k < k_end; k += blockDim.x) {
-            V a = x[k], b = B[k];
-            sr.add(fma(a.x, b.x, -a.y * b.y));
-            si.add(fma(a.x, b.y, a.y * b.x));
-        }
-        T re = sr.s, im = si.s;
-        __shared__ T sre[256], sim[256];
-        sre[threadIdx.x] = re;
-        sim[threadIdx.x] = im;
-        __syncthreads();
-        for (int w = 128; w > 0; w >>= 1) {
-            if ((int)threadIdx.x < w) {
-                sre[threadIdx.x] += sre[threadIdx.x + w];
-                sim[threadIdx.x] += sim[threadIdx.x + w];
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0)
-            out[0] = V{sre[0] * scale, sim[0] * scale};
-        return;
-    }
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N)
-        return;
     KahanSum<T> sr, si;
-    for (int64_t k = k_begin; k < k_end; ++k) {
-        V a = x[k], b = B[k * N + n];
-        sr.add(fma(a.x, b.x, -a.y * b.y));
-        si.add(fma(a.x, b.y, a.y * b.x));
+    if (n < N)
+        for (int64_t k = k_begin + tk; k < k_end; k += tk_count) {
+            V a = x[k], v = B[k * N + n];
+            sr.add(fma(a.x, v.x, -a.y * v.y));
+            si.add(fma(a.x, v.y, a.y * v.x));
+        }
+    if (tk_count == 1) {
+        if (n < N)
+            out[n] = V{sr.s * scale, si.s * scale};
+        return;
     }
-    out[n] = V{sr.s * scale, si.s * scale};
+    __shared__ T pre[256], pim[256];
+    pre[threadIdx.x] = sr.s;
+    pim[threadIdx.x] = si.s;
+    __syncthreads();
+    if (tk == 0 && n < N) {
+        T re = 0, im = 0;
+        for (int j = 0; j < tk_count; ++j) { // fixed order: deterministic
+            re += pre[j * cols + tn];
+            im += pim[j * cols + tn];
+        }
+        out[n] = V{re * scale, im * scale};
+    }
 }
 
 template <typename T>
@@ -294,17 +307,28 @@ int64_t SplitK(int64_t blocks_per_split, int64_t K)
     return s < 1 ? 1 : s;
 }
 
-// CTAs per batch element of the vector kernels, and the vector length.
-inline void VectorShape(int64_t m, int64_t n, int64_t &blocks, int64_t &len)
+// Smallest power of two >= v, at most `cap`.
+inline int Pow2AtLeast(int64_t v, int cap)
+{
+    int p = 1;
+    while (p < v && p < cap)
+        p <<= 1;
+    return p;
+}
+
+// CTAs per batch element of the vector kernels, the rows (gemv_rows_kernel)
+// or columns (gemv_cols_kernel) each CTA covers, and the vector length.
+inline void VectorShape(int64_t m, int64_t n, int64_t &blocks, int &per_cta, int64_t &len)
 {
     if (n == 1 && m > 1) {
-        blocks = (m + 7) / 8; // gemv_rows_kernel: 8 rows per CTA
+        per_cta = Pow2AtLeast(m, 8);
         len = m;
     }
     else {
-        blocks = n == 1 ? 1 : (n + 255) / 256; // gemv_cols_kernel (DOTU: one CTA)
+        per_cta = Pow2AtLeast(n, 256); // 1: the dot product
         len = n;
     }
+    blocks = (len + per_cta - 1) / per_cta;
 }
 
 // Bytes of partial sums the split-k vector products of `batch` products use
@@ -316,7 +340,8 @@ size_t VectorWorkspace(int64_t batch, int64_t m, int64_t n, int64_t k)
     if ((m > 1 && n > 1) || batch < 1)
         return 0;
     int64_t blocks, len;
-    VectorShape(m, n, blocks, len);
+    int per_cta;
+    VectorShape(m, n, blocks, per_cta, len);
     const int64_t S = SplitK(blocks * batch, k);
     return S > 1 ? (size_t)(S * batch * len) * sizeof(V) : 0;
 }
@@ -335,15 +360,18 @@ int MultiplyVectorT(const typename C2<T>::type *A, const typename C2<T>::type *B
     const size_t need = VectorWorkspace<T>(batch, M, N, K);
     const bool split = need > 0 && ws != nullptr && ws_bytes >= need;
     int64_t blocks, len;
-    VectorShape(M, N, blocks, len);
+    int per_cta;
+    VectorShape(M, N, blocks, per_cta, len);
     const int64_t S = split ? SplitK(blocks * batch, K) : 1;
     const int64_t kchunk = (K + S - 1) / S;
     V *dst = S > 1 ? (V *)ws : C;
     const dim3 grid((unsigned)blocks, (unsigned)S, (unsigned)batch);
     if (N == 1 && M > 1)
-        gemv_rows_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, M, K, kchunk, scale, sa, sb);
+        gemv_rows_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, M, K, kchunk, scale, sa, sb,
+                                                      per_cta);
     else
-        gemv_cols_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, N, K, kchunk, scale, sa, sb);
+        gemv_cols_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, N, K, kchunk, scale, sa, sb,
+                                                      per_cta);
     int rc = CheckLaunch(N == 1 && M > 1 ? "gemv_rows_kernel" : "gemv_cols_kernel");
     if (rc || S == 1)
         return rc;
