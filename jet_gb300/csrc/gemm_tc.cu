@@ -26,6 +26,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 
@@ -308,14 +309,10 @@ template <int V>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_split_kernel(const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB,
-                          float2 *__restrict__ C, int M, int N, int ktiles,
+                          float2 *__restrict__ C, int M, int N, int ktiles, int batch,
                           float scale, int a_batched, int b_batched, int chunk_stages,
                           const int *__restrict__ scale_exps)
 {
-    // Batch b = blockIdx.z: a batched operand is read through a 4-D map
-    // (k, row, batch, plane), a shared one through a 3-D map (k, row, plane).
-    const int bz = blockIdx.z;
-    C += (size_t)bz * M * N;
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
     constexpr int kFmt = Cfg::Fmt;
@@ -336,20 +333,34 @@ __global__ void __launch_bounds__(kThreads, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    // Grouped tile order: consecutive CTAs walk kGroupM tile rows down one
-    // tile column before moving to the next column, so the CTAs resident at
-    // one time cover a compact block of C (about 8 x 19 tiles on 152 SMs) and
-    // share their A and B tiles through L2 instead of each tile row
-    // streaming all of B from HBM.
+    // Persistent: CTA c takes tiles c, c + G, c + 2G, ... (G = gridDim.x) of
+    // the batch's tiles laid end to end. Within one product the order is
+    // grouped: consecutive tiles walk kGroupM tile rows down one tile column
+    // before moving to the next column, so the tiles in flight at one time
+    // cover a compact block of C (about 8 x 19 tiles on 152 SMs) and share
+    // their A and B tiles through L2 instead of each tile row streaming all
+    // of B from HBM. The stage ring and the two TMEM accumulator sets run on
+    // across tiles, so one tile's epilogue overlaps the next tile's loads and
+    // MMAs. Batch b of a batched operand is read through a 4-D map (k, row,
+    // batch, plane), a shared one through a 3-D map (k, row, plane).
     const int n_tiles = (N + kBN - 1) / kBN;
     const int m_tiles = (M + kBM - 1) / kBM;
+    const int tiles_per_product = m_tiles * n_tiles;
     const int span = kGroupM * n_tiles;
-    const int group = (int)blockIdx.x / span;
-    const int first_m = group * kGroupM;
-    const int gm = min(kGroupM, m_tiles - first_m);
-    const int in_group = (int)blockIdx.x - group * span;
-    const int m0 = (first_m + in_group % gm) * kBM;
-    const int n0 = (in_group / gm) * kBN;
+    const int my_tiles =
+        ((int)(tiles_per_product * batch) - (int)blockIdx.x + (int)gridDim.x - 1) /
+        (int)gridDim.x;
+    auto tile_at = [&](int i, int &bz, int &m0, int &n0) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        bz = t / tiles_per_product;
+        const int u = t - bz * tiles_per_product;
+        const int group = u / span;
+        const int first_m = group * kGroupM;
+        const int gm = min(kGroupM, m_tiles - first_m);
+        const int in_group = u - group * span;
+        m0 = (first_m + in_group % gm) * kBM;
+        n0 = (in_group / gm) * kBN;
+    };
     const int nchunks = (ktiles + chunk_stages - 1) / chunk_stages;
 
     if (threadIdx.x == 0) {
@@ -378,11 +389,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         if (lane == 0) {
             // TMA producer.
+            bool ok = true;
+            for (int i = 0; i < my_tiles && ok; ++i) {
+            int bz, m0, n0;
+            tile_at(i, bz, m0, n0);
             for (int kt = 0; kt < ktiles; ++kt) {
-                const int s = kt % kStages;
-                const uint32_t phase = (uint32_t)(kt / kStages) & 1u;
-                if (!MbarWait(SmemAddr(&empty_bar[s]), phase ^ 1u))
+                const long long g = (long long)i * ktiles + kt; // stage-ring position
+                const int s = (int)(g % kStages);
+                const uint32_t phase = (uint32_t)(g / kStages) & 1u;
+                if (!MbarWait(SmemAddr(&empty_bar[s]), phase ^ 1u)) {
+                    ok = false;
                     break;
+                }
                 const uint32_t fb = SmemAddr(&full_bar[s]);
                 MbarArriveExpectTx(fb, kStageBytes);
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
@@ -409,6 +427,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         TmaLoad3d(base + (4 + t) * kTileBytes, &tmB, k0, n0, plane, fb);
                 }
             }
+            }
         }
         __syncwarp();
     }
@@ -418,19 +437,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false, kFmt);
             constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kFmt);
             bool ok = true;
+            for (int i = 0; i < my_tiles && ok; ++i)
             for (int kt = 0; kt < ktiles && ok; ++kt) {
                 const int chunk = kt / chunk_stages;
-                const int buf = chunk & 1;
+                // Accumulator set: chunks alternate across tiles too.
+                const long long gc = (long long)i * nchunks + chunk;
+                const int buf = (int)(gc & 1);
                 const int in_chunk = kt - chunk * chunk_stages;
                 const bool chunk_start = in_chunk == 0;
                 const bool chunk_end = in_chunk == chunk_stages - 1 || kt == ktiles - 1;
                 if (chunk_start &&
-                    !MbarWait(SmemAddr(&acc_empty[buf]), ((uint32_t)(chunk >> 1) & 1u) ^ 1u)) {
+                    !MbarWait(SmemAddr(&acc_empty[buf]), ((uint32_t)(gc >> 1) & 1u) ^ 1u)) {
                     ok = false;
                     break;
                 }
-                const int s = kt % kStages;
-                const uint32_t phase = (uint32_t)(kt / kStages) & 1u;
+                const long long g = (long long)i * ktiles + kt;
+                const int s = (int)(g % kStages);
+                const uint32_t phase = (uint32_t)(g / kStages) & 1u;
                 if (!MbarWait(SmemAddr(&full_bar[s]), phase)) {
                     ok = false;
                     break;
@@ -506,16 +529,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int quad = warp & 3;
         const int half = (warp - 2) >> 2;
         const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+        // The FP16 form's operand scales, undone in the epilogue by two exact
+        // multiplies (each factor inside the float range).
+        float f1 = 1.f, f2 = 1.f;
+        if (scale_exps != nullptr) {
+            const int e = -(Fp16ScaleExp(scale_exps[0]) + Fp16ScaleExp(scale_exps[1]));
+            f1 = Pow2f(e / 2);
+            f2 = Pow2f(e - e / 2);
+        }
+        bool ok = true;
+        for (int i = 0; i < my_tiles && ok; ++i) {
+        int bz, m0, n0;
+        tile_at(i, bz, m0, n0);
         float acc_re[64], acc_im[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) {
             acc_re[j] = 0.f;
             acc_im[j] = 0.f;
         }
-        bool ok = true;
         for (int chunk = 0; chunk < nchunks; ++chunk) {
-            const int buf = chunk & 1;
-            ok = MbarWait(SmemAddr(&acc_full[buf]), (uint32_t)(chunk >> 1) & 1u);
+            const long long gc = (long long)i * nchunks + chunk;
+            const int buf = (int)(gc & 1);
+            ok = MbarWait(SmemAddr(&acc_full[buf]), (uint32_t)(gc >> 1) & 1u);
             __syncwarp();
             if (!ok)
                 break;
@@ -541,10 +576,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                              : "memory");
         }
         if (scale_exps != nullptr) {
-            // Undo the operands' power-of-two FP16 scales: two exact
-            // multiplies keep each factor inside the float range.
-            const int e = -(Fp16ScaleExp(scale_exps[0]) + Fp16ScaleExp(scale_exps[1]));
-            const float f1 = Pow2f(e / 2), f2 = Pow2f(e - e / 2);
 #pragma unroll
             for (int j = 0; j < 64; ++j) {
                 acc_re[j] = acc_re[j] * f1 * f2;
@@ -554,7 +585,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int row = m0 + quad * 32 + lane;
         if (ok && row < M) {
             const int cbase = n0 + half * 64;
-            float2 *dst = C + (size_t)row * N + cbase;
+            float2 *dst = C + (size_t)bz * M * N + (size_t)row * N + cbase;
             if (cbase + 64 <= N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
 #pragma unroll
                 for (int j = 0; j < 64; j += 2) {
@@ -569,6 +600,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (cbase + j < N)
                         dst[j] = make_float2(acc_re[j] * scale, acc_im[j] * scale);
             }
+        }
         }
     }
     FenceBeforeSync();
@@ -674,12 +706,15 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
                                              (int)smem));
         configured_dev = dev;
     }
-    // One CTA per 128 x 128 tile of C in the grouped order, blockIdx.z = batch.
-    dim3 grid((unsigned)(((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM)), 1, (unsigned)batch);
+    // Persistent: one CTA per SM (at most one per 128 x 128 tile of C), each
+    // walking the batch's tiles in the grouped order.
+    const uint64_t tiles = ((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM) * batch;
+    JETGPU_REQUIRE(tiles <= 0x7fffffffull, "too many tiles");
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)SmCount());
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
-        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, out_scale, a_batched,
-        b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev);
+        ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
+        a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev);
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
