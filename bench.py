@@ -198,6 +198,18 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def apply_tc_knobs(args):
+    """The tensor-core product settings given on the command line."""
+    import jet_gb300.capi as capi
+
+    if args.tc_variant is not None:
+        capi.set_tc_variant(args.tc_variant)
+    if args.tc_chunk is not None:
+        capi.set_tc_chunk_depth(args.tc_chunk)
+    if args.tc_persistent is not None:
+        capi.set_tc_persistent(args.tc_persistent)
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -205,10 +217,7 @@ def run_ours(args, rank, world, local_rank):
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
-    if args.tc_variant is not None:
-        capi.set_tc_variant(args.tc_variant)
-    if args.tc_chunk is not None:
-        capi.set_tc_chunk_depth(args.tc_chunk)
+    apply_tc_knobs(args)
     w = workload(12, N_COMMON, 12) if args.small else workload()
     m, n, k = w["m"], w["n"], w["k"]
     kp = k
@@ -501,6 +510,7 @@ def run_sliced(args, rank, world, local_rank):
     from jet_gb300 import capi, circuits
 
     torch.cuda.set_device(local_rank)
+    apply_tc_knobs(args)
     rows, cols, cycles, removed, n_sliced, batch, chunks, restarts = SLICED_CONFIGS[args.config]
     if args.sliced_batch:
         batch = args.sliced_batch
@@ -751,6 +761,9 @@ def main():
                     help="batches timed by the sliced configs (0: the config's own)")
     ap.add_argument("--tc-chunk", type=int, default=None,
                     help="K depth accumulated in tensor memory per fold (0 = defaults)")
+    ap.add_argument("--tc-persistent", type=int, default=None, choices=[0, 1],
+                    help="tensor-core products: 1 one persistent CTA per SM (default), "
+                         "0 one CTA per tile")
     ap.add_argument("--tc-variant", type=int, default=None,
                     help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",

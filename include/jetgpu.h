@@ -292,6 +292,14 @@ int jetgpu_set_tc_variant(int variant);
 int jetgpu_tc_b_planes(void);
 
 /*
+ * jetgpu_set_tc_persistent(1) (the default) runs the tensor-core products as
+ * one persistent CTA per SM walking the tiles, each tile's epilogue
+ * overlapping the next tile's loads and MMAs; 0 launches one CTA per tile and
+ * lets the hardware schedule them.
+ */
+int jetgpu_set_tc_persistent(int on);
+
+/*
  * jetgpu_set_tc_chunk_depth sets, for the calling process, the K depth the
  * tensor-core products accumulate in tensor memory before folding the partial
  * sum into FP32 registers (round to nearest); 0 restores the defaults (16 for

@@ -70,6 +70,7 @@ lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                   ctypes.c_int, _vp, _vp]
 lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
+lib.jetgpu_set_tc_persistent.argtypes = [ctypes.c_int]
 lib.jetgpu_set_tc_chunk_depth.argtypes = [ctypes.c_int]
 lib.jetgpu_set_auto_form.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
@@ -255,6 +256,12 @@ def set_tc_variant(variant: int) -> None:
     """0: default main loops; 1: TF32 with N = 256 MMAs (six B planes);
     2: BF16 with 32-byte rows in 6 stages."""
     check(lib.jetgpu_set_tc_variant(int(variant)))
+
+
+def set_tc_persistent(on: bool) -> None:
+    """Tensor-core products as one persistent CTA per SM (default) or one CTA
+    per tile."""
+    check(lib.jetgpu_set_tc_persistent(int(bool(on))))
 
 
 def set_auto_form(precision: int) -> None:

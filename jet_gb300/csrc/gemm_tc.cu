@@ -691,6 +691,10 @@ int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint6
     return JETGPU_OK;
 }
 
+// Persistent launch (one CTA per SM walking the tiles) or one CTA per tile
+// (jetgpu_set_tc_persistent).
+std::atomic<int> g_tc_persistent{1};
+
 template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
@@ -707,10 +711,13 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
         configured_dev = dev;
     }
     // Persistent: one CTA per SM (at most one per 128 x 128 tile of C), each
-    // walking the batch's tiles in the grouped order.
+    // walking the batch's tiles in the grouped order; otherwise one CTA per
+    // tile.
     const uint64_t tiles = ((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM) * batch;
     JETGPU_REQUIRE(tiles <= 0x7fffffffull, "too many tiles");
-    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)SmCount());
+    const unsigned grid = (unsigned)(g_tc_persistent.load(std::memory_order_relaxed)
+                                         ? std::min<uint64_t>(tiles, (uint64_t)SmCount())
+                                         : tiles);
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
@@ -800,6 +807,14 @@ bool TcWide() { return TcVariant() == 1; }
 } // namespace jetgpu
 
 extern "C" int jetgpu_tc_b_planes(void) { return jetgpu::TcWide() ? 6 : 4; }
+
+extern "C" int jetgpu_set_tc_persistent(int on)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(on == 0 || on == 1, "persistent must be 0 or 1");
+    jetgpu::g_tc_persistent.store(on, std::memory_order_relaxed);
+    return JETGPU_OK;
+}
 
 extern "C" int jetgpu_set_tc_variant(int variant)
 {

@@ -214,3 +214,36 @@ def test_tmem_chunk_depth_controls_accumulation_error(cuda):
     assert errs[0] == errs[16]
     assert errs[16] < errs[128]
     assert errs[16] <= 1e-6, errs
+
+
+@pytest.mark.parametrize("precision", [1, 3, 4])
+def test_persistent_and_per_tile_launches_agree_bitwise(cuda, precision):
+    """The persistent tensor-core launch (one CTA per SM walking the tiles)
+    computes every tile exactly as the one-CTA-per-tile launch: same bits, for
+    partial edge tiles and a batch whose tiles span several rounds."""
+    import torch
+
+    from jet_gb300 import capi
+
+    m, n, k, batch = 1000, 700, 900, 3
+    g = torch.Generator(device=cuda)
+    g.manual_seed(precision)
+    a = torch.randn(batch * m * k, dtype=torch.complex64, device=cuda, generator=g)
+    b = torch.randn(batch * k * n, dtype=torch.complex64, device=cuda, generator=g)
+    outs = []
+    try:
+        for persistent in (1, 0):
+            capi.set_tc_persistent(persistent)
+            c = capi.contract_batched(batch, a, [m, k], [0, 1], 1, b, [k, n], [0, 1], 1, m, n, k,
+                                      precision=precision)
+            c1 = capi.contract(a[: m * k], [m, k], [0, 1], b[: k * n], [k, n], [0, 1], m, n, k,
+                               precision=precision)
+            outs.append((c.clone(), c1.clone()))
+    finally:
+        capi.set_tc_persistent(1)
+    assert torch.equal(outs[0][0].view(torch.int64), outs[1][0].view(torch.int64))
+    assert torch.equal(outs[0][1].view(torch.int64), outs[1][1].view(torch.int64))
+    want = (a[: m * k].view(m, k).cpu().numpy().astype(np.complex128)
+            @ b[: k * n].view(k, n).cpu().numpy().astype(np.complex128))
+    got = outs[0][0][: m * n].view(m, n).cpu().numpy()
+    assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
