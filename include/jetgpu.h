@@ -300,6 +300,13 @@ int jetgpu_tc_b_planes(void);
 int jetgpu_set_tc_persistent(int on);
 
 /*
+ * jetgpu_set_tc_group_m sets the tile order of the tensor-core products:
+ * consecutive tiles walk `group_m` tile rows (128 rows each) down one tile
+ * column before moving to the next column (default 8; 1 is row-major).
+ */
+int jetgpu_set_tc_group_m(int group_m);
+
+/*
  * jetgpu_set_tc_chunk_depth sets, for the calling process, the K depth the
  * tensor-core products accumulate in tensor memory before folding the partial
  * sum into FP32 registers (round to nearest); 0 restores the defaults (16 for

@@ -71,6 +71,7 @@ lib.jetgpu_split_tf32.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint
                                   ctypes.c_int, _vp, _vp]
 lib.jetgpu_set_tc_variant.argtypes = [ctypes.c_int]
 lib.jetgpu_set_tc_persistent.argtypes = [ctypes.c_int]
+lib.jetgpu_set_tc_group_m.argtypes = [ctypes.c_int]
 lib.jetgpu_set_tc_chunk_depth.argtypes = [ctypes.c_int]
 lib.jetgpu_set_auto_form.argtypes = [ctypes.c_int]
 lib.jetgpu_gemm_tf32x3.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
@@ -262,6 +263,11 @@ def set_tc_persistent(on: bool) -> None:
     """Tensor-core products as one persistent CTA per SM (default) or one CTA
     per tile."""
     check(lib.jetgpu_set_tc_persistent(int(bool(on))))
+
+
+def set_tc_group_m(group_m: int) -> None:
+    """Tile rows per group of the tensor-core products' tile order (default 8)."""
+    check(lib.jetgpu_set_tc_group_m(int(group_m)))
 
 
 def set_auto_form(precision: int) -> None:

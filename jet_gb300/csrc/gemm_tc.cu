@@ -43,7 +43,7 @@ constexpr int kBN = 128;
 constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
-constexpr int kGroupM = 8;                    // tile rows per group of the tile order
+constexpr int kGroupM = 8;                    // default tile rows per group of the tile order
 
 // Every stage holds boxes of 128 rows x RowBytes (swizzled by RowBytes);
 // every MMA consumes 32 bytes of K per row. Main-loop variants:
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles, int batch,
                           float scale, int a_batched, int b_batched, int chunk_stages,
-                          const int *__restrict__ scale_exps)
+                          const int *__restrict__ scale_exps, int group_m)
 {
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int lane = threadIdx.x & 31;
     // Persistent: CTA c takes tiles c, c + G, c + 2G, ... (G = gridDim.x) of
     // the batch's tiles laid end to end. Within one product the order is
-    // grouped: consecutive tiles walk kGroupM tile rows down one tile column
+    // grouped: consecutive tiles walk group_m tile rows down one tile column
     // before moving to the next column, so the tiles in flight at one time
     // cover a compact block of C (about 8 x 19 tiles on 152 SMs) and share
     // their A and B tiles through L2 instead of each tile row streaming all
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int n_tiles = (N + kBN - 1) / kBN;
     const int m_tiles = (M + kBM - 1) / kBM;
     const int tiles_per_product = m_tiles * n_tiles;
-    const int span = kGroupM * n_tiles;
+    const int span = group_m * n_tiles;
     const int my_tiles =
         ((int)(tiles_per_product * batch) - (int)blockIdx.x + (int)gridDim.x - 1) /
         (int)gridDim.x;
@@ -355,8 +355,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         bz = t / tiles_per_product;
         const int u = t - bz * tiles_per_product;
         const int group = u / span;
-        const int first_m = group * kGroupM;
-        const int gm = min(kGroupM, m_tiles - first_m);
+        const int first_m = group * group_m;
+        const int gm = min(group_m, m_tiles - first_m);
         const int in_group = u - group * span;
         m0 = (first_m + in_group % gm) * kBM;
         n0 = (in_group / gm) * kBN;
@@ -694,6 +694,8 @@ int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint6
 // Persistent launch (one CTA per SM walking the tiles) or one CTA per tile
 // (jetgpu_set_tc_persistent).
 std::atomic<int> g_tc_persistent{1};
+// Tile rows per group of the tile order (jetgpu_set_tc_group_m).
+std::atomic<int> g_tc_group_m{kGroupM};
 
 template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
@@ -721,7 +723,8 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
-        a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev);
+        a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev,
+        g_tc_group_m.load(std::memory_order_relaxed));
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
@@ -807,6 +810,14 @@ bool TcWide() { return TcVariant() == 1; }
 } // namespace jetgpu
 
 extern "C" int jetgpu_tc_b_planes(void) { return jetgpu::TcWide() ? 6 : 4; }
+
+extern "C" int jetgpu_set_tc_group_m(int group_m)
+{
+    jetgpu::ClearError();
+    JETGPU_REQUIRE(group_m >= 1 && group_m <= 1024, "group_m must be in [1, 1024]");
+    jetgpu::g_tc_group_m.store(group_m, std::memory_order_relaxed);
+    return JETGPU_OK;
+}
 
 extern "C" int jetgpu_set_tc_persistent(int on)
 {
