@@ -44,6 +44,7 @@ constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
 constexpr int kGroupM = 8;                    // default tile rows per group of the tile order
+constexpr int kTileRing = 4;                  // tile indices in flight between the warp roles
 
 // Every stage holds boxes of 128 rows x RowBytes (swizzled by RowBytes);
 // every MMA consumes 32 bytes of K per row. Main-loop variants:
@@ -311,7 +312,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                           const __grid_constant__ CUtensorMap tmB,
                           float2 *__restrict__ C, int M, int N, int ktiles, int batch,
                           float scale, int a_batched, int b_batched, int chunk_stages,
-                          const int *__restrict__ scale_exps, int group_m)
+                          const int *__restrict__ scale_exps, int group_m,
+                          unsigned int *__restrict__ tile_counter)
 {
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
@@ -327,14 +329,23 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ __align__(8) uint64_t empty_bar[kStages];
     __shared__ __align__(8) uint64_t acc_full[2];
     __shared__ __align__(8) uint64_t acc_empty[2];
+    __shared__ __align__(8) uint64_t tile_full[kTileRing];
+    __shared__ __align__(8) uint64_t tile_empty[kTileRing];
+    __shared__ int tile_ring[kTileRing];
     __shared__ uint32_t tmem_slot;
 
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    // Persistent: CTA c takes tiles c, c + G, c + 2G, ... (G = gridDim.x) of
-    // the batch's tiles laid end to end. Within one product the order is
+    // Persistent: the batch's tiles laid end to end are handed out in order,
+    // by an atomic counter when the launch has one (tile_counter, zeroed
+    // before the launch), else CTA c takes tiles c, c + G, c + 2G, ...
+    // (G = gridDim.x). The producer warp draws each tile and passes its index
+    // to the MMA and accumulator warps through a ring in shared memory
+    // (tile_full / tile_empty); an index past the end stops them. Drawing
+    // from a counter keeps the tiles in flight a compact window of the order
+    // however the CTAs' speeds drift apart. Within one product the order is
     // grouped: consecutive tiles walk group_m tile rows down one tile column
     // before moving to the next column, so the tiles in flight at one time
     // cover a compact block of C (about 8 x 19 tiles on 152 SMs) and share
@@ -347,11 +358,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int m_tiles = (M + kBM - 1) / kBM;
     const int tiles_per_product = m_tiles * n_tiles;
     const int span = group_m * n_tiles;
-    const int my_tiles =
-        ((int)(tiles_per_product * batch) - (int)blockIdx.x + (int)gridDim.x - 1) /
-        (int)gridDim.x;
-    auto tile_at = [&](int i, int &bz, int &m0, int &n0) {
-        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+    const int total_tiles = tiles_per_product * batch;
+    auto tile_at = [&](int t, int &bz, int &m0, int &n0) {
         bz = t / tiles_per_product;
         const int u = t - bz * tiles_per_product;
         const int group = u / span;
@@ -372,6 +380,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             MbarInit(SmemAddr(&acc_full[b]), 1);
             MbarInit(SmemAddr(&acc_empty[b]), kAccWarps);
         }
+        for (int r = 0; r < kTileRing; ++r) {
+            MbarInit(SmemAddr(&tile_full[r]), 1);
+            MbarInit(SmemAddr(&tile_empty[r]), 1 + kAccWarps);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -388,11 +400,23 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            // TMA producer.
+            // Tile scheduler and TMA producer.
             bool ok = true;
-            for (int i = 0; i < my_tiles && ok; ++i) {
+            for (int i = 0; ok; ++i) {
+            const int r = i % kTileRing;
+            if (!MbarWait(SmemAddr(&tile_empty[r]), ((uint32_t)(i / kTileRing) & 1u) ^ 1u))
+                break;
+            int t = tile_counter ? (int)atomicAdd(tile_counter, 1u)
+                                 : (int)blockIdx.x + i * (int)gridDim.x;
+            t = min(t, total_tiles);
+            tile_ring[r] = t;
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                             SmemAddr(&tile_full[r]))
+                         : "memory");
+            if (t >= total_tiles)
+                break;
             int bz, m0, n0;
-            tile_at(i, bz, m0, n0);
+            tile_at(t, bz, m0, n0);
             for (int kt = 0; kt < ktiles; ++kt) {
                 const long long g = (long long)i * ktiles + kt; // stage-ring position
                 const int s = (int)(g % kStages);
@@ -437,7 +461,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             constexpr uint32_t kIdesc = InstrDesc(kBM, kBN, false, kFmt);
             constexpr uint32_t kIdescNeg = InstrDesc(kBM, kBN, true, kFmt);
             bool ok = true;
-            for (int i = 0; i < my_tiles && ok; ++i)
+            for (int i = 0; ok; ++i) {
+            const int r = i % kTileRing;
+            if (!MbarWait(SmemAddr(&tile_full[r]), (uint32_t)(i / kTileRing) & 1u))
+                break;
+            const int t = tile_ring[r];
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                             SmemAddr(&tile_empty[r]))
+                         : "memory");
+            if (t >= total_tiles)
+                break;
             for (int kt = 0; kt < ktiles && ok; ++kt) {
                 const int chunk = kt / chunk_stages;
                 // Accumulator set: chunks alternate across tiles too.
@@ -521,6 +554,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (chunk_end)
                     MmaCommit(SmemAddr(&acc_full[buf]));
             }
+            }
         }
         __syncwarp();
     }
@@ -538,9 +572,22 @@ __global__ void __launch_bounds__(kThreads, 1)
             f2 = Pow2f(e - e / 2);
         }
         bool ok = true;
-        for (int i = 0; i < my_tiles && ok; ++i) {
+        for (int i = 0; ok; ++i) {
+        const int r = i % kTileRing;
+        ok = MbarWait(SmemAddr(&tile_full[r]), (uint32_t)(i / kTileRing) & 1u);
+        __syncwarp();
+        if (!ok)
+            break;
+        const int t = tile_ring[r];
+        __syncwarp();
+        if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                             SmemAddr(&tile_empty[r]))
+                         : "memory");
+        if (t >= total_tiles)
+            break;
         int bz, m0, n0;
-        tile_at(i, bz, m0, n0);
+        tile_at(t, bz, m0, n0);
         float acc_re[64], acc_im[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) {
@@ -694,6 +741,44 @@ int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint6
 // Persistent launch (one CTA per SM walking the tiles) or one CTA per tile
 // (jetgpu_set_tc_persistent).
 std::atomic<int> g_tc_persistent{1};
+
+// A zeroed tile counter for one persistent launch on `stream`: a slot of a
+// per-device array, reset by a memset enqueued before the launch (so a
+// captured graph resets it on every replay). Consecutive launches take
+// consecutive slots. nullptr (the static tile order) if the array cannot be
+// made.
+unsigned int *TileCounter(cudaStream_t stream)
+{
+    constexpr uint32_t kSlots = 4096;
+    static std::mutex mu;
+    static unsigned int *slots[64] = {};
+    static std::atomic<uint32_t> next[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (slots[dev] == nullptr) {
+            // Allowed even while a stream of this thread is being captured.
+            cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+            cudaThreadExchangeStreamCaptureMode(&mode);
+            void *p = nullptr;
+            const cudaError_t err = cudaMalloc(&p, kSlots * sizeof(unsigned int));
+            cudaThreadExchangeStreamCaptureMode(&mode);
+            if (err != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            slots[dev] = static_cast<unsigned int *>(p);
+        }
+    }
+    unsigned int *c = slots[dev] + next[dev].fetch_add(1u, std::memory_order_relaxed) % kSlots;
+    if (cudaMemsetAsync(c, 0, sizeof(unsigned int), stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return c;
+}
 // Tile rows per group of the tile order (jetgpu_set_tc_group_m).
 std::atomic<int> g_tc_group_m{kGroupM};
 
@@ -717,14 +802,15 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     // tile.
     const uint64_t tiles = ((n + kBN - 1) / kBN) * ((m + kBM - 1) / kBM) * batch;
     JETGPU_REQUIRE(tiles <= 0x7fffffffull, "too many tiles");
-    const unsigned grid = (unsigned)(g_tc_persistent.load(std::memory_order_relaxed)
-                                         ? std::min<uint64_t>(tiles, (uint64_t)SmCount())
-                                         : tiles);
+    const bool persistent = g_tc_persistent.load(std::memory_order_relaxed) != 0;
+    const unsigned grid =
+        (unsigned)(persistent ? std::min<uint64_t>(tiles, (uint64_t)SmCount()) : tiles);
+    unsigned int *counter = persistent && grid < tiles ? TileCounter(stream) : nullptr;
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
         a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev,
-        g_tc_group_m.load(std::memory_order_relaxed));
+        g_tc_group_m.load(std::memory_order_relaxed), counter);
     return CheckLaunch("tc_gemm_split_kernel");
 }
 

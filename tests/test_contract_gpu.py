@@ -220,12 +220,13 @@ def test_tmem_chunk_depth_controls_accumulation_error(cuda):
 def test_persistent_and_per_tile_launches_agree_bitwise(cuda, precision):
     """The persistent tensor-core launch (one CTA per SM walking the tiles)
     computes every tile exactly as the one-CTA-per-tile launch: same bits, for
-    partial edge tiles and a batch whose tiles span several rounds."""
+    partial edge tiles, a single product of fewer tiles than SMs (static
+    order) and a batch of more tiles than SMs (tiles drawn from the counter)."""
     import torch
 
     from jet_gb300 import capi
 
-    m, n, k, batch = 1000, 700, 900, 3
+    m, n, k, batch = 1100, 1900, 600, 3  # 135 tiles per product, 405 in the batch
     g = torch.Generator(device=cuda)
     g.manual_seed(precision)
     a = torch.randn(batch * m * k, dtype=torch.complex64, device=cuda, generator=g)
