@@ -49,7 +49,8 @@ extern "C" {
                                 operands, 3 products, FP32 accumulate: twice the TF32 rate,
                                 ~2^-22 truncation per product (TF32x3's) */
 #define JETGPU_PREC_TUNED 5  /* per contraction key, the fastest of FP32, TF32X3 (either main
-                                loop) and FP16X3, timed on first use (jetgpu_autotune_*);
+                                loop) and FP16X3 (either tile order), timed on first use
+                                (jetgpu_autotune_*);
                                 AUTO for small steps and for keys first met during capture */
 
 /* Complex product algorithms for the tensor-core form. */
@@ -332,14 +333,17 @@ int jetgpu_set_auto_form(int precision);
  * keeps the fastest; later ones with that key run it directly, also inside a
  * stream capture. Steps whose m n k times the batch is below `mnk` (default
  * 2^20) take AUTO's rule. jetgpu_autotune_entry reports entry `index` (in the
- * order they were made): batch, m, n, k, the chosen precision and main-loop
- * variant, and the measured ms per contraction of the candidates FP32,
- * TF32X3 (variant 0), TF32X3 (variant 1), FP16X3 (-1: not timed).
+ * order they were made): batch, m, n, k, the chosen precision, main-loop
+ * variant and tile order (group_m, 0 = the jetgpu_set_tc_group_m setting),
+ * and the measured ms per contraction of the JETGPU_AUTOTUNE_CANDIDATES
+ * candidates: FP32, TF32X3 (variant 0), TF32X3 (variant 1), FP16X3, FP16X3
+ * in row-major tile order (group_m 1); -1: not timed.
  */
+#define JETGPU_AUTOTUNE_CANDIDATES 5
 int jetgpu_set_autotune_min_work(uint64_t mnk);
 size_t jetgpu_autotune_count(void);
 int jetgpu_autotune_entry(size_t index, uint64_t *batch_m_n_k, int *precision, int *variant,
-                          float *times_ms);
+                          int *group_m, float *times_ms);
 int jetgpu_autotune_clear(void);
 
 int jetgpu_gemm_tf32x3(const float *a_planes, const float *b_planes, void *C,

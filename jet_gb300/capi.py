@@ -108,6 +108,7 @@ lib.jetgpu_autotune_count.restype = ctypes.c_size_t
 lib.jetgpu_autotune_count.argtypes = []
 lib.jetgpu_autotune_entry.argtypes = [ctypes.c_size_t, _u64p, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_float)]
 lib.jetgpu_malloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(_vp)]
 lib.jetgpu_free.argtypes = [_vp]
@@ -376,7 +377,7 @@ def max_exponent(x, stream=None, out=None):
     return e if out is not None else int(e.item())
 
 
-AUTOTUNE_CANDIDATES = ("fp32", "tf32x3", "tf32x3_wide", "fp16x3")
+AUTOTUNE_CANDIDATES = ("fp32", "tf32x3", "tf32x3_wide", "fp16x3", "fp16x3_rowmajor")
 
 
 def set_autotune_min_work(mnk: int) -> None:
@@ -395,11 +396,16 @@ def autotune_table():
     out = []
     for i in range(int(lib.jetgpu_autotune_count())):
         bmnk = (ctypes.c_uint64 * 4)()
-        prec, var = ctypes.c_int(0), ctypes.c_int(0)
-        times = (ctypes.c_float * 4)()
-        check(lib.jetgpu_autotune_entry(i, bmnk, ctypes.byref(prec), ctypes.byref(var), times))
-        choice = {PREC_FP32: "fp32", PREC_FP16X3: "fp16x3"}.get(
-            prec.value, "tf32x3_wide" if var.value == 1 else "tf32x3")
+        prec, var, grp = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        times = (ctypes.c_float * len(AUTOTUNE_CANDIDATES))()
+        check(lib.jetgpu_autotune_entry(i, bmnk, ctypes.byref(prec), ctypes.byref(var),
+                                        ctypes.byref(grp), times))
+        if prec.value == PREC_FP32:
+            choice = "fp32"
+        elif prec.value == PREC_FP16X3:
+            choice = "fp16x3_rowmajor" if grp.value == 1 else "fp16x3"
+        else:
+            choice = "tf32x3_wide" if var.value == 1 else "tf32x3"
         out.append({"batch": bmnk[0], "m": bmnk[1], "n": bmnk[2], "k": bmnk[3],
                     "choice": choice,
                     "ms": {c: (float(t) if t >= 0 else None)

@@ -3,9 +3,12 @@
 // The reference contracts every path step with one BLAS call
 // (TensorHelpers::MultiplyTensorData, TensorHelpers.hpp:128-168), so it has
 // nothing to choose. Here a step can run as the plain FP32 product or as a
-// tensor-core split product (TF32x3 with either main loop, FP16x3), all
-// within the same error bound, and which is fastest depends on the step's
-// shape, batch and operand permutations (the permute passes differ per form).
+// tensor-core split product (TF32x3 with either main loop, FP16x3 in the
+// grouped or the row-major tile order), all within the same error bound, and
+// which is fastest depends on the step's shape, batch and operand
+// permutations (the permute passes differ per form; the tile order decides
+// how the operands are shared through L2 and where in memory the tiles in
+// flight write).
 //
 // The first contraction with a given key -- device, batch, which operands are
 // batched, m, n, k, dtype, and both operands' shapes and permutations -- runs
@@ -28,18 +31,20 @@
 namespace jetgpu {
 namespace {
 
-constexpr int kCandidates = 4;
+constexpr int kCandidates = JETGPU_AUTOTUNE_CANDIDATES;
 struct Candidate {
     int precision;
-    int variant;
+    int variant; // tensor-core main loop
+    int group_m; // tile order: tile rows per group (0: the setting, 8 by default)
 };
 // Reporting order (jetgpu_autotune_entry's times).
-constexpr Candidate kCandidate[kCandidates] = {{JETGPU_PREC_FP32, -1},
-                                               {JETGPU_PREC_TF32X3, 0},
-                                               {JETGPU_PREC_TF32X3, 1},
-                                               {JETGPU_PREC_FP16X3, 0}};
+constexpr Candidate kCandidate[kCandidates] = {{JETGPU_PREC_FP32, -1, 0},
+                                               {JETGPU_PREC_TF32X3, 0, 0},
+                                               {JETGPU_PREC_TF32X3, 1, 0},
+                                               {JETGPU_PREC_FP16X3, 0, 0},
+                                               {JETGPU_PREC_FP16X3, 0, 1}};
 // Trial order: fastest expected first, so the slow forms are cut short.
-constexpr int kTrialOrder[kCandidates] = {3, 1, 2, 0};
+constexpr int kTrialOrder[kCandidates] = {3, 4, 1, 2, 0};
 
 struct Entry {
     uint64_t batch, m, n, k;
@@ -124,10 +129,10 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
         batch = 1;
         a_batched = b_batched = 0;
     }
-    auto run = [&](int precision, int variant) {
+    auto run = [&](int precision, int variant, int group_m = 0) {
         return ContractForm(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
                             b_perm, b_batched, C, m, n, k, dtype, precision, variant, scale_a,
-                            scale_b, workspace, st);
+                            scale_b, workspace, st, group_m);
     };
     if (dtype != JETGPU_C64)
         return run(JETGPU_PREC_FP32, -1);
@@ -143,7 +148,7 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
         const auto it = g_index.find(key);
         if (it != g_index.end()) {
             const Candidate c = kCandidate[g_entries[it->second].choice];
-            return run(c.precision, c.variant);
+            return run(c.precision, c.variant, c.group_m);
         }
     }
     if (Capturing(st))
@@ -152,13 +157,15 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
     Events ev;
     JETGPU_CUDA_TRY(cudaEventCreate(&ev.e0));
     JETGPU_CUDA_TRY(cudaEventCreate(&ev.e1));
-    Entry e{batch, m, n, k, -1, {-1.f, -1.f, -1.f, -1.f}};
+    Entry e{batch, m, n, k, -1, {}};
+    for (int c = 0; c < kCandidates; ++c)
+        e.ms[c] = -1.f;
     float best = FLT_MAX;
     int last = -1;
     for (int t = 0; t < kCandidates; ++t) {
         const int ci = kTrialOrder[t];
         const Candidate c = kCandidate[ci];
-        auto once = [&] { return run(c.precision, c.variant); };
+        auto once = [&] { return run(c.precision, c.variant, c.group_m); };
         float first = 0;
         int rc = Time(once, 1, st, ev.e0, ev.e1, &first);
         if (rc != JETGPU_OK) {
@@ -194,7 +201,7 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
     if (last == e.choice)
         return JETGPU_OK; // C holds the chosen form's result
     const Candidate c = kCandidate[e.choice];
-    return run(c.precision, c.variant);
+    return run(c.precision, c.variant, c.group_m);
 }
 
 } // namespace jetgpu
@@ -217,7 +224,7 @@ size_t jetgpu_autotune_count(void)
 }
 
 int jetgpu_autotune_entry(size_t index, uint64_t *batch_m_n_k, int *precision, int *variant,
-                          float *times_ms)
+                          int *group_m, float *times_ms)
 {
     ClearError();
     std::lock_guard<std::mutex> lock(g_mutex);
@@ -233,6 +240,8 @@ int jetgpu_autotune_entry(size_t index, uint64_t *batch_m_n_k, int *precision, i
         *precision = kCandidate[e.choice].precision;
     if (variant)
         *variant = kCandidate[e.choice].variant < 0 ? 0 : kCandidate[e.choice].variant;
+    if (group_m)
+        *group_m = kCandidate[e.choice].group_m;
     if (times_ms)
         for (int i = 0; i < kCandidates; ++i)
             times_ms[i] = e.ms[i];

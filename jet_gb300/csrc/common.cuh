@@ -161,12 +161,13 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 // caller, so the planes it wrote and the loop that reads them agree; -1 reads
 // the current setting.
 // For FP16, `e_max_dev` points at the two operands' max exponents (A, B) and
-// the epilogue undoes their scales.
+// the epilogue undoes their scales. `group_m`: tile rows per group of the
+// tile order (0: the jetgpu_set_tc_group_m setting).
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant = -1,
-                           const int *e_max_dev = nullptr);
+                           const int *e_max_dev = nullptr, int group_m = 0);
 
 // Workspace bytes of a (batched) contraction in `precision` (JETGPU_PREC_TUNED:
 // the largest of its candidates' and AUTO's).
@@ -177,12 +178,13 @@ size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
 
 // A checked (batched) contraction in one form: precision FP32, TF32X3,
 // BF16X3, FP16X3 or AUTO; `variant` the tensor-core main loop (-1: the
-// jetgpu_set_tc_variant setting).
+// jetgpu_set_tc_variant setting), `group_m` its tile order (0: the
+// jetgpu_set_tc_group_m setting).
 int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
-                 int scale_a, int scale_b, void *workspace, cudaStream_t st);
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m = 0);
 
 // JETGPU_PREC_TUNED: the form the autotuner measured fastest for this
 // contraction's key, timing the candidates on first use (autotune.cu).

@@ -33,6 +33,7 @@ struct SplitLayout {
     uint64_t kp;      // row pitch in words
     uint64_t word;    // bytes per word
     int b_planes;     // 4, or 6 for the N = 256 TF32 main loop
+    int group_m;      // tile order (0: the setting)
     size_t a_bytes(uint64_t rows) const { return AlignUp(4 * rows * kp * word); }
     size_t b_bytes(uint64_t rows) const { return AlignUp(b_planes * rows * kp * word); }
     // FP16: two ints (max exponents of A and B) after the planes.
@@ -51,7 +52,8 @@ std::atomic<int> g_auto_form{JETGPU_PREC_FP16X3};
 // pass costs more than the faster product saves, TF32x3 (same precision).
 constexpr double kAutoFp16MinWork = 1073741824.0; // 2^30
 
-SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1)
+SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1,
+                      int group_m = 0)
 {
     if (precision == JETGPU_PREC_AUTO) {
         precision = g_auto_form.load(std::memory_order_relaxed);
@@ -67,6 +69,7 @@ SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1)
     l.word = SplitWordBytes(l.fmt);
     l.variant = variant >= 0 ? variant : TcVariant();
     l.b_planes = (l.fmt == SplitFormat::kTf32 && l.variant == 1) ? 6 : 4;
+    l.group_m = group_m;
     return l;
 }
 
@@ -157,7 +160,7 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
                                  e_dev ? e_dev + 1 : nullptr)))
         return rc;
     return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
-                                  l.fmt, st, l.variant, e_dev);
+                                  l.fmt, st, l.variant, e_dev, l.group_m);
 }
 
 } // namespace
@@ -357,7 +360,7 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
-                 int scale_a, int scale_b, void *workspace, cudaStream_t st)
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m)
 {
     if (batch <= 1 || (!a_batched && !b_batched)) {
         batch = 1;
@@ -370,13 +373,13 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
         return ContractForm(1, A, a_rank + 1, s.data(), pm.data(), 0, B, b_rank, b_shape, b_perm,
                             0, C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
-                            workspace, st);
+                            workspace, st, group_m);
     }
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc)
-        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant), batch, A,
-                            a_rank, a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm, p.bb, C, m,
-                            n, k, dtype, scale_a, scale_b, ws, st);
+        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant, group_m),
+                            batch, A, a_rank, a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm,
+                            p.bb, C, m, n, k, dtype, scale_a, scale_b, ws, st);
     int rc;
     const size_t eb = ElemBytes(dtype);
     const void *at = A;

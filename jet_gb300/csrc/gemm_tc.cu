@@ -785,7 +785,7 @@ std::atomic<int> g_tc_group_m{kGroupM};
 template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
-             cudaStream_t stream, const int *e_max_dev = nullptr)
+             cudaStream_t stream, const int *e_max_dev = nullptr, int group_m = 0)
 {
     const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + 1024;
     static thread_local int configured_dev = -1;
@@ -810,7 +810,7 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
         a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev,
-        g_tc_group_m.load(std::memory_order_relaxed), counter);
+        group_m > 0 ? group_m : g_tc_group_m.load(std::memory_order_relaxed), counter);
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
@@ -839,7 +839,7 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream, int variant, const int *e_max_dev)
+                           cudaStream_t stream, int variant, const int *e_max_dev, int group_m)
 {
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
@@ -880,14 +880,17 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (fp16)
         return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           e_max_dev);
+                           e_max_dev, group_m);
     if (deep)
-        return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
+        return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           nullptr, group_m);
     if (bf16)
-        return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream);
-    return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream)
+        return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           nullptr, group_m);
+    return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                              nullptr, group_m)
                 : LaunchTc<0>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
-                              stream);
+                              stream, nullptr, group_m);
 }
 
 int TcVariant() { return g_tc_variant.load(std::memory_order_relaxed); }

@@ -151,4 +151,4 @@ def test_tuned_precision_accepted_and_workspace_covers_every_form():
                                   6, capi.ALGO_4M, 0, 0, None, 0, None)
     assert rc == capi.ERR_INVALID and b"bad precision" in capi.lib.jetgpu_last_error()
     assert capi.lib.jetgpu_autotune_count() == 0
-    assert capi.lib.jetgpu_autotune_entry(0, None, None, None, None) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_autotune_entry(0, None, None, None, None, None) == capi.ERR_INVALID
