@@ -42,6 +42,7 @@ constexpr int kBM = 128;
 constexpr int kBN = 128;
 constexpr int kTmemCols = 512;                // two (Cr, Ci) accumulator sets
 constexpr int kAccWarps = 8;                  // accumulator warps
+constexpr int kStoreBytes = 32 * 128;         // per accumulator warp: a 32 x 16 complex C block
 constexpr int kThreads = 32 * (2 + kAccWarps); // + TMA and MMA warps
 constexpr int kGroupM = 8;                    // default tile rows per group of the tile order
 constexpr int kTileRing = 4;                  // tile indices in flight between the warp roles
@@ -630,23 +631,49 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
         const int row = m0 + quad * 32 + lane;
-        if (ok && row < M) {
-            const int cbase = n0 + half * 64;
-            float2 *dst = C + (size_t)bz * M * N + (size_t)row * N + cbase;
-            if (cbase + 64 <= N && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+        const int cbase = n0 + half * 64;
+        float2 *Cb = C + (size_t)bz * M * N;
+        // Whole 32-row block with 16-byte aligned rows: stage each 32 x 16
+        // complex block through shared memory (16-byte chunks XOR-swizzled by
+        // row) so every warp store writes four full 128-byte row segments
+        // instead of 32 scattered 16-byte pieces, one per row.
+        const bool staged = ok && m0 + quad * 32 + 32 <= M && cbase + 64 <= N && (N & 1) == 0 &&
+                            (reinterpret_cast<uintptr_t>(Cb) & 15) == 0;
+        if (staged) {
+            float4 *buf = reinterpret_cast<float4 *>(smem + kStages * kStageBytes +
+                                                     (warp - 2) * kStoreBytes);
+            const int sub = lane >> 3; // row within a group of 4 rows
+            const int chunk = lane & 7;
+            // Row m0 + quad * 32 + sub, columns cbase + 2 chunk, + 1; 4 rows
+            // further down per step (2 N float4).
+            float4 *gp = reinterpret_cast<float4 *>(Cb + (size_t)(m0 + quad * 32 + sub) * N +
+                                                    cbase + 2 * chunk);
+            const size_t step4 = (size_t)2 * N;
 #pragma unroll
-                for (int j = 0; j < 64; j += 2) {
-                    float4 v = make_float4(acc_re[j] * scale, acc_im[j] * scale,
-                                           acc_re[j + 1] * scale, acc_im[j + 1] * scale);
-                    *reinterpret_cast<float4 *>(dst + j) = v;
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+#pragma unroll
+                for (int p = 0; p < 8; ++p)
+                    buf[lane * 8 + (p ^ (lane & 7))] =
+                        make_float4(acc_re[c0 + 2 * p] * scale, acc_im[c0 + 2 * p] * scale,
+                                    acc_re[c0 + 2 * p + 1] * scale, acc_im[c0 + 2 * p + 1] * scale);
+                __syncwarp();
+                float4 *g = gp + c0 / 2;
+#pragma unroll 1
+                for (int it = 0; it < 8; ++it) {
+                    const int r = it * 4 + sub;
+                    *g = buf[r * 8 + (chunk ^ (r & 7))];
+                    g += step4;
                 }
+                __syncwarp();
             }
-            else {
+        }
+        else if (ok && row < M) {
+            // Edge blocks (rows past M, columns past N) and unaligned rows.
+            float2 *dst = Cb + (size_t)row * N + cbase;
 #pragma unroll
-                for (int j = 0; j < 64; ++j)
-                    if (cbase + j < N)
-                        dst[j] = make_float2(acc_re[j] * scale, acc_im[j] * scale);
-            }
+            for (int j = 0; j < 64; ++j)
+                if (cbase + j < N)
+                    dst[j] = make_float2(acc_re[j] * scale, acc_im[j] * scale);
         }
         }
     }
@@ -787,7 +814,7 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
              cudaStream_t stream, const int *e_max_dev = nullptr, int group_m = 0)
 {
-    const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + 1024;
+    const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + kAccWarps * kStoreBytes + 1024;
     static thread_local int configured_dev = -1;
     int dev = 0;
     JETGPU_CUDA_TRY(cudaGetDevice(&dev));
