@@ -353,6 +353,19 @@ def run_ours(args, rank, world, local_rank):
     plain_err = rel_err_of(C2)
     del ws, C2
 
+    # The plain permute of A alone (bitperm_kernel, 2^27 complex64 elements:
+    # 1.07 GB read + 1.07 GB written), the transpose of Tensor::Transpose.
+    At = torch.empty_like(A)
+    capi.permute(A, w["a_shape"], w["a_perm"], out=At, stream=stream)
+    e0.record(stream)
+    for _ in range(5):
+        capi.permute(A, w["a_shape"], w["a_perm"], out=At, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    permute_ms = e0.elapsed_time(e1) / 5
+    permute_gbs = 16.0 * A.numel() / (permute_ms * 1e-3) / 1e9
+    del At
+
     # End to end through the public API with host buffers: every step copies
     # its A and B from pinned host memory to the device, contracts them with
     # jetgpu_contract (the headline form) and copies C back to pinned host
@@ -462,6 +475,10 @@ def run_ours(args, rank, world, local_rank):
                            "unit": "GB/s",
                            "frac": split_bytes / (split_ms * 1e-3) / 1e9 / hbm_peak,
                            "peak_source": peak_src},
+        "roofline_permute": {"bound": "hbm", "kernel": "bitperm_kernel (plain store)",
+                             "achieved": permute_gbs, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": permute_gbs / hbm_peak, "ms": permute_ms,
+                             "peak_source": peak_src},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": int(A.numel() * 8 + B.numel() * 8),
                 "d2h_bytes_per_step": int(C.numel() * 8), "ms_per_step": e2e_ms,
