@@ -230,6 +230,24 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank,
                             size_t workspace_bytes, void *stream);
 
 /*
+ * jetgpu_contract_batched (no scales) passing operand exponents between the
+ * steps of a path, so the FP16x3 form does not scan operands that an earlier
+ * product wrote. a_emax / b_emax (device ints, may be NULL): the binary
+ * exponent of the largest |re| or |im| of A / B as jetgpu_max_exponent
+ * defines it, when known; values below -1000 mean not known, and the operand
+ * is scanned. c_emax (device int, may be NULL): set, stream-ordered, to C's
+ * exponent when the product runs on the tensor cores, and to a value below
+ * -1000 otherwise. No counterpart in the reference.
+ */
+int jetgpu_contract_batched_hinted(uint64_t batch, const void *A, int a_rank,
+                                   const uint64_t *a_shape, const int32_t *a_perm, int a_batched,
+                                   const void *B, int b_rank, const uint64_t *b_shape,
+                                   const int32_t *b_perm, int b_batched, void *C, uint64_t m,
+                                   uint64_t n, uint64_t k, int dtype, int precision, int algo,
+                                   const int *a_emax, const int *b_emax, int *c_emax,
+                                   void *workspace, size_t workspace_bytes, void *stream);
+
+/*
  * jetgpu_contract without a workspace argument and without allocating: for
  * callers that cannot allocate device memory when they contract -- inside a
  * CUDA stream capture, where cudaMalloc is illegal; under a host's own fixed

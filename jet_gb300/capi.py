@@ -93,6 +93,10 @@ lib.jetgpu_contract_batched.argtypes = [
     ctypes.c_uint64, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp, ctypes.c_int, _u64p,
     _i32p, ctypes.c_int, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_size_t, _vp]
+lib.jetgpu_contract_batched_hinted.argtypes = [
+    ctypes.c_uint64, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp, ctypes.c_int, _u64p,
+    _i32p, ctypes.c_int, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+    ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]
 lib.jetgpu_add.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
 lib.jetgpu_conj.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
 lib.jetgpu_slice_sum_f64.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _vp,
@@ -242,6 +246,31 @@ def contract_batched(batch, a, a_shape, a_perm, a_batched, b, b_shape, b_perm, b
                                       i32(b_perm), int(b_batched), _ptr(out), m, n, k, dc,
                                       precision, ALGO_4M, 0, 0, _ptr(workspace), ws_bytes,
                                       _stream(stream)))
+    return out
+
+
+def contract_batched_hinted(batch, a, a_shape, a_perm, a_batched, b, b_shape, b_perm, b_batched,
+                            m, n, k, precision=PREC_FP32, a_emax=None, b_emax=None, c_emax=None,
+                            out=None, workspace=None, stream=None):
+    """contract_batched passing max-exponent hints (device int32 tensors of one
+    element, or None): a_emax / b_emax known exponents of the operands,
+    c_emax receives C's when the product runs on the tensor cores."""
+    import torch
+
+    dc = dtype_code(a.dtype)
+    if out is None:
+        out = torch.empty(max(batch * m * n, 1), dtype=a.dtype, device=a.device)
+    need = int(lib.jetgpu_contract_batched_workspace_size(
+        batch, len(a_shape), u64(a_shape), i32(a_perm), int(a_batched), len(b_shape),
+        u64(b_shape), i32(b_perm), int(b_batched), m, n, k, dc, precision))
+    if workspace is None and need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=a.device)
+    ws_bytes = 0 if workspace is None else workspace.numel() * workspace.element_size()
+    check(lib.jetgpu_contract_batched_hinted(
+        batch, _ptr(a), len(a_shape), u64(a_shape), i32(a_perm), int(a_batched), _ptr(b),
+        len(b_shape), u64(b_shape), i32(b_perm), int(b_batched), _ptr(out), m, n, k, dc,
+        precision, ALGO_4M, _ptr(a_emax), _ptr(b_emax), _ptr(c_emax), _ptr(workspace), ws_bytes,
+        _stream(stream)))
     return out
 
 

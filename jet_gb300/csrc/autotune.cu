@@ -123,16 +123,26 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
                   const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                   const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                   uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a, int scale_b,
-                  void *workspace, cudaStream_t st)
+                  void *workspace, cudaStream_t st, const ExpHints *hints)
 {
     if (batch <= 1 || (!a_batched && !b_batched)) {
         batch = 1;
         a_batched = b_batched = 0;
     }
-    auto run = [&](int precision, int variant, int group_m = 0) {
+    // Trials read the operand hints but record no exponent of C: only the
+    // run whose result is kept does.
+    ExpHints trial;
+    if (hints != nullptr) {
+        trial.a = hints->a;
+        trial.b = hints->b;
+    }
+    auto run_with = [&](int precision, int variant, int group_m, const ExpHints *h) {
         return ContractForm(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
                             b_perm, b_batched, C, m, n, k, dtype, precision, variant, scale_a,
-                            scale_b, workspace, st, group_m);
+                            scale_b, workspace, st, group_m, h);
+    };
+    auto run = [&](int precision, int variant, int group_m = 0) {
+        return run_with(precision, variant, group_m, hints);
     };
     if (dtype != JETGPU_C64)
         return run(JETGPU_PREC_FP32, -1);
@@ -165,7 +175,7 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
     for (int t = 0; t < kCandidates; ++t) {
         const int ci = kTrialOrder[t];
         const Candidate c = kCandidate[ci];
-        auto once = [&] { return run(c.precision, c.variant, c.group_m); };
+        auto once = [&] { return run_with(c.precision, c.variant, c.group_m, &trial); };
         float first = 0;
         int rc = Time(once, 1, st, ev.e0, ev.e1, &first);
         if (rc != JETGPU_OK) {
@@ -198,7 +208,7 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
         }
     }
     ClearError();
-    if (last == e.choice)
+    if (last == e.choice && (hints == nullptr || hints->c == nullptr))
         return JETGPU_OK; // C holds the chosen form's result
     const Candidate c = kCandidate[e.choice];
     return run(c.precision, c.variant, c.group_m);

@@ -137,8 +137,16 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
 int MaxExponent(const void *x, uint64_t size, int dtype, int *e_dev, cudaStream_t stream);
 
 // Max exponents of two operands into e[0], e[1] in one fill and one launch.
+// hint0 / hint1 (device ints, may be null): an operand whose hint holds an
+// exponent (>= kExpZero, recorded by the kernel that wrote the operand) is
+// not read.
 int MaxExponent2(const void *x0, uint64_t n0, const void *x1, uint64_t n1, int dtype, int *e,
-                 cudaStream_t stream, int operands = 2);
+                 cudaStream_t stream, int operands = 2, const int *hint0 = nullptr,
+                 const int *hint1 = nullptr);
+
+// Max exponent of an all-zero operand; smaller values (the 0x80 byte fill)
+// mean "no exponent recorded".
+constexpr int kExpZero = -1000;
 
 // C[b] = A[b] B[b] for b < batch (strides sa, sb in elements; 0 = shared
 // operand), C packed as batch x m x n. Vector-shaped products split over k
@@ -167,7 +175,8 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant = -1,
-                           const int *e_max_dev = nullptr, int group_m = 0);
+                           const int *e_max_dev = nullptr, int group_m = 0,
+                           int *out_emax = nullptr);
 
 // Workspace bytes of a (batched) contraction in `precision` (JETGPU_PREC_TUNED:
 // the largest of its candidates' and AUTO's).
@@ -175,6 +184,17 @@ size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
                          const int32_t *a_perm, int a_batched, int b_rank,
                          const uint64_t *b_shape, const int32_t *b_perm, int b_batched, uint64_t m,
                          uint64_t n, uint64_t k, int dtype, int precision);
+
+// Max-exponent hints of one contraction (device ints; each may be null):
+// `a` / `b` hold the operands' exponents when the kernels that wrote them
+// recorded them (values below kExpZero: not recorded), so the FP16 form need
+// not scan them; `c` receives C's when the product runs on the tensor cores
+// and is left unrecorded otherwise.
+struct ExpHints {
+    const int *a = nullptr;
+    const int *b = nullptr;
+    int *c = nullptr;
+};
 
 // A checked (batched) contraction in one form: precision FP32, TF32X3,
 // BF16X3, FP16X3 or AUTO; `variant` the tensor-core main loop (-1: the
@@ -184,7 +204,8 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
-                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m = 0);
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m = 0,
+                 const ExpHints *hints = nullptr);
 
 // JETGPU_PREC_TUNED: the form the autotuner measured fastest for this
 // contraction's key, timing the candidates on first use (autotune.cu).
@@ -192,7 +213,7 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
                   const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                   const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                   uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a, int scale_b,
-                  void *workspace, cudaStream_t st);
+                  void *workspace, cudaStream_t st, const ExpHints *hints = nullptr);
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,

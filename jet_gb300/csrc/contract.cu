@@ -129,7 +129,7 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
                  const uint64_t *a_shape, const int32_t *a_perm, uint64_t ba, const void *B,
                  int b_rank, const uint64_t *b_shape, const int32_t *b_perm, uint64_t bb,
                  void *C, uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a,
-                 int scale_b, uint8_t *ws, cudaStream_t st)
+                 int scale_b, uint8_t *ws, cudaStream_t st, const ExpHints *hints)
 {
     int rc;
     uint8_t *pa = ws;
@@ -142,7 +142,8 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
         JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
                        "scale_a + scale_b out of range for FP16x3");
         e_dev = reinterpret_cast<int *>(pb + AlignUp((size_t)l.b_planes * bb * n * l.kp * l.word));
-        if ((rc = MaxExponent2(A, ba * m * k, B, bb * k * n, dtype, e_dev, st)))
+        if ((rc = MaxExponent2(A, ba * m * k, B, bb * k * n, dtype, e_dev, st, 2,
+                               hints ? hints->a : nullptr, hints ? hints->b : nullptr)))
             return rc;
         out_scale = Pow2f(scale_a + scale_b);
         scale_a = scale_b = 0;
@@ -160,7 +161,8 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
                                  e_dev ? e_dev + 1 : nullptr)))
         return rc;
     return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
-                                  l.fmt, st, l.variant, e_dev, l.group_m);
+                                  l.fmt, st, l.variant, e_dev, l.group_m,
+                                  hints ? hints->c : nullptr);
 }
 
 } // namespace
@@ -360,7 +362,8 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                  const int32_t *a_perm, int a_batched, const void *B, int b_rank,
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
-                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m)
+                 int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m,
+                 const ExpHints *hints)
 {
     if (batch <= 1 || (!a_batched && !b_batched)) {
         batch = 1;
@@ -373,13 +376,13 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
         return ContractForm(1, A, a_rank + 1, s.data(), pm.data(), 0, B, b_rank, b_shape, b_perm,
                             0, C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
-                            workspace, st, group_m);
+                            workspace, st, group_m, hints);
     }
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc)
         return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant, group_m),
                             batch, A, a_rank, a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm,
-                            p.bb, C, m, n, k, dtype, scale_a, scale_b, ws, st);
+                            p.bb, C, m, n, k, dtype, scale_a, scale_b, ws, st, hints);
     int rc;
     const size_t eb = ElemBytes(dtype);
     const void *at = A;
@@ -447,21 +450,26 @@ int Contract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
              const int32_t *a_perm, int a_batched, const void *B, int b_rank,
              const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C, uint64_t m,
              uint64_t n, uint64_t k, int dtype, int precision, int algo, int scale_a, int scale_b,
-             void *workspace, size_t workspace_bytes, cudaStream_t st)
+             void *workspace, size_t workspace_bytes, cudaStream_t st,
+             const ExpHints *hints = nullptr)
 {
     bool empty = false;
     int rc = CheckContract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
                            b_perm, b_batched, C, m, n, k, dtype, precision, algo, workspace,
                            workspace_bytes, &empty);
-    if (rc || empty)
+    if (rc)
         return rc;
+    if (hints != nullptr && hints->c != nullptr) // unrecorded until a product records it
+        JETGPU_CUDA_TRY(cudaMemsetAsync(hints->c, 0x80, sizeof(int), st));
+    if (empty)
+        return JETGPU_OK;
     if (precision == JETGPU_PREC_TUNED)
         return ContractTuned(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
                              b_perm, b_batched, C, m, n, k, dtype, scale_a, scale_b, workspace,
-                             st);
+                             st, hints);
     return ContractForm(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
                         b_batched, C, m, n, k, dtype, precision, -1, scale_a, scale_b, workspace,
-                        st);
+                        st, 0, hints);
 }
 
 } // namespace
@@ -518,6 +526,28 @@ int jetgpu_contract_batched(uint64_t batch, const void *A, int a_rank, const uin
     return Contract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
                     b_batched, C, m, n, k, dtype, precision, algo, scale_a, scale_b, workspace,
                     workspace_bytes, AsStream(stream));
+}
+
+int jetgpu_contract_batched_hinted(uint64_t batch, const void *A, int a_rank,
+                                   const uint64_t *a_shape, const int32_t *a_perm, int a_batched,
+                                   const void *B, int b_rank, const uint64_t *b_shape,
+                                   const int32_t *b_perm, int b_batched, void *C, uint64_t m,
+                                   uint64_t n, uint64_t k, int dtype, int precision, int algo,
+                                   const int *a_emax, const int *b_emax, int *c_emax,
+                                   void *workspace, size_t workspace_bytes, void *stream)
+{
+    NvtxRange range("jetgpu_contract_batched_hinted");
+    ClearError();
+    JETGPU_REQUIRE(batch >= 1, "batch must be at least 1");
+    JETGPU_REQUIRE(batch == 1 || a_batched || b_batched,
+                   "a batch needs at least one batched operand");
+    ExpHints hints;
+    hints.a = a_emax;
+    hints.b = b_emax;
+    hints.c = c_emax;
+    return Contract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
+                    b_batched, C, m, n, k, dtype, precision, algo, 0, 0, workspace,
+                    workspace_bytes, AsStream(stream), &hints);
 }
 
 } // extern "C"

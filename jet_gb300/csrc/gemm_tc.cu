@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                           float2 *__restrict__ C, int M, int N, int ktiles, int batch,
                           float scale, int a_batched, int b_batched, int chunk_stages,
                           const int *__restrict__ scale_exps, int group_m,
-                          unsigned int *__restrict__ tile_counter)
+                          unsigned int *__restrict__ tile_counter, int *__restrict__ out_emax)
 {
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
@@ -630,6 +630,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                 acc_im[j] = acc_im[j] * f1 * f2;
             }
         }
+        if (out_emax != nullptr && ok) {
+            // Binary exponent of the largest |re| or |im| written (as the
+            // max-exponent pass defines it); accumulators outside C hold 0.
+            uint32_t best = 0;
+#pragma unroll
+            for (int j = 0; j < 64; ++j)
+                best = max(best, max(__float_as_uint(acc_re[j] * scale) & 0x7fffffffu,
+                                     __float_as_uint(acc_im[j] * scale) & 0x7fffffffu));
+            const int biased = (int)(best >> 23);
+            int ex = best == 0 ? kExpZero : (biased == 0 ? -127 : biased - 127);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, o));
+            if (lane == 0)
+                atomicMax(out_emax, ex);
+        }
         const int row = m0 + quad * 32 + lane;
         const int cbase = n0 + half * 64;
         float2 *Cb = C + (size_t)bz * M * N;
@@ -812,7 +828,8 @@ std::atomic<int> g_tc_group_m{kGroupM};
 template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
-             cudaStream_t stream, const int *e_max_dev = nullptr, int group_m = 0)
+             cudaStream_t stream, const int *e_max_dev = nullptr, int group_m = 0,
+             int *out_emax = nullptr)
 {
     const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + kAccWarps * kStoreBytes + 1024;
     static thread_local int configured_dev = -1;
@@ -837,7 +854,7 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
         a_batched, b_batched, ChunkStages(TcCfg<V>::Fmt, BlockK<V>()), e_max_dev,
-        group_m > 0 ? group_m : g_tc_group_m.load(std::memory_order_relaxed), counter);
+        group_m > 0 ? group_m : g_tc_group_m.load(std::memory_order_relaxed), counter, out_emax);
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
@@ -866,7 +883,8 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
-                           cudaStream_t stream, int variant, const int *e_max_dev, int group_m)
+                           cudaStream_t stream, int variant, const int *e_max_dev, int group_m,
+                           int *out_emax)
 {
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
@@ -907,17 +925,17 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (fp16)
         return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           e_max_dev, group_m);
+                           e_max_dev, group_m, out_emax);
     if (deep)
         return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           nullptr, group_m);
+                           nullptr, group_m, out_emax);
     if (bf16)
         return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           nullptr, group_m);
+                           nullptr, group_m, out_emax);
     return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                              nullptr, group_m)
+                              nullptr, group_m, out_emax)
                 : LaunchTc<0>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
-                              stream, nullptr, group_m);
+                              stream, nullptr, group_m, out_emax);
 }
 
 int TcVariant() { return g_tc_variant.load(std::memory_order_relaxed); }

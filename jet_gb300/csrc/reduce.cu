@@ -124,19 +124,31 @@ __global__ void slice_gather_kernel(const __grid_constant__ SliceParams p,
     }
 }
 
-__global__ void init_exp_kernel(int *e) { *e = -1000; }
+__global__ void init_exp_kernel(int *e) { *e = kExpZero; }
 
 __global__ void counter_add_kernel(uint64_t *c, uint64_t delta) { *c += delta; }
 
 // Max exponent of operand blockIdx.y (x0 or x1) into e[blockIdx.y]; e must
 // start below -1000 (the 0x80 byte fill), so all-zero operands give -1000.
+// An operand whose hint (h0 / h1, may be null) already holds its exponent
+// (>= -1000: recorded by the kernel that produced it) is not read: its hint
+// is copied.
 template <typename V, typename U>
 __global__ void max_exp_kernel(const V *__restrict__ x0, uint64_t n0, const V *__restrict__ x1,
-                               uint64_t n1, int *e)
+                               uint64_t n1, int *e, const int *h0, const int *h1)
 {
     const V *__restrict__ x = blockIdx.y ? x1 : x0;
     const uint64_t n = blockIdx.y ? n1 : n0;
+    const int *h = blockIdx.y ? h1 : h0;
     e += blockIdx.y;
+    if (h != nullptr) {
+        const int known = *h;
+        if (known >= kExpZero) {
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                atomicMax(e, known);
+            return;
+        }
+    }
     U best = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -158,7 +170,7 @@ __global__ void max_exp_kernel(const V *__restrict__ x0, uint64_t n0, const V *_
     // non-negative floats order like the values).
     int ex;
     if (best == 0) {
-        ex = -1000;
+        ex = kExpZero;
     }
     else if constexpr (sizeof(U) == 4) {
         const int biased = (int)((best >> 23) & 0xff);
@@ -357,7 +369,7 @@ int MaxExponent(const void *x, uint64_t size, int dtype, int *exp_dev, cudaStrea
 // launch; `operands` = 1 computes e[0] only. Empty operands leave their word
 // at the fill value (below any exponent).
 int MaxExponent2(const void *x0, uint64_t n0, const void *x1, uint64_t n1, int dtype, int *e,
-                 cudaStream_t st, int operands)
+                 cudaStream_t st, int operands, const int *hint0, const int *hint1)
 {
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     JETGPU_REQUIRE(e != nullptr, "null exponent pointer");
@@ -367,10 +379,10 @@ int MaxExponent2(const void *x0, uint64_t n0, const void *x1, uint64_t n1, int d
     const dim3 grid(GridFor((n + kThreads - 1) / kThreads, 8), (unsigned)operands);
     if (dtype == JETGPU_C64)
         max_exp_kernel<float2, uint32_t><<<grid, kThreads, 0, st>>>(
-            (const float2 *)x0, n0, (const float2 *)x1, n1, e);
+            (const float2 *)x0, n0, (const float2 *)x1, n1, e, hint0, hint1);
     else
         max_exp_kernel<double2, unsigned long long><<<grid, kThreads, 0, st>>>(
-            (const double2 *)x0, n0, (const double2 *)x1, n1, e);
+            (const double2 *)x0, n0, (const double2 *)x1, n1, e, hint0, hint1);
     return CheckLaunch("max_exp_kernel");
 }
 

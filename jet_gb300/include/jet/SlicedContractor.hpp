@@ -104,6 +104,15 @@ template <class T = std::complex<float>> class SlicedContractor {
     }
 
     size_t GetBatchSize() const { return batch_; }
+
+    // Pass each step's recorded output exponent to the steps consuming it, so
+    // the FP16x3 form skips its scan of tensor-core outputs (default on; the
+    // results are the same either way).
+    void SetExponentHints(bool on)
+    {
+        exponent_hints_ = on;
+        ReleaseGraph();
+    }
     size_t GetNumSlices() const { return num_slices_; }
 
     // Sum over slices [first, first + count) of the network's result, in FP64.
@@ -263,6 +272,10 @@ template <class T = std::complex<float>> class SlicedContractor {
     std::vector<char> persist_;
     std::vector<int> prefix_last_use_;
     Gpu::DeviceBuffer arena_, ws_, tmp_a_, tmp_b_, acc_, counter_, final_tmp_;
+    // One int per node: the max exponent its producing step recorded
+    // (jetgpu_contract_batched_hinted), read by the steps consuming it.
+    Gpu::DeviceBuffer emax_;
+    bool exponent_hints_ = true;
     std::vector<Gpu::DeviceBuffer> alt_bufs_;
     void *graph_ = nullptr;
 
@@ -519,6 +532,16 @@ template <class T = std::complex<float>> class SlicedContractor {
         tmp_b_ = Gpu::DeviceBuffer(tmp_bytes_);
         acc_ = Gpu::DeviceBuffer(std::max<size_t>(result_size_ * 16, 16));
         counter_ = Gpu::DeviceBuffer(8);
+        emax_ = Gpu::DeviceBuffer(std::max<size_t>(nodes_.size(), 1) * sizeof(int));
+        {
+            // Nothing recorded yet (any value below -1000).
+            const std::vector<int> unknown(std::max<size_t>(nodes_.size(), 1),
+                                           std::numeric_limits<int>::min());
+            Gpu::Check(jetgpu_memcpy(emax_.get(), unknown.data(), unknown.size() * sizeof(int),
+                                     0, Gpu::Stream()),
+                       "exponent slots");
+            Gpu::Synchronize();
+        }
         final_tmp_ = Gpu::DeviceBuffer(final_perm_needed_ ? nodes_[final_id_].bytes : 0);
         // Slice-independent tensors that the captured graph reads (leaves,
         // prefix outputs consumed by "$s" steps, the final result) keep one
@@ -601,11 +624,17 @@ template <class T = std::complex<float>> class SlicedContractor {
         // Steps that run once gain nothing from tuning: AUTO's rule.
         const int prec =
             (!s.chunk && precision_ == JETGPU_PREC_TUNED) ? JETGPU_PREC_AUTO : precision_;
-        Gpu::Check(jetgpu_contract_batched(
+        // Intermediates carry the max exponent their producing step recorded
+        // (a reorder keeps the values); leaves are scanned when needed.
+        int *emax = static_cast<int *>(emax_.get());
+        const bool hints = exponent_hints_ && emax != nullptr;
+        Gpu::Check(jetgpu_contract_batched_hinted(
                        s.batch, a, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(),
                        s.batched, b, (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(),
                        s.batched, Buffer(s.out), s.m, s.n, s.k, dt, prec, JETGPU_ALGO_4M,
-                       0, 0, ws_.get(), ws_.size(), st),
+                       hints && s.a >= (int)num_leaves_ ? emax + s.a : nullptr,
+                       hints && s.b >= (int)num_leaves_ ? emax + s.b : nullptr,
+                       hints ? emax + s.out : nullptr, ws_.get(), ws_.size(), st),
                    "batched contraction");
         if (prof)
             prof->Mark("contract", idx, s.batch, s.m, s.n, s.k);

@@ -260,3 +260,33 @@ def test_auto_form_knob(cuda):
                               run(capi.PREC_TF32X3, *small, *ops[small]))
     finally:
         capi.set_auto_form(capi.PREC_FP16X3)
+
+
+@pytest.mark.parametrize("producer", [1, 3, 4, 5])
+def test_exponent_hints_pass_between_steps(cuda, producer):
+    """A tensor-core product records its output's max exponent (the value the
+    scan would find); FP16x3 with that hint gives the same bits as with the
+    scan; plain products record nothing (the consumer then scans)."""
+    import torch
+
+    from jet_gb300 import capi
+
+    g = torch.Generator(device=cuda)
+    g.manual_seed(producer)
+    m, k, n, n2 = 384, 256, 320, 200
+    a = torch.randn(m * k, dtype=torch.complex64, device=cuda, generator=g) * 2.0**-30
+    b = torch.randn(k * n, dtype=torch.complex64, device=cuda, generator=g)
+    x = torch.randn(n * n2, dtype=torch.complex64, device=cuda, generator=g) * 2.0**20
+    e = torch.empty(1, dtype=torch.int32, device=cuda)
+    c = capi.contract_batched_hinted(1, a, [m, k], [0, 1], 0, b, [k, n], [0, 1], 0, m, n, k,
+                                     precision=producer, c_emax=e)
+    assert int(e.item()) == capi.max_exponent(c[: m * n])
+    d_scan = capi.contract(c, [m, n], [0, 1], x, [n, n2], [0, 1], m, n2, n,
+                           precision=capi.PREC_FP16X3)
+    d_hint = capi.contract_batched_hinted(1, c, [m, n], [0, 1], 0, x, [n, n2], [0, 1], 0, m, n2,
+                                          n, precision=capi.PREC_FP16X3, a_emax=e)
+    assert torch.equal(d_scan.view(torch.int64), d_hint.view(torch.int64))
+    capi.contract_batched_hinted(1, a, [m, k], [0, 1], 0, b, [k, n], [0, 1], 0, m, n, k,
+                                 precision=capi.PREC_FP32, c_emax=e)
+    assert int(e.item()) < -1000
+    assert capi.take_device_status() == 0

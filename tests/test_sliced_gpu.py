@@ -222,3 +222,26 @@ def test_profile_chunk_times_every_launch(jet):
     with pytest.raises(Exception, match="multiple of the batch size"):
         sc.profile_chunk(2)
     assert sc.contract()[0] == want
+
+
+@pytest.mark.parametrize("precision", [2, 4])
+def test_exponent_hints_do_not_change_the_amplitude(jet, precision):
+    """Passing recorded exponents between the steps (default) skips scans but
+    gives the same bits as scanning every FP16x3 operand."""
+    from jet_gb300 import circuits
+
+    net = circuits.random_circuit_network(5, 6, 10, seed=3)
+    best = None
+    for s in range(4):
+        p = circuits.greedy_path(net, seed=s, score="gain")
+        f, _ = circuits.path_cost(net, p)
+        if best is None or f < best[0]:
+            best = (f, p)
+    path = best[1]
+    sliced = circuits.choose_slices(net, path, 2)
+    sc = jet.SlicedContractorC64(_tn(jet, net, "complex64"), path, sliced, precision)
+    sc.set_batch_size(2)
+    with_hints = sc.contract()
+    sc.set_exponent_hints(False)
+    scanned = sc.contract()
+    assert with_hints == scanned
