@@ -280,7 +280,11 @@ def test_exponent_hints_pass_between_steps(cuda, producer):
     e = torch.empty(1, dtype=torch.int32, device=cuda)
     c = capi.contract_batched_hinted(1, a, [m, k], [0, 1], 0, b, [k, n], [0, 1], 0, m, n, k,
                                      precision=producer, c_emax=e)
-    assert int(e.item()) == capi.max_exponent(c[: m * n])
+    recorded = int(e.item())
+    if producer == capi.PREC_TUNED:  # the tuner may pick the plain form
+        assert recorded == capi.max_exponent(c[: m * n]) or recorded < -1000
+    else:
+        assert recorded == capi.max_exponent(c[: m * n])
     d_scan = capi.contract(c, [m, n], [0, 1], x, [n, n2], [0, 1], m, n2, n,
                            precision=capi.PREC_FP16X3)
     d_hint = capi.contract_batched_hinted(1, c, [m, n], [0, 1], 0, x, [n, n2], [0, 1], 0, m, n2,
