@@ -7,7 +7,9 @@
 //  * gemm_kernel: 128x64 (complex64) / 64x64 (complex128) CTA tiles, 8-deep
 //    k slices staged in shared memory with register double buffering, each
 //    thread accumulating an 8x4 (4x4) block of complex outputs with 4 FMAs
-//    per complex multiply-add.
+//    per complex multiply-add. Products whose tiles would leave SMs idle
+//    split k into partial sums in the workspace (GemmSplits), reduced in a
+//    fixed order.
 //  * gemv_rows_kernel (n == 1) / gemv_cols_kernel (m == 1, also DOTU): split
 //    over k into partial sums, reduced in a fixed order by reduce_partials
 //    (deterministic).
@@ -41,14 +43,25 @@ __global__ void __launch_bounds__(256)
     gemm_kernel(const typename C2<T>::type *__restrict__ A,
                 const typename C2<T>::type *__restrict__ B,
                 typename C2<T>::type *__restrict__ C, int64_t M, int64_t N,
-                int64_t K, T scale, int64_t sa, int64_t sb)
+                int64_t K, T scale, int64_t sa, int64_t sb, int splits, int64_t kchunk)
 {
     using V = typename C2<T>::type;
     constexpr int TM = GemmCfg<T>::TM;
-    // Batch b = blockIdx.z: operand strides sa, sb (0 = shared), C packed.
-    A += (int64_t)blockIdx.z * sa;
-    B += (int64_t)blockIdx.z * sb;
-    C += (int64_t)blockIdx.z * M * N;
+    // blockIdx.z = b * splits + s: batch b (operand strides sa, sb, 0 =
+    // shared; C packed) and k range s (splits > 1: [s kchunk, (s + 1)
+    // kchunk), partial sums to C + (s * batch + b) * M * N, reduced later).
+    const int64_t s = (int64_t)blockIdx.z % splits;
+    const int64_t bz = (int64_t)blockIdx.z / splits;
+    const int64_t batch = (int64_t)gridDim.z / splits;
+    A += bz * sa;
+    B += bz * sb;
+    C += (s * batch + bz) * M * N;
+    const int64_t lda = K; // A's row length
+    const int64_t k_begin = s * kchunk;
+    const int64_t k_end = min(K, k_begin + kchunk);
+    A += k_begin;
+    B += k_begin * N;
+    K = k_end > k_begin ? k_end - k_begin : 0; // this split's k range
     constexpr int BM = TM * kTY;
     constexpr int BN = kTN * kTX;
     constexpr int A_PER = BM * kBK / 256; // A elements loaded per thread
@@ -76,7 +89,7 @@ __global__ void __launch_bounds__(256)
             int row = tid / kBK + q * (256 / kBK);
             int col = tid % kBK;
             int64_t gm = m0 + row, gk = k0 + col;
-            ra[q] = (gm < M && gk < K) ? A[gm * K + gk] : V{0, 0};
+            ra[q] = (gm < M && gk < K) ? A[gm * lda + gk] : V{0, 0};
         }
 #pragma unroll
         for (int q = 0; q < B_PER; ++q) {
@@ -295,13 +308,36 @@ __global__ void fill_zero(typename C2<T>::type *out, int64_t len)
         out[i] = V{0, 0};
 }
 
+// Split-k factor of the matrix product when its tiles (times the batch) do
+// not fill the GPU: up to two CTAs per SM, at least 256 k per split, and at
+// most 32 MiB of partial sums (out_bytes: the bytes of C).
+int64_t GemmSplits(int64_t ctas, int64_t batch, int64_t K, int64_t out_bytes)
+{
+    const int64_t target = (int64_t)SmCount() * 2;
+    if (ctas >= target / 2 || K < 512)
+        return 1;
+    int64_t s = (target + ctas - 1) / ctas;
+    s = min(s, K / 256);
+    s = min(s, (int64_t)65535 / (batch > 0 ? batch : 1));
+    s = min(s, (int64_t)(32ll << 20) / (out_bytes > 0 ? out_bytes : 1));
+    return s < 2 ? 1 : s;
+}
+
+template <typename T> inline void GemmGrid(int64_t M, int64_t N, int64_t &tiles_n, int64_t &tiles_m)
+{
+    constexpr int BM = GemmCfg<T>::TM * kTY;
+    constexpr int BN = kTN * kTX;
+    tiles_n = (N + BN - 1) / BN;
+    tiles_m = (M + BM - 1) / BM;
+}
+
 // Split-k factor for the vector kernels: enough CTAs to fill the GPU, with at
-// least 4096 k per chunk.
+// least 1024 k per chunk.
 int64_t SplitK(int64_t blocks_per_split, int64_t K)
 {
     int64_t target = (int64_t)SmCount() * 4;
     int64_t s = blocks_per_split >= target ? 1 : target / blocks_per_split;
-    int64_t max_s = (K + 4095) / 4096;
+    int64_t max_s = (K + 1023) / 1024;
     if (s > max_s)
         s = max_s;
     return s < 1 ? 1 : s;
@@ -337,8 +373,15 @@ template <typename T>
 size_t VectorWorkspace(int64_t batch, int64_t m, int64_t n, int64_t k)
 {
     using V = typename C2<T>::type;
-    if ((m > 1 && n > 1) || batch < 1)
+    if (batch < 1)
         return 0;
+    if (m > 1 && n > 1) {
+        // Matrix products: partial sums of the k splits (GemmSplits).
+        int64_t tn, tm;
+        GemmGrid<T>(m, n, tn, tm);
+        const int64_t S = GemmSplits(tn * tm * batch, batch, k, batch * m * n * (int64_t)sizeof(V));
+        return S > 1 ? (size_t)(S * batch * m * n) * sizeof(V) : 0;
+    }
     int64_t blocks, len;
     int per_cta;
     VectorShape(m, n, blocks, per_cta, len);
@@ -380,6 +423,35 @@ int MultiplyVectorT(const typename C2<T>::type *A, const typename C2<T>::type *B
     return CheckLaunch("reduce_partials");
 }
 
+// Matrix product of `batch` pairs (strides sa, sb; 0 = shared), split over k
+// into the workspace when the tiles alone would leave SMs idle and the caller
+// supplied room for the partial sums (reduced in a fixed order).
+template <typename T>
+int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename C2<T>::type *C,
+          int64_t batch, int64_t sa, int64_t sb, int64_t M, int64_t N, int64_t K, T scale,
+          void *ws, size_t ws_bytes, cudaStream_t stream)
+{
+    using V = typename C2<T>::type;
+    int64_t tn, tm;
+    GemmGrid<T>(M, N, tn, tm);
+    const size_t need = VectorWorkspace<T>(batch, M, N, K);
+    const int64_t S =
+        (need > 0 && ws != nullptr && ws_bytes >= need)
+            ? GemmSplits(tn * tm * batch, batch, K, batch * M * N * (int64_t)sizeof(V))
+            : 1;
+    const int64_t kchunk = (K + S - 1) / S;
+    const dim3 grid((unsigned)tn, (unsigned)tm, (unsigned)(batch * S));
+    JETGPU_REQUIRE(tm <= 65535 && batch * S <= 65535, "product too large for one launch");
+    V *dst = S > 1 ? (V *)ws : C;
+    gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa, sb, (int)S, kchunk);
+    int rc = CheckLaunch("gemm_kernel");
+    if (rc || S == 1)
+        return rc;
+    reduce_partials<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(
+        dst, C, batch * M * N, S);
+    return CheckLaunch("reduce_partials");
+}
+
 template <typename T>
 int MultiplyT(const void *Av, const void *Bv, void *Cv, int64_t M, int64_t N,
               int64_t K, int scale_exp, void *ws, size_t ws_bytes,
@@ -397,14 +469,8 @@ int MultiplyT(const void *Av, const void *Bv, void *Cv, int64_t M, int64_t N,
             C, M * N);
         return CheckLaunch("fill_zero");
     }
-    if (M > 1 && N > 1) {
-        constexpr int BM = GemmCfg<T>::TM * kTY;
-        constexpr int BN = kTN * kTX;
-        dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
-        JETGPU_REQUIRE(grid.y <= 65535u, "m too large for one launch");
-        gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, 0, 0);
-        return CheckLaunch("gemm_kernel");
-    }
+    if (M > 1 && N > 1)
+        return GemmT<T>(A, B, C, 1, 0, 0, M, N, K, scale, ws, ws_bytes, stream);
     return MultiplyVectorT<T>(A, B, C, 1, 0, 0, M, N, K, scale, ws, ws_bytes, stream);
 }
 
@@ -424,14 +490,8 @@ int MultiplyBatchedT(const void *Av, const void *Bv, void *Cv, int64_t batch, in
         fill_zero<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(C, batch * M * N);
         return CheckLaunch("fill_zero");
     }
-    if (M > 1 && N > 1) {
-        constexpr int BM = GemmCfg<T>::TM * kTY;
-        constexpr int BN = kTN * kTX;
-        dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
-        JETGPU_REQUIRE(grid.y <= 65535u && grid.z <= 65535u, "batched product too large");
-        gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, scale, sa, sb);
-        return CheckLaunch("gemm_kernel (batched)");
-    }
+    if (M > 1 && N > 1)
+        return GemmT<T>(A, B, C, batch, sa, sb, M, N, K, scale, ws, ws_bytes, stream);
     return MultiplyVectorT<T>(A, B, C, batch, sa, sb, M, N, K, scale, ws, ws_bytes, stream);
 }
 

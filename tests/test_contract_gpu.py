@@ -152,11 +152,13 @@ def test_tf32x3_transposed_operands_config1_shape_reduced(cuda, tc_variant):
 @pytest.mark.parametrize("m,n,k", [(1, 1, 1), (1, 1, 100000), (7, 1, 5), (3000, 1, 4096),
                                    (1, 5000, 64), (1, 3, 300000), (2, 2, 0), (5, 7, 1),
                                    (333, 77, 1), (2, 1, 200000), (3, 1, 70001), (9, 1, 1000),
-                                   (1, 2, 400000), (1, 5, 123457), (1, 300, 5000)])
+                                   (1, 2, 400000), (1, 5, 123457), (1, 300, 5000),
+                                   (64, 64, 8192), (200, 100, 3000), (27, 243, 729)])
 @pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
 def test_multiply_vector_and_edge_shapes(cuda, m, n, k, dtype):
     """GEMV, GEMV^T, DOTU and k = 0 cases of MultiplyTensorData, including few
-    rows or columns over a long k (several warps or threads per row / column)."""
+    rows or columns over a long k (several warps or threads per row / column)
+    and small matrices over a long k (k split across CTAs)."""
     from jet_gb300 import capi
 
     a = cases.tensor_data(m * 3 + k, [m * k], dtype)
