@@ -202,9 +202,13 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
 
 /*
  * Batched contraction: C[b] = contract(A[b], B[b]) for b < batch, C packed as
- * batch x m x n. A batched operand (a_batched / b_batched != 0) holds `batch`
- * tensors of its shape back to back; a shared one holds one tensor used by
- * every b. Orderings, m, n, k, precision and scales as in jetgpu_contract.
+ * batch x m x n. a_batched / b_batched: 0, a shared operand (one tensor used
+ * by every b); 1, `batch` tensors of the given shape back to back; 2, one
+ * tensor whose permutation lists first the batch axes (extents multiplying to
+ * `batch`, in batch-index order) and then the operand's own axes, so the
+ * batch may sit anywhere in its layout and the product's permute pass moves
+ * it (no separate reorder). Orderings, m, n, k, precision and scales as in
+ * jetgpu_contract.
  * This is the slice batch of TensorNetwork::SliceIndices /
  * TaskBasedContractor (TensorNetwork.hpp:210-284, TaskBasedContractor.hpp:
  * 162-248): slice-dependent tensors carry the batch, slice-independent ones

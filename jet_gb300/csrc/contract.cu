@@ -126,10 +126,10 @@ int Validate(int rank, const uint64_t *shape, const int32_t *perm, uint64_t lead
 // (and, for FP16, the operands' max exponents) in `ws`, then the tcgen05
 // product. ba / bb: tensors of A / B (batch or 1, shared operands are 1).
 int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank,
-                 const uint64_t *a_shape, const int32_t *a_perm, uint64_t ba, const void *B,
-                 int b_rank, const uint64_t *b_shape, const int32_t *b_perm, uint64_t bb,
-                 void *C, uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a,
-                 int scale_b, uint8_t *ws, cudaStream_t st, const ExpHints *hints)
+                 const uint64_t *a_shape, const int32_t *a_perm, uint64_t ba, int a_mode,
+                 const void *B, int b_rank, const uint64_t *b_shape, const int32_t *b_perm,
+                 uint64_t bb, int b_mode, void *C, uint64_t m, uint64_t n, uint64_t k, int dtype,
+                 int scale_a, int scale_b, uint8_t *ws, cudaStream_t st, const ExpHints *hints)
 {
     int rc;
     uint8_t *pa = ws;
@@ -148,17 +148,22 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
         out_scale = Pow2f(scale_a + scale_b);
         scale_a = scale_b = 0;
     }
-    // B is wanted as (right ++ common): rotate its (common ++ right) order.
-    const int nc = SplitPoint(b_rank, b_shape, b_perm, k);
-    std::vector<int32_t> bt(b_rank);
-    for (int j = 0; j < b_rank; ++j)
-        bt[j] = b_perm[(j + nc) % b_rank];
-    if ((rc = PermuteSplitPlanes(A, pa, ba, a_rank, a_shape, a_perm, m, k, l.kp, ba * m * l.kp,
-                                 scale_a, l.fmt, 0, st, e_dev)))
+    // B is wanted as (right ++ common): rotate its (common ++ right) order,
+    // behind its batch axes when they are part of its permutation (mode 2).
+    const int nb = b_mode == 2 ? SplitPoint(b_rank, b_shape, b_perm, bb) : 0;
+    const int nc = SplitPoint(b_rank, b_shape, b_perm, (b_mode == 2 ? bb : 1) * k);
+    std::vector<int32_t> bt(b_perm, b_perm + b_rank);
+    for (int j = nb; j < b_rank; ++j)
+        bt[j] = b_perm[nb + (j - nb + nc - nb) % (b_rank - nb)];
+    // Mode 1: `ba` tensors back to back; mode 2: one tensor whose leading
+    // permuted axes are the batch, i.e. ba * m rows of one split.
+    if ((rc = PermuteSplitPlanes(A, pa, a_mode == 1 ? ba : 1, a_rank, a_shape, a_perm,
+                                 (a_mode == 2 ? ba : 1) * m, k, l.kp, ba * m * l.kp, scale_a,
+                                 l.fmt, 0, st, e_dev)))
         return rc;
-    if ((rc = PermuteSplitPlanes(B, pb, bb, b_rank, b_shape, bt.data(), n, k, l.kp,
-                                 bb * n * l.kp, scale_b, l.fmt, l.b_planes == 6 ? 1 : 0, st,
-                                 e_dev ? e_dev + 1 : nullptr)))
+    if ((rc = PermuteSplitPlanes(B, pb, b_mode == 1 ? bb : 1, b_rank, b_shape, bt.data(),
+                                 (b_mode == 2 ? bb : 1) * n, k, l.kp, bb * n * l.kp, scale_b,
+                                 l.fmt, l.b_planes == 6 ? 1 : 0, st, e_dev ? e_dev + 1 : nullptr)))
         return rc;
     return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
                                   l.fmt, st, l.variant, e_dev, l.group_m,
@@ -312,6 +317,9 @@ size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const 
     }
     const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
     if (p.fold) {
+        if (a_batched == 2) // the batch axes already lead A's permutation
+            return FormWorkspace(1, a_rank, a_shape, a_perm, 0, b_rank, b_shape, b_perm, 0,
+                                 batch * m, n, k, dtype, precision);
         std::vector<uint64_t> s;
         std::vector<int32_t> pm;
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
@@ -371,6 +379,10 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
     }
     const BatchPlan p = PlanBatch(batch, a_batched, b_batched, m, n, k, dtype, precision);
     if (p.fold) {
+        if (a_batched == 2) // the batch axes already lead A's permutation
+            return ContractForm(1, A, a_rank, a_shape, a_perm, 0, B, b_rank, b_shape, b_perm, 0,
+                                C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
+                                workspace, st, group_m, hints);
         std::vector<uint64_t> s;
         std::vector<int32_t> pm;
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
@@ -381,20 +393,24 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc)
         return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant, group_m),
-                            batch, A, a_rank, a_shape, a_perm, p.ba, B, b_rank, b_shape, b_perm,
-                            p.bb, C, m, n, k, dtype, scale_a, scale_b, ws, st, hints);
+                            batch, A, a_rank, a_shape, a_perm, p.ba, p.ba > 1 ? a_batched : 0, B,
+                            b_rank, b_shape, b_perm, p.bb, p.bb > 1 ? b_batched : 0, C, m, n, k,
+                            dtype, scale_a, scale_b, ws, st, hints);
     int rc;
     const size_t eb = ElemBytes(dtype);
     const void *at = A;
     const void *btp = B;
+    // Mode 2 operands are one tensor whose permutation leads with the batch.
     if (k > 0 && !IsIdentity(a_rank, a_perm)) {
-        if ((rc = PermuteImpl(A, ws, p.ba, a_rank, a_shape, a_perm, dtype, st)))
+        if ((rc = PermuteImpl(A, ws, a_batched == 2 ? 1 : p.ba, a_rank, a_shape, a_perm, dtype,
+                              st)))
             return rc;
         at = ws;
         ws += AlignUp(p.ba * m * k * eb);
     }
     if (k > 0 && !IsIdentity(b_rank, b_perm)) {
-        if ((rc = PermuteImpl(B, ws, p.bb, b_rank, b_shape, b_perm, dtype, st)))
+        if ((rc = PermuteImpl(B, ws, b_batched == 2 ? 1 : p.bb, b_rank, b_shape, b_perm, dtype,
+                              st)))
             return rc;
         btp = ws;
         ws += AlignUp(p.bb * k * n * eb);
@@ -427,11 +443,21 @@ int CheckContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
          precision == JETGPU_PREC_FP16X3) &&
         dtype != JETGPU_C64)
         return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
-    int rc = Validate(a_rank, a_shape, a_perm, m, k, "A");
+    JETGPU_REQUIRE(a_batched >= 0 && a_batched <= 2 && b_batched >= 0 && b_batched <= 2,
+                   "batched flags must be 0, 1 or 2");
+    // Mode 2: the operand is one tensor whose permutation leads with axes of
+    // total extent `batch` (the batch), then its (left ++ common) or
+    // (common ++ right) axes.
+    const uint64_t a_lead = (batch > 1 && a_batched == 2) ? batch : 1;
+    const uint64_t b_lead = (batch > 1 && b_batched == 2) ? batch : 1;
+    int rc = Validate(a_rank, a_shape, a_perm, a_lead * m, k, "A");
     if (rc)
         return rc;
-    if ((rc = Validate(b_rank, b_shape, b_perm, k, n, "B")))
+    if ((rc = Validate(b_rank, b_shape, b_perm, b_lead * k, n, "B")))
         return rc;
+    JETGPU_REQUIRE(SplitPoint(a_rank, a_shape, a_perm, a_lead) >= 0 &&
+                       SplitPoint(b_rank, b_shape, b_perm, b_lead) >= 0,
+                   "permutation does not lead with the batch axes");
     if (m * n == 0) {
         *empty = true;
         return JETGPU_OK;

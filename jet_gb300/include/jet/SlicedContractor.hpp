@@ -149,9 +149,9 @@ template <class T = std::complex<float>> class SlicedContractor {
         return out;
     }
 
-    // One entry of ProfileChunk: a slice gather ("gather"), an operand
-    // reorder ("reorder"), a path step ("contract"), the result reorder
-    // ("result reorder") or the FP64 slice sum ("slice sum").
+    // One entry of ProfileChunk: a slice gather ("gather"), a path step
+    // ("contract"), the result reorder ("result reorder") or the FP64 slice
+    // sum ("slice sum").
     struct ChunkProfileEntry {
         std::string kind;
         int step; // index into the path (-1 when not a step)
@@ -160,7 +160,7 @@ template <class T = std::complex<float>> class SlicedContractor {
     };
 
     // Runs one chunk (slices [first, first + batch size)) eagerly with a CUDA
-    // event after every gather, reorder, contraction and the slice sum, and
+    // event after every gather, contraction and the slice sum, and
     // returns each one's device time: a per-step profile of what the captured
     // graph replays. The accumulator holds that chunk's sum afterwards.
     std::vector<ChunkProfileEntry> ProfileChunk(size_t first = 0)
@@ -223,12 +223,12 @@ template <class T = std::complex<float>> class SlicedContractor {
         bool chunk;
         bool batched; // "$s"/"$b" on both operands
         uint64_t batch, m, n, k;
-        // Operand views: optional pre-permutation into a temporary (batched
-        // steps whose shared hyper labels are not leading).
-        std::vector<uint64_t> a_shape, b_shape; // views passed to the product
+        // Operand views passed to the product, and how each carries the batch
+        // (jetgpu_contract_batched's a_batched / b_batched: 0 shared, 1
+        // tensors back to back, 2 batch axes leading the permutation).
+        std::vector<uint64_t> a_shape, b_shape;
         std::vector<int32_t> a_perm, b_perm;
-        std::vector<uint64_t> a_pre_shape, b_pre_shape;
-        std::vector<int32_t> a_pre_perm, b_pre_perm;
+        int a_mode = 0, b_mode = 0;
         size_t ws = 0;
     };
     struct Profile {
@@ -266,12 +266,12 @@ template <class T = std::complex<float>> class SlicedContractor {
     std::vector<size_t> result_dims_;
     size_t result_size_ = 1;
     double slice_flops_ = 0, slice_dep_flops_ = 0;
-    size_t arena_bytes_ = 0, ws_bytes_ = 0, tmp_bytes_ = 0;
+    size_t arena_bytes_ = 0, ws_bytes_ = 0;
     bool planned_ = false;
     bool prefix_done_ = false;
     std::vector<char> persist_;
     std::vector<int> prefix_last_use_;
-    Gpu::DeviceBuffer arena_, ws_, tmp_a_, tmp_b_, acc_, counter_, final_tmp_;
+    Gpu::DeviceBuffer arena_, ws_, acc_, counter_, final_tmp_;
     // One int per node: the max exponent its producing step recorded
     // (jetgpu_contract_batched_hinted), read by the steps consuming it.
     Gpu::DeviceBuffer emax_;
@@ -359,7 +359,7 @@ template <class T = std::complex<float>> class SlicedContractor {
         }
         // Steps (symbolic).
         slice_flops_ = slice_dep_flops_ = 0;
-        ws_bytes_ = tmp_bytes_ = 0;
+        ws_bytes_ = 0;
         for (size_t i = 0; i < path_.size(); ++i) {
             const auto [ia, ib] = path_[i];
             JET_ABORT_IF_NOT(ia < nodes_.size() && ib < nodes_.size(),
@@ -398,44 +398,36 @@ template <class T = std::complex<float>> class SlicedContractor {
                 out.dims.push_back(Dim(B, x));
             // Operand views.
             auto view = [&](const Node &X, const std::vector<std::string> &order,
-                            std::vector<uint64_t> &pre_shape, std::vector<int32_t> &pre_perm,
                             std::vector<uint64_t> &shape, std::vector<int32_t> &perm) {
-                // The product wants X as `hyper` (leading, the batch) followed by
-                // the other axes; pre-permute when hyper is not already leading.
-                bool leading = X.labels.size() >= hyper.size() &&
-                               std::equal(hyper.begin(), hyper.end(), X.labels.begin());
-                std::vector<std::string> body_labels;
-                std::vector<uint64_t> body_dims;
-                if (!leading) {
-                    pre_shape = X.dims;
-                    std::vector<std::string> ordered = hyper;
-                    for (const auto &x : X.labels)
-                        if (!InVector(x, hyper))
-                            ordered.push_back(x);
-                    for (const auto &x : ordered)
-                        pre_perm.push_back(Pos(X.labels, x));
-                    body_labels.assign(ordered.begin() + hyper.size(), ordered.end());
+                // The product wants X as `hyper` (the batch) followed by `order`.
+                // With hyper leading X's labels, X is batch tensors back to back
+                // (mode 1); otherwise the batch axes lead X's permutation and
+                // the product's own permute pass moves them (mode 2).
+                const bool leading = X.labels.size() >= hyper.size() &&
+                                     std::equal(hyper.begin(), hyper.end(), X.labels.begin());
+                if (leading) {
+                    const std::vector<std::string> body(X.labels.begin() + hyper.size(),
+                                                        X.labels.end());
+                    for (const auto &x : body)
+                        shape.push_back(Dim(X, x));
+                    for (const auto &x : order)
+                        perm.push_back(Pos(body, x));
+                    return 1;
                 }
-                else {
-                    body_labels.assign(X.labels.begin() + hyper.size(), X.labels.end());
-                }
-                for (const auto &x : body_labels)
-                    body_dims.push_back(Dim(X, x));
-                shape = body_dims;
+                shape = X.dims;
+                for (const auto &x : hyper)
+                    perm.push_back(Pos(X.labels, x));
                 for (const auto &x : order)
-                    perm.push_back(Pos(body_labels, x));
+                    perm.push_back(Pos(X.labels, x));
+                return 2;
             };
-            view(A, VectorConcatenation(left, common), s.a_pre_shape, s.a_pre_perm, s.a_shape,
-                 s.a_perm);
-            view(B, VectorConcatenation(common, right), s.b_pre_shape, s.b_pre_perm, s.b_shape,
-                 s.b_perm);
-            if (!s.a_pre_perm.empty())
-                tmp_bytes_ = std::max(tmp_bytes_, A.bytes);
-            if (!s.b_pre_perm.empty())
-                tmp_bytes_ = std::max(tmp_bytes_, B.bytes);
+            s.a_mode = view(A, VectorConcatenation(left, common), s.a_shape, s.a_perm);
+            s.b_mode = view(B, VectorConcatenation(common, right), s.b_shape, s.b_perm);
+            if (!s.batched)
+                s.a_mode = s.b_mode = 0;
             s.ws = jetgpu_contract_batched_workspace_size(
-                s.batch, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(), s.batched,
-                (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(), s.batched, s.m, s.n,
+                s.batch, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(), s.a_mode,
+                (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(), s.b_mode, s.m, s.n,
                 s.k, dt, precision_);
             ws_bytes_ = std::max(ws_bytes_, s.ws);
             out.chunk = InVector(std::string(kSlice), out.labels);
@@ -528,8 +520,6 @@ template <class T = std::complex<float>> class SlicedContractor {
         arena_bytes_ = top;
         arena_ = Gpu::DeviceBuffer(std::max<size_t>(arena_bytes_, 256));
         ws_ = Gpu::DeviceBuffer(ws_bytes_);
-        tmp_a_ = Gpu::DeviceBuffer(tmp_bytes_);
-        tmp_b_ = Gpu::DeviceBuffer(tmp_bytes_);
         acc_ = Gpu::DeviceBuffer(std::max<size_t>(result_size_ * 16, 16));
         counter_ = Gpu::DeviceBuffer(8);
         emax_ = Gpu::DeviceBuffer(std::max<size_t>(nodes_.size(), 1) * sizeof(int));
@@ -605,33 +595,17 @@ template <class T = std::complex<float>> class SlicedContractor {
         const int idx = (int)(&s - steps_.data());
         const void *a = Buffer(s.a);
         const void *b = Buffer(s.b);
-        if (!s.a_pre_perm.empty()) {
-            Gpu::Check(jetgpu_permute(a, tmp_a_.get(), (int)s.a_pre_shape.size(),
-                                      s.a_pre_shape.data(), s.a_pre_perm.data(), dt, st),
-                       "operand reorder");
-            a = tmp_a_.get();
-            if (prof)
-                prof->Mark("reorder", idx, s.batch, s.m, s.k, 0);
-        }
-        if (!s.b_pre_perm.empty()) {
-            Gpu::Check(jetgpu_permute(b, tmp_b_.get(), (int)s.b_pre_shape.size(),
-                                      s.b_pre_shape.data(), s.b_pre_perm.data(), dt, st),
-                       "operand reorder");
-            b = tmp_b_.get();
-            if (prof)
-                prof->Mark("reorder", idx, s.batch, s.k, s.n, 0);
-        }
         // Steps that run once gain nothing from tuning: AUTO's rule.
         const int prec =
             (!s.chunk && precision_ == JETGPU_PREC_TUNED) ? JETGPU_PREC_AUTO : precision_;
-        // Intermediates carry the max exponent their producing step recorded
-        // (a reorder keeps the values); leaves are scanned when needed.
+        // Intermediates carry the max exponent their producing step recorded;
+        // leaves are scanned when needed.
         int *emax = static_cast<int *>(emax_.get());
         const bool hints = exponent_hints_ && emax != nullptr;
         Gpu::Check(jetgpu_contract_batched_hinted(
                        s.batch, a, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(),
-                       s.batched, b, (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(),
-                       s.batched, Buffer(s.out), s.m, s.n, s.k, dt, prec, JETGPU_ALGO_4M,
+                       s.a_mode, b, (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(),
+                       s.b_mode, Buffer(s.out), s.m, s.n, s.k, dt, prec, JETGPU_ALGO_4M,
                        hints && s.a >= (int)num_leaves_ ? emax + s.a : nullptr,
                        hints && s.b >= (int)num_leaves_ ? emax + s.b : nullptr,
                        hints ? emax + s.out : nullptr, ws_.get(), ws_.size(), st),

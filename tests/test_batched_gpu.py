@@ -62,3 +62,51 @@ def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape, variant
         assert err <= tol, (bi, err)
     assert capi.take_device_status() == 0
     capi.set_tc_variant(0)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 3, 4])
+@pytest.mark.parametrize("modes", [(2, 2), (2, 0), (0, 2), (2, 1), (1, 2)])
+def test_batch_axes_inside_the_permutation(cuda, precision, modes):
+    """a_batched / b_batched = 2: the operand is one tensor whose batch axes
+    (two of them here, anywhere in its layout) lead its permutation. Same bits
+    as reordering the batch to the front first and passing mode 1."""
+    import torch
+
+    from jet_gb300 import capi
+
+    rng = np.random.default_rng(17 + 3 * modes[0] + modes[1] + 10 * precision)
+    batch, m, k, n = 4, 2 ** 7, 2 ** 6, 2 ** 6
+
+    def operand(mode, lead, tail, seed):
+        # Own axes: log2(lead) + log2(tail) axes of 2, in a random layout
+        # order; mode 2 adds two batch axes of 2 at random places.
+        own = int(np.log2(lead)) + int(np.log2(tail))
+        labels = ["o%d" % i for i in range(own)]
+        layout = [labels[i] for i in rng.permutation(own)]
+        if mode == 2:
+            for b in ("s0", "s1"):
+                layout.insert(int(rng.integers(0, len(layout) + 1)), b)
+        count = batch if mode == 1 else 1
+        g = torch.Generator(device=cuda)
+        g.manual_seed(seed)
+        x = torch.randn(count * 2 ** len(layout), dtype=torch.complex64, device=cuda, generator=g)
+        shape = [2] * len(layout)
+        own_perm = [layout.index(l) for l in labels]
+        if mode == 2:
+            perm = [layout.index("s0"), layout.index("s1")] + own_perm
+            # The reference: batch axes moved to the front, then mode 1.
+            front = capi.permute(x, shape, [layout.index("s0"), layout.index("s1")] +
+                                 [i for i, l in enumerate(layout) if l not in ("s0", "s1")])
+            rest = [l for l in layout if l not in ("s0", "s1")]
+            ref = (front, [2] * len(rest), [rest.index(l) for l in labels], 1)
+            return (x, shape, perm, 2), ref
+        return (x, shape, own_perm, mode), (x, shape, own_perm, mode)
+
+    (a, a_ref) = operand(modes[0], m, k, 5)
+    (b, b_ref) = operand(modes[1], k, n, 6)
+    got = capi.contract_batched(batch, a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], m, n, k,
+                                precision=precision)
+    want = capi.contract_batched(batch, a_ref[0], a_ref[1], a_ref[2], a_ref[3], b_ref[0],
+                                 b_ref[1], b_ref[2], b_ref[3], m, n, k, precision=precision)
+    assert torch.equal(got.view(torch.int64), want.view(torch.int64))
+    assert capi.take_device_status() == 0
