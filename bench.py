@@ -369,34 +369,36 @@ def run_ours(args, rank, world, local_rank):
     # End to end through the public API with host buffers: every step copies
     # its A and B from pinned host memory to the device, contracts them with
     # jetgpu_contract (the headline form) and copies C back to pinned host
-    # memory. Steps
-    # are pipelined over two device buffer sets, so step i's uploads and step
-    # i-1's download (copy streams) overlap step i-1's and i's contractions.
+    # memory. Steps are pipelined over three device buffer sets, so step i's
+    # uploads and the downloads of earlier steps (copy streams) overlap the
+    # contractions before it; the host link (about 210 GB/s up, 190 down, 280
+    # both ways at once on this machine) moves 1.88 GB per step.
     hA = A.cpu().pin_memory()
     hB = B.cpu().pin_memory()
+    n_slots = 3
     slots = [dict(a=torch.empty_like(A), b=torch.empty_like(B), c=torch.empty_like(C),
-                  hc=torch.empty(C.shape, dtype=C.dtype).pin_memory()) for _ in range(2)]
+                  hc=torch.empty(C.shape, dtype=C.dtype).pin_memory()) for _ in range(n_slots)]
     ws_tc = torch.empty(capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
                                                      w["b_perm_kn"], m, n, k, capi.C64,
                                                      head_prec),
                         dtype=torch.uint8, device=dev)
     cs_in = torch.cuda.Stream(dev)
     cs_out = torch.cuda.Stream(dev)
-    ev = {key: [torch.cuda.Event() for _ in range(2)] for key in ("in", "comp", "out")}
+    ev = {key: [torch.cuda.Event() for _ in range(n_slots)] for key in ("in", "comp", "out")}
     for key in ev:
         for e in ev[key]:
             e.record(stream)
 
     def e2e_step(i):
-        j = i % 2
+        j = i % n_slots
         sl = slots[j]
         with torch.cuda.stream(cs_in):
-            cs_in.wait_event(ev["comp"][j])       # slot j's inputs consumed by step i-2
+            cs_in.wait_event(ev["comp"][j])       # slot j's inputs consumed by step i-3
             sl["a"].copy_(hA, non_blocking=True)
             sl["b"].copy_(hB, non_blocking=True)
             ev["in"][j].record(cs_in)
         stream.wait_event(ev["in"][j])
-        stream.wait_event(ev["out"][j])           # slot j's C read back by step i-2
+        stream.wait_event(ev["out"][j])           # slot j's C read back by step i-3
         capi.contract(sl["a"], w["a_shape"], w["a_perm"], sl["b"], w["b_shape"], w["b_perm_kn"],
                       m, n, k, precision=head_prec, out=sl["c"], workspace=ws_tc,
                       stream=stream)
@@ -418,7 +420,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_value = world * flops / (e2e_ms * 1e-3) / 1e12
-    e2e_err = rel_err_of(slots[(e2e_steps - 1) % 2]["hc"])
+    e2e_err = rel_err_of(slots[(e2e_steps - 1) % n_slots]["hc"])
     del slots, ws_tc
 
     hbm_peak, bf16_peak, peak_src = measured_peaks()
@@ -483,7 +485,7 @@ def run_ours(args, rank, world, local_rank):
                 "h2d_bytes_per_step": int(A.numel() * 8 + B.numel() * 8),
                 "d2h_bytes_per_step": int(C.numel() * 8), "ms_per_step": e2e_ms,
                 "rel_err_vs_fp64": e2e_err,
-                "pipeline": "two device buffer sets; H2D and D2H on copy streams overlap "
+                "pipeline": "three device buffer sets; H2D and D2H on copy streams overlap "
                             "the contractions"},
         # per step: 2 splits + 1 product (FP16: + one max-exponent kernel per
         # operand, each after a 4-byte memset)
