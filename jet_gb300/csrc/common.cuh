@@ -170,13 +170,15 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 // the current setting.
 // For FP16, `e_max_dev` points at the two operands' max exponents (A, B) and
 // the epilogue undoes their scales. `group_m`: tile rows per group of the
-// tile order (0: the jetgpu_set_tc_group_m setting).
+// tile order (0: the jetgpu_set_tc_group_m setting). `tile_counter`: device
+// word of the caller's workspace for the persistent launch's tile counter
+// (null: a slot of a library-wide ring).
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant = -1,
                            const int *e_max_dev = nullptr, int group_m = 0,
-                           int *out_emax = nullptr);
+                           int *out_emax = nullptr, unsigned int *tile_counter = nullptr);
 
 // Workspace bytes of a (batched) contraction in `precision` (JETGPU_PREC_TUNED:
 // the largest of its candidates' and AUTO's).

@@ -36,8 +36,9 @@ struct SplitLayout {
     int group_m;      // tile order (0: the setting)
     size_t a_bytes(uint64_t rows) const { return AlignUp(4 * rows * kp * word); }
     size_t b_bytes(uint64_t rows) const { return AlignUp(b_planes * rows * kp * word); }
-    // FP16: two ints (max exponents of A and B) after the planes.
-    size_t exp_bytes() const { return fmt == SplitFormat::kFp16 ? kAlign : 0; }
+    // After the planes: the operands' max exponents (two ints, FP16) and the
+    // product's tile counter (one unsigned int at byte 16).
+    size_t exp_bytes() const { return kAlign; }
 };
 
 // The split form JETGPU_PREC_AUTO uses on tensor-core steps
@@ -134,6 +135,8 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
     int rc;
     uint8_t *pa = ws;
     uint8_t *pb = ws + l.a_bytes(ba * m);
+    uint8_t *tail = pb + AlignUp((size_t)l.b_planes * bb * n * l.kp * l.word);
+    unsigned int *tile_counter = reinterpret_cast<unsigned int *>(tail + 16);
     int *e_dev = nullptr;
     float out_scale = 1.0f;
     if (l.fmt == SplitFormat::kFp16) {
@@ -141,7 +144,7 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
         // scales move to the epilogue.
         JETGPU_REQUIRE(scale_a + scale_b >= -126 && scale_a + scale_b <= 126,
                        "scale_a + scale_b out of range for FP16x3");
-        e_dev = reinterpret_cast<int *>(pb + AlignUp((size_t)l.b_planes * bb * n * l.kp * l.word));
+        e_dev = reinterpret_cast<int *>(tail);
         if ((rc = MaxExponent2(A, ba * m * k, B, bb * k * n, dtype, e_dev, st, 2,
                                hints ? hints->a : nullptr, hints ? hints->b : nullptr)))
             return rc;
@@ -167,7 +170,7 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
         return rc;
     return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
                                   l.fmt, st, l.variant, e_dev, l.group_m,
-                                  hints ? hints->c : nullptr);
+                                  hints ? hints->c : nullptr, tile_counter);
 }
 
 } // namespace

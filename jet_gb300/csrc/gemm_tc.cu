@@ -785,11 +785,13 @@ int EncodePlanesBatched(CUtensorMap *map, const void *base, uint64_t rows, uint6
 // (jetgpu_set_tc_persistent).
 std::atomic<int> g_tc_persistent{1};
 
-// A zeroed tile counter for one persistent launch on `stream`: a slot of a
-// per-device array, reset by a memset enqueued before the launch (so a
-// captured graph resets it on every replay). Consecutive launches take
-// consecutive slots. nullptr (the static tile order) if the array cannot be
-// made.
+// A zeroed tile counter for a persistent launch whose caller gave no
+// workspace word (the two-stage entry points): a slot of a per-device ring,
+// reset by a memset enqueued before the launch (so a captured graph resets
+// it on every replay). Consecutive launches take consecutive slots, so two
+// launches share a slot only 4096 launches apart. nullptr (the static tile
+// order) if the ring cannot be made. Contractions through jetgpu_contract*
+// keep their counter in their own workspace instead.
 unsigned int *TileCounter(cudaStream_t stream)
 {
     constexpr uint32_t kSlots = 4096;
@@ -829,7 +831,7 @@ template <int V>
 int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t batch, uint64_t m,
              uint64_t n, uint64_t k, float out_scale, int a_batched, int b_batched,
              cudaStream_t stream, const int *e_max_dev = nullptr, int group_m = 0,
-             int *out_emax = nullptr)
+             int *out_emax = nullptr, unsigned int *tile_counter = nullptr)
 {
     const size_t smem = (size_t)TcCfg<V>::Stages * StageBytes<V>() + kAccWarps * kStoreBytes + 1024;
     static thread_local int configured_dev = -1;
@@ -849,7 +851,16 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     const bool persistent = g_tc_persistent.load(std::memory_order_relaxed) != 0;
     const unsigned grid =
         (unsigned)(persistent ? std::min<uint64_t>(tiles, (uint64_t)SmCount()) : tiles);
-    unsigned int *counter = persistent && grid < tiles ? TileCounter(stream) : nullptr;
+    unsigned int *counter = nullptr;
+    if (persistent && grid < tiles) {
+        if (tile_counter != nullptr) {
+            JETGPU_CUDA_TRY(cudaMemsetAsync(tile_counter, 0, sizeof(unsigned int), stream));
+            counter = tile_counter;
+        }
+        else {
+            counter = TileCounter(stream);
+        }
+    }
     const int ktiles = (int)((k + BlockK<V>() - 1) / BlockK<V>());
     tc_gemm_split_kernel<V><<<grid, kThreads, smem, stream>>>(
         ta, tb, reinterpret_cast<float2 *>(C), (int)m, (int)n, ktiles, (int)batch, out_scale,
@@ -884,7 +895,7 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant, const int *e_max_dev, int group_m,
-                           int *out_emax)
+                           int *out_emax, unsigned int *tile_counter)
 {
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
@@ -925,17 +936,17 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (fp16)
         return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           e_max_dev, group_m, out_emax);
+                           e_max_dev, group_m, out_emax, tile_counter);
     if (deep)
         return LaunchTc<3>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           nullptr, group_m, out_emax);
+                           nullptr, group_m, out_emax, tile_counter);
     if (bf16)
         return LaunchTc<2>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                           nullptr, group_m, out_emax);
+                           nullptr, group_m, out_emax, tile_counter);
     return wide ? LaunchTc<1>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
-                              nullptr, group_m, out_emax)
+                              nullptr, group_m, out_emax, tile_counter)
                 : LaunchTc<0>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
-                              stream, nullptr, group_m, out_emax);
+                              stream, nullptr, group_m, out_emax, tile_counter);
 }
 
 int TcVariant() { return g_tc_variant.load(std::memory_order_relaxed); }
