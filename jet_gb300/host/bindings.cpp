@@ -259,7 +259,7 @@ template <class T> void BindSliced(py::module_ &m)
                  return out;
              },
              py::arg("first") = 0,
-             "Device ms of every gather, reorder, contraction and the slice sum of one chunk.")
+             "Device ms of every gather, contraction and the slice sum of one chunk.")
         .def_property_readonly("batch_size", &sc_t::GetBatchSize)
         .def_property_readonly("num_slices", &sc_t::GetNumSlices)
         .def_property_readonly("result_indices", &sc_t::GetResultIndices)

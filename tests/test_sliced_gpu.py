@@ -199,7 +199,7 @@ def test_network_amplitude_within_1e5_of_fp64(jet, precision):
 
 
 def test_profile_chunk_times_every_launch(jet):
-    """profile_chunk: one entry per slice gather, operand reorder, path step
+    """profile_chunk: one entry per slice gather, path step, result reorder
     and the slice sum of a chunk, each with a device time; the chunk's sum is
     left in the accumulator and later contractions are unaffected."""
     from jet_gb300 import circuits
@@ -214,7 +214,7 @@ def test_profile_chunk_times_every_launch(jet):
     kinds = [e["kind"] for e in prof]
     assert kinds.count("slice sum") == 1 and kinds[-1] == "slice sum"
     assert kinds.count("gather") >= 1 and kinds.count("contract") >= 1
-    assert set(kinds) <= {"gather", "reorder", "contract", "result reorder", "slice sum"}
+    assert set(kinds) <= {"gather", "contract", "result reorder", "slice sum"}
     assert all(e["ms"] >= 0 for e in prof)
     steps = [e["step"] for e in prof if e["kind"] == "contract"]
     assert steps == sorted(steps) and len(set(steps)) == len(steps)
