@@ -121,7 +121,8 @@ def test_split_bf16_bit_exact(cuda, shape, perm):
 
 @pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 128, 64), (200, 136, 100),
                                    (1024, 512, 256), (130, 300, 33), (4096, 256, 1024),
-                                   (64, 512, 2048), (384, 256, 4096)])
+                                   (64, 512, 2048), (384, 256, 4096), (129, 131, 77),
+                                   (300, 257, 64)])
 def test_bf16x3_random_gemm(cuda, m, n, k, bf16_variant):
     """Config-1 value distribution against complex128 (1e-5) and against the
     exact three-product model (2e-6, the accumulation alone)."""

@@ -99,7 +99,7 @@ def test_reference_literal_values(cuda):
 
 @pytest.mark.parametrize("m,n,k", [(128, 128, 16), (256, 128, 64), (200, 136, 100),
                                    (1024, 512, 256), (130, 300, 33), (4096, 256, 1024),
-                                   (64, 512, 2048)])
+                                   (64, 512, 2048), (129, 131, 77), (300, 257, 64)])
 def test_tf32x3_random_gemm(cuda, m, n, k, tc_variant):
     """Random N(0, 1/2) complex entries scaled by 2^-10 (the config-1
     distribution) against the complex128 product."""
