@@ -567,6 +567,37 @@ def run_sliced(args, rank, world, local_rank):
     profiles = {}
     for name, prec, auto_form in sliced_forms:
         capi.set_auto_form(auto_form or capi.PREC_FP16X3)
+        if not sliced:
+            # No slices (config 0): the network is one amplitude; time the
+            # reference's own flow, a TaskBasedContractor over the path, built
+            # and run afresh each time (the sliced contractor would cache it).
+            jet.set_precision(prec)
+            info = jet.PathInfo(tn=tn, path=path)
+
+            def run_tbc():
+                tbc = jet.TaskBasedContractor(dtype="complex64")
+                tbc.add_contraction_tasks(tn, info)
+                tbc.add_deletion_tasks()
+                tbc.contract()
+                return tbc.results[0]
+
+            for _ in range(3):
+                res = run_tbc()
+            reps = []
+            while sum(reps) < 0.3 or len(reps) < 5:
+                t1 = time.perf_counter()
+                res = run_tbc()
+                reps.append(time.perf_counter() - t1)
+            jet.set_precision(jet.PREC_FP32)
+            dt = statistics.median(reps)
+            flops = info.total_flops()
+            forms[name] = {"slices_per_s": 1.0 / dt, "s_per_slice": dt,
+                           "eff_tflops": 4.0 * flops / dt / 1e12, "slices_timed": 1,
+                           "runs": len(reps), "arena_gb": 0.0,
+                           "flow": "TaskBasedContractor, built and run per amplitude"}
+            amps[name] = complex(res.data[0]) if hasattr(res, "data") else complex(res[0])
+            slice_flops = dep_flops = flops
+            continue
         sc = jet.SlicedContractorC64(tn, path, sliced, prec)
         sc.set_batch_size(batch)
         n_all = sc.num_slices
