@@ -252,6 +252,32 @@ int jetgpu_contract_batched_hinted(uint64_t batch, const void *A, int a_rank,
                                    void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * A group of small independent contractions in one launch (no counterpart in
+ * the reference, which makes one BLAS call per step): task t computes
+ * C_t[b] = A_t[b] B_t[b] for b < batch, C_t packed batch x m x n row-major,
+ * in the plain form (complex FMA in the element type). Operands are read
+ * through device offset tables: element (b, i, j) of A's m x k view is
+ * A[a_bat[b] + a_row[i] + a_col[j]], of B's k x n view B[b_bat[b] + b_row[i]
+ * + b_col[j]] (element offsets; a shared operand's bat table is zeros), so
+ * any axis order and batch placement needs no transpose pass. `tasks` is a
+ * device array of n_tasks (<= 256) descriptors; total_tiles is the sum over
+ * the tasks of jetgpu_group_tiles(batch, m, n). No task may write another's
+ * operands.
+ */
+typedef struct {
+    const void *A;
+    const void *B;
+    void *C;
+    uint64_t batch, m, n, k;
+    const int64_t *a_bat, *a_row, *a_col;
+    const int64_t *b_bat, *b_row, *b_col;
+} jetgpu_group_task;
+
+uint64_t jetgpu_group_tiles(uint64_t batch, uint64_t m, uint64_t n);
+int jetgpu_contract_group(const jetgpu_group_task *tasks, int n_tasks, uint64_t total_tiles,
+                          int dtype, void *stream);
+
+/*
  * jetgpu_contract without a workspace argument and without allocating: for
  * callers that cannot allocate device memory when they contract -- inside a
  * CUDA stream capture, where cudaMalloc is illegal; under a host's own fixed

@@ -97,6 +97,17 @@ lib.jetgpu_contract_batched_hinted.argtypes = [
     ctypes.c_uint64, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp, ctypes.c_int, _u64p,
     _i32p, ctypes.c_int, _vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
     ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]
+class GroupTask(ctypes.Structure):
+    """jetgpu_group_task (include/jetgpu.h)."""
+    _fields_ = [("A", _vp), ("B", _vp), ("C", _vp), ("batch", ctypes.c_uint64),
+                ("m", ctypes.c_uint64), ("n", ctypes.c_uint64), ("k", ctypes.c_uint64),
+                ("a_bat", _vp), ("a_row", _vp), ("a_col", _vp),
+                ("b_bat", _vp), ("b_row", _vp), ("b_col", _vp)]
+
+
+lib.jetgpu_group_tiles.restype = ctypes.c_uint64
+lib.jetgpu_group_tiles.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+lib.jetgpu_contract_group.argtypes = [_vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, _vp]
 lib.jetgpu_add.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
 lib.jetgpu_conj.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _vp]
 lib.jetgpu_slice_sum_f64.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _vp,
@@ -272,6 +283,45 @@ def contract_batched_hinted(batch, a, a_shape, a_perm, a_batched, b, b_shape, b_
         precision, ALGO_4M, _ptr(a_emax), _ptr(b_emax), _ptr(c_emax), _ptr(workspace), ws_bytes,
         _stream(stream)))
     return out
+
+
+def view_offsets(shape, axes):
+    """Element offsets in a row-major tensor of `shape` of every index
+    combination of `axes` (first axis slowest): a grouped task's table."""
+    import numpy as np
+
+    strides = [1] * len(shape)
+    for j in range(len(shape) - 2, -1, -1):
+        strides[j] = strides[j + 1] * shape[j + 1]
+    out = np.zeros(1, dtype=np.int64)
+    for ax in axes:
+        out = (out[:, None] + np.arange(shape[ax], dtype=np.int64)[None, :] * strides[ax]).ravel()
+    return out
+
+
+def contract_group(tasks, stream=None):
+    """Grouped launch (jetgpu_contract_group). `tasks`: list of dicts with
+    A, B, C (device tensors of one dtype), batch, m, n, k and the six offset
+    tables a_bat, a_row, a_col, b_bat, b_row, b_col (int64 device tensors).
+    Returns the device buffer holding the task array (keep it alive until the
+    launch has run)."""
+    import torch
+
+    if not tasks:
+        return None
+    arr = (GroupTask * len(tasks))()
+    total = 0
+    for q, t in zip(arr, tasks):
+        q.A, q.B, q.C = _ptr(t["A"]), _ptr(t["B"]), _ptr(t["C"])
+        q.batch, q.m, q.n, q.k = t["batch"], t["m"], t["n"], t["k"]
+        for f in ("a_bat", "a_row", "a_col", "b_bat", "b_row", "b_col"):
+            setattr(q, f, _ptr(t[f]))
+        total += int(lib.jetgpu_group_tiles(t["batch"], t["m"], t["n"]))
+    dev = tasks[0]["A"].device
+    raw = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+    check(lib.jetgpu_contract_group(_ptr(raw), len(tasks), total,
+                                    dtype_code(tasks[0]["A"].dtype), _stream(stream)))
+    return raw
 
 
 def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, n_planes=4,

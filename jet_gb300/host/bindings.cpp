@@ -228,6 +228,7 @@ template <class T> void BindSliced(py::module_ &m)
              py::arg("tn"), py::arg("path"), py::arg("sliced_indices"), py::arg("precision") = 0)
         .def("set_batch_size", &sc_t::SetBatchSize, py::arg("slices_per_batch"))
         .def("set_exponent_hints", &sc_t::SetExponentHints, py::arg("on"))
+        .def("set_grouping", &sc_t::SetGrouping, py::arg("on"))
         .def("set_leaf_alternatives", &sc_t::SetLeafAlternatives, py::arg("node_id"),
              py::arg("values"), py::arg("count"))
         .def("contract",

@@ -29,6 +29,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <complex>
 #include <limits>
 #include <map>
@@ -105,6 +106,14 @@ template <class T = std::complex<float>> class SlicedContractor {
 
     size_t GetBatchSize() const { return batch_; }
 
+    // Run consecutive independent tiny steps (AUTO / TUNED / FP32 only) as
+    // one grouped launch (default on; off: one launch per step).
+    void SetGrouping(bool on)
+    {
+        grouping_ = on;
+        planned_ = false;
+    }
+
     // Pass each step's recorded output exponent to the steps consuming it, so
     // the FP16x3 form skips its scan of tensor-core outputs (default on; the
     // results are the same either way).
@@ -150,8 +159,9 @@ template <class T = std::complex<float>> class SlicedContractor {
     }
 
     // One entry of ProfileChunk: a slice gather ("gather"), a path step
-    // ("contract"), the result reorder ("result reorder") or the FP64 slice
-    // sum ("slice sum").
+    // ("contract"), a grouped launch of tiny steps ("group": `step` is its
+    // first step, `batch` the number of steps), the result reorder ("result
+    // reorder") or the FP64 slice sum ("slice sum").
     struct ChunkProfileEntry {
         std::string kind;
         int step; // index into the path (-1 when not a step)
@@ -230,6 +240,16 @@ template <class T = std::complex<float>> class SlicedContractor {
         std::vector<int32_t> a_perm, b_perm;
         int a_mode = 0, b_mode = 0;
         size_t ws = 0;
+        // Labels of the product's view: batch (hyper), rows, k, columns.
+        std::vector<std::string> hyper, left, common, right;
+    };
+    // What one chunk replays, in order: one step, or a group of independent
+    // tiny steps run as one grouped launch (jetgpu_contract_group).
+    struct Item {
+        std::vector<int> steps;
+        bool grouped = false;
+        const jetgpu_group_task *tasks = nullptr; // device task table (grouped)
+        uint64_t tiles = 0;
     };
     struct Profile {
         explicit Profile(void *st) : timer(st) {}
@@ -276,6 +296,11 @@ template <class T = std::complex<float>> class SlicedContractor {
     // (jetgpu_contract_batched_hinted), read by the steps consuming it.
     Gpu::DeviceBuffer emax_;
     bool exponent_hints_ = true;
+    // Grouped launches of tiny steps (jetgpu_contract_group).
+    static constexpr double kGroupMaxWork = 131072.0; // batch m n k below AUTO's smallest TC step
+    std::vector<Item> items_;
+    Gpu::DeviceBuffer group_buf_;
+    bool grouping_ = true;
     std::vector<Gpu::DeviceBuffer> alt_bufs_;
     void *graph_ = nullptr;
 
@@ -425,6 +450,10 @@ template <class T = std::complex<float>> class SlicedContractor {
             s.b_mode = view(B, VectorConcatenation(common, right), s.b_shape, s.b_perm);
             if (!s.batched)
                 s.a_mode = s.b_mode = 0;
+            s.hyper = hyper;
+            s.left = left;
+            s.common = common;
+            s.right = right;
             s.ws = jetgpu_contract_batched_workspace_size(
                 s.batch, (int)s.a_shape.size(), s.a_shape.data(), s.a_perm.data(), s.a_mode,
                 (int)s.b_shape.size(), s.b_shape.data(), s.b_perm.data(), s.b_mode, s.m, s.n,
@@ -465,13 +494,46 @@ template <class T = std::complex<float>> class SlicedContractor {
             result_size_ *= fin.dims[j];
         }
         final_perm_needed_ = spos > 0 && spos < (int)fin.labels.size();
-        // Chunk arena: liveness-planned offsets (first fit, 256-byte aligned).
-        std::vector<int> last_use(nodes_.size(), -1);
-        for (size_t i = 0; i < steps_.size(); ++i) {
-            last_use[steps_[i].a] = (int)i;
-            last_use[steps_[i].b] = (int)i;
+        // What a chunk replays: consecutive independent tiny steps become one
+        // grouped launch; every other step is its own item.
+        items_.clear();
+        {
+            std::vector<int> group;
+            std::vector<int> group_outs;
+            auto flush = [&] {
+                if (group.size() == 1)
+                    items_.push_back(Item{group, false});
+                else if (!group.empty())
+                    items_.push_back(Item{group, true});
+                group.clear();
+                group_outs.clear();
+            };
+            for (size_t i = 0; i < steps_.size(); ++i) {
+                const Step &st = steps_[i];
+                if (!st.chunk)
+                    continue;
+                if (!Groupable(st)) {
+                    flush();
+                    items_.push_back(Item{{(int)i}, false});
+                    continue;
+                }
+                if (InVector(st.a, group_outs) || InVector(st.b, group_outs) ||
+                    group.size() >= 256)
+                    flush();
+                group.push_back((int)i);
+                group_outs.push_back(st.out);
+            }
+            flush();
         }
-        last_use[final_id_] = (int)steps_.size();
+        // Chunk arena: liveness-planned offsets (first fit, 256-byte aligned)
+        // over the items: a group's outputs are all live while it runs.
+        std::vector<int> last_use(nodes_.size(), -1);
+        for (size_t it = 0; it < items_.size(); ++it)
+            for (int i : items_[it].steps) {
+                last_use[steps_[i].a] = (int)it;
+                last_use[steps_[i].b] = (int)it;
+            }
+        last_use[final_id_] = (int)items_.size();
         std::map<size_t, size_t> free_blocks; // offset -> size
         size_t top = 0;
         auto align = [](size_t v) { return (v + 255) / 256 * 256; };
@@ -509,13 +571,15 @@ template <class T = std::complex<float>> class SlicedContractor {
         for (size_t i = 0; i < num_leaves_; ++i)
             if (nodes_[i].chunk)
                 nodes_[i].offset = alloc(nodes_[i].bytes);
-        for (size_t i = 0; i < steps_.size(); ++i) {
-            const Step &s = steps_[i];
-            if (s.chunk)
-                nodes_[s.out].offset = alloc(nodes_[s.out].bytes);
-            for (int id : {s.a, s.b})
-                if (nodes_[id].chunk && last_use[id] == (int)i && id != final_id_)
-                    release(nodes_[id].offset, nodes_[id].bytes);
+        for (size_t it = 0; it < items_.size(); ++it) {
+            for (int i : items_[it].steps)
+                nodes_[steps_[i].out].offset = alloc(nodes_[steps_[i].out].bytes);
+            for (int i : items_[it].steps)
+                for (int id : {steps_[i].a, steps_[i].b})
+                    if (nodes_[id].chunk && last_use[id] == (int)it && id != final_id_) {
+                        release(nodes_[id].offset, nodes_[id].bytes);
+                        last_use[id] = -2; // released once
+                    }
         }
         arena_bytes_ = top;
         arena_ = Gpu::DeviceBuffer(std::max<size_t>(arena_bytes_, 256));
@@ -554,8 +618,118 @@ template <class T = std::complex<float>> class SlicedContractor {
         for (size_t i = 0; i < nodes_.size(); ++i)
             if (!nodes_[i].chunk && persist_[i])
                 nodes_[i].own = Gpu::DeviceBuffer(nodes_[i].bytes);
+        BuildGroups();
         prefix_done_ = false;
         planned_ = true;
+    }
+
+    // Tiny slice-dependent steps that AUTO and TUNED give to the plain
+    // product anyway (and every tiny step in plain FP32): one grouped launch
+    // per run of independent ones.
+    bool Groupable(const Step &st) const
+    {
+        if (!grouping_ || !(precision_ == JETGPU_PREC_FP32 || precision_ == JETGPU_PREC_AUTO ||
+                            precision_ == JETGPU_PREC_TUNED))
+            return false;
+        return (double)st.batch * (double)st.m * (double)st.n * (double)st.k < kGroupMaxWork;
+    }
+
+    // Element offsets, in node X, of every index combination of `labels`
+    // (first label slowest): a product view's batch, row or column table.
+    static std::vector<int64_t> Offsets(const Node &X, const std::vector<std::string> &labels)
+    {
+        std::vector<int64_t> strides(X.dims.size());
+        int64_t st = 1;
+        for (size_t j = X.dims.size(); j-- > 0;) {
+            strides[j] = st;
+            st *= (int64_t)X.dims[j];
+        }
+        std::vector<int64_t> out{0};
+        for (const auto &l : labels) {
+            const size_t p = (size_t)Pos(X.labels, l);
+            std::vector<int64_t> next;
+            next.reserve(out.size() * X.dims[p]);
+            for (int64_t o : out)
+                for (uint64_t d = 0; d < X.dims[p]; ++d)
+                    next.push_back(o + (int64_t)d * strides[p]);
+            out.swap(next);
+        }
+        return out;
+    }
+
+    // Device task tables of the grouped items (offset tables, then tasks).
+    void BuildGroups()
+    {
+        std::vector<int64_t> tables;
+        struct Pending {
+            size_t item;
+            std::vector<std::array<size_t, 6>> table_at; // per task: 6 table offsets
+        };
+        std::vector<Pending> pend;
+        for (size_t it = 0; it < items_.size(); ++it) {
+            if (!items_[it].grouped)
+                continue;
+            Pending p{it, {}};
+            for (int i : items_[it].steps) {
+                const Step &st = steps_[i];
+                const Node &A = nodes_[st.a], &B = nodes_[st.b];
+                const std::vector<std::vector<int64_t>> t6{
+                    Offsets(A, st.hyper), Offsets(A, st.left),   Offsets(A, st.common),
+                    Offsets(B, st.hyper), Offsets(B, st.common), Offsets(B, st.right)};
+                std::array<size_t, 6> at{};
+                for (int q = 0; q < 6; ++q) {
+                    at[q] = tables.size();
+                    tables.insert(tables.end(), t6[q].begin(), t6[q].end());
+                }
+                p.table_at.push_back(at);
+            }
+            pend.push_back(std::move(p));
+        }
+        size_t n_tasks = 0;
+        for (const auto &p : pend)
+            n_tasks += p.table_at.size();
+        const size_t tables_bytes = (tables.size() * sizeof(int64_t) + 255) / 256 * 256;
+        group_buf_ = Gpu::DeviceBuffer(tables_bytes + n_tasks * sizeof(jetgpu_group_task));
+        if (n_tasks == 0)
+            return;
+        const auto *tdev = static_cast<const int64_t *>(group_buf_.get());
+        auto *task_dev = reinterpret_cast<jetgpu_group_task *>(
+            static_cast<char *>(group_buf_.get()) + tables_bytes);
+        std::vector<jetgpu_group_task> tasks;
+        for (const auto &p : pend) {
+            Item &item = items_[p.item];
+            item.tasks = task_dev + tasks.size();
+            item.tiles = 0;
+            for (size_t j = 0; j < item.steps.size(); ++j) {
+                const Step &st = steps_[item.steps[j]];
+                const auto &at = p.table_at[j];
+                jetgpu_group_task q;
+                q.A = Buffer(st.a);
+                q.B = Buffer(st.b);
+                q.C = Buffer(st.out);
+                q.batch = st.batch;
+                q.m = st.m;
+                q.n = st.n;
+                q.k = st.k;
+                q.a_bat = tdev + at[0];
+                q.a_row = tdev + at[1];
+                q.a_col = tdev + at[2];
+                q.b_bat = tdev + at[3];
+                q.b_row = tdev + at[4];
+                q.b_col = tdev + at[5];
+                tasks.push_back(q);
+                item.tiles += jetgpu_group_tiles(st.batch, st.m, st.n);
+            }
+        }
+        void *st = Gpu::Stream();
+        if (!tables.empty())
+            Gpu::Check(jetgpu_memcpy(group_buf_.get(), tables.data(),
+                                     tables.size() * sizeof(int64_t), 0, st),
+                       "group tables");
+        Gpu::Check(jetgpu_memcpy(task_dev, tasks.data(), tasks.size() * sizeof(jetgpu_group_task),
+                                 0, st),
+                   "group tasks");
+        Gpu::Synchronize();
     }
 
     // Runs every step whose output has no "$s" (once per Contract call) and
@@ -647,9 +821,17 @@ template <class T = std::complex<float>> class SlicedContractor {
             if (prof)
                 prof->Mark("gather", -1, batch_, 0, 0, 0);
         }
-        for (const Step &s : steps_)
-            if (s.chunk)
-                Launch(s, st, prof);
+        for (const Item &item : items_) {
+            if (!item.grouped) {
+                Launch(steps_[item.steps[0]], st, prof);
+                continue;
+            }
+            Gpu::Check(jetgpu_contract_group(item.tasks, (int)item.steps.size(), item.tiles, dt,
+                                             st),
+                       "grouped contraction");
+            if (prof)
+                prof->Mark("group", item.steps.front(), item.steps.size(), 0, 0, 0);
+        }
         const void *fin = Buffer(final_id_);
         if (final_perm_needed_) {
             Gpu::Check(jetgpu_permute(fin, final_tmp_.get(), (int)final_shape_.size(),

@@ -213,10 +213,10 @@ def test_profile_chunk_times_every_launch(jet):
     prof = sc.profile_chunk(4)
     kinds = [e["kind"] for e in prof]
     assert kinds.count("slice sum") == 1 and kinds[-1] == "slice sum"
-    assert kinds.count("gather") >= 1 and kinds.count("contract") >= 1
-    assert set(kinds) <= {"gather", "contract", "result reorder", "slice sum"}
+    assert kinds.count("gather") >= 1 and kinds.count("contract") + kinds.count("group") >= 1
+    assert set(kinds) <= {"gather", "contract", "group", "result reorder", "slice sum"}
     assert all(e["ms"] >= 0 for e in prof)
-    steps = [e["step"] for e in prof if e["kind"] == "contract"]
+    steps = [e["step"] for e in prof if e["kind"] in ("contract", "group")]
     assert steps == sorted(steps) and len(set(steps)) == len(steps)
     assert all(0 <= s < len(path) for s in steps)
     with pytest.raises(Exception, match="multiple of the batch size"):
