@@ -500,7 +500,7 @@ template <class T = std::complex<float>> class SlicedContractor {
         {
             std::vector<int> group;
             std::vector<int> group_outs;
-            auto flush = [&] {
+            auto flush = [&] { // a lone step keeps its own launch (split-k, tuned forms)
                 if (group.size() == 1)
                     items_.push_back(Item{group, false});
                 else if (!group.empty())
@@ -625,7 +625,8 @@ template <class T = std::complex<float>> class SlicedContractor {
 
     // Tiny slice-dependent steps that AUTO and TUNED give to the plain
     // product anyway (and every tiny step in plain FP32): one grouped launch
-    // per run of independent ones.
+    // per run of two or more independent ones. (The grouped kernel has no
+    // split-k: a long-k step alone keeps its own launch.)
     bool Groupable(const Step &st) const
     {
         if (!grouping_ || !(precision_ == JETGPU_PREC_FP32 || precision_ == JETGPU_PREC_AUTO ||
