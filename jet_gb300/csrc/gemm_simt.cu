@@ -4,7 +4,8 @@
 // 128-168), which dispatches row-major CBLAS cgemm/zgemm (m, n > 1),
 // cgemv (right labels empty), cgemv^T (left labels empty) and cdotu (both
 // empty) with alpha = 1, beta = 0. Here:
-//  * gemm_kernel: 128x64 (complex64) / 64x64 (complex128) CTA tiles, 8-deep
+//  * gemm_kernel: 128x64 (complex64) / 64x64 (complex128) CTA tiles (32x64
+//    when M <= 32), 8-deep
 //    k slices staged in shared memory with register double buffering, each
 //    thread accumulating an 8x4 (4x4) block of complex outputs with 4 FMAs
 //    per complex multiply-add. Products whose tiles would leave SMs idle
@@ -38,7 +39,7 @@ constexpr int kBK = 8;
 constexpr int kTN = 4;
 constexpr int kTX = 16, kTY = 16; // 256 threads
 
-template <typename T>
+template <typename T, int TM>
 __global__ void __launch_bounds__(256)
     gemm_kernel(const typename C2<T>::type *__restrict__ A,
                 const typename C2<T>::type *__restrict__ B,
@@ -46,7 +47,6 @@ __global__ void __launch_bounds__(256)
                 int64_t K, T scale, int64_t sa, int64_t sb, int splits, int64_t kchunk)
 {
     using V = typename C2<T>::type;
-    constexpr int TM = GemmCfg<T>::TM;
     // blockIdx.z = b * splits + s: batch b (operand strides sa, sb, 0 =
     // shared; C packed) and k range s (splits > 1: [s kchunk, (s + 1)
     // kchunk), partial sums to C + (s * batch + b) * M * N, reduced later).
@@ -323,9 +323,14 @@ int64_t GemmSplits(int64_t ctas, int64_t batch, int64_t K, int64_t out_bytes)
     return s < 2 ? 1 : s;
 }
 
+// Rows per thread of the SIMT product: the full 128 (complex64) / 64
+// (complex128) row tiles, or 32-row tiles when M is at most 32 (skinny
+// products would leave most of a full tile empty).
+template <typename T> inline int GemmTM(int64_t M) { return M <= 32 ? 2 : GemmCfg<T>::TM; }
+
 template <typename T> inline void GemmGrid(int64_t M, int64_t N, int64_t &tiles_n, int64_t &tiles_m)
 {
-    constexpr int BM = GemmCfg<T>::TM * kTY;
+    const int BM = GemmTM<T>(M) * kTY;
     constexpr int BN = kTN * kTX;
     tiles_n = (N + BN - 1) / BN;
     tiles_m = (M + BM - 1) / BM;
@@ -443,7 +448,12 @@ int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename
     const dim3 grid((unsigned)tn, (unsigned)tm, (unsigned)(batch * S));
     JETGPU_REQUIRE(tm <= 65535 && batch * S <= 65535, "product too large for one launch");
     V *dst = S > 1 ? (V *)ws : C;
-    gemm_kernel<T><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa, sb, (int)S, kchunk);
+    if (GemmTM<T>(M) == 2)
+        gemm_kernel<T, 2><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa, sb, (int)S,
+                                                    kchunk);
+    else
+        gemm_kernel<T, GemmCfg<T>::TM><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa,
+                                                                 sb, (int)S, kchunk);
     int rc = CheckLaunch("gemm_kernel");
     if (rc || S == 1)
         return rc;
