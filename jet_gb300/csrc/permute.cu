@@ -104,17 +104,49 @@ int Simplify(int rank, const uint64_t *shape, const int32_t *perm,
 // ---------------------------------------------------------------------------
 struct GatherParams {
     int rank;
+    int narrow;                    // total < 2^32: the 32-bit index path
     uint64_t out_dims[kMaxRank];   // output dims, [rank-1] fastest
     uint64_t in_strides[kMaxRank]; // input element stride of output axis j
     uint64_t size;                 // elements per tensor
     uint64_t total;                // batch * size
+    // Division by out_dims[j] (and by size) on the 32-bit path: multiply and
+    // shift (Granlund-Montgomery invariant divisors); magic 0 means d = 1.
+    uint32_t magic[kMaxRank], shift[kMaxRank];
+    uint32_t size_magic, size_shift;
 };
+
+// n / d for 32-bit n, with (m, s) from Magic32(d): t = hi32(n m),
+// q = (t + (n - t) / 2) >> s (the round-up method; exact for every n < 2^32).
+__device__ __forceinline__ uint32_t DivMagic(uint32_t n, uint32_t m, uint32_t s)
+{
+    if (m == 0)
+        return n;
+    const uint32_t t = __umulhi(n, m);
+    return (t + ((n - t) >> 1)) >> s;
+}
 
 template <typename E>
 __global__ void __launch_bounds__(kThreads)
     gather_kernel(const __grid_constant__ GatherParams p,
                   const E *__restrict__ in, E *__restrict__ out)
 {
+    if (p.narrow) {
+        // Same walk with 32-bit indices and no hardware division.
+        for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.total;
+             idx += (uint64_t)gridDim.x * blockDim.x) {
+            uint32_t o = (uint32_t)idx;
+            const uint32_t b = DivMagic(o, p.size_magic, p.size_shift);
+            o -= b * (uint32_t)p.size;
+            uint32_t src = b * (uint32_t)p.size;
+            for (int j = p.rank - 1; j >= 0; --j) {
+                const uint32_t q = DivMagic(o, p.magic[j], p.shift[j]);
+                src += (o - q * (uint32_t)p.out_dims[j]) * (uint32_t)p.in_strides[j];
+                o = q;
+            }
+            out[idx] = in[src];
+        }
+        return;
+    }
     for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
          idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t b = idx / p.size;
@@ -261,6 +293,22 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Multiplier and shift for dividing 32-bit values by d (d = 1: magic 0):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, s = l - 1.
+void Magic32(uint64_t d, uint32_t &m, uint32_t &sh)
+{
+    if (d <= 1) {
+        m = 0;
+        sh = 0;
+        return;
+    }
+    int l = 0;
+    while ((1ull << l) < d)
+        ++l;
+    m = (uint32_t)(((((1ull << l) - d) << 32) / d) + 1);
+    sh = (uint32_t)(l - 1);
+}
+
 void BuildGather(const Simplified &s, uint64_t batch, GatherParams &p)
 {
     int r = (int)s.dims.size();
@@ -275,6 +323,12 @@ void BuildGather(const Simplified &s, uint64_t batch, GatherParams &p)
     }
     p.size = s.size;
     p.total = s.size * batch;
+    p.narrow = p.total < (1ull << 32) ? 1 : 0;
+    if (p.narrow) {
+        for (int j = 0; j < r; ++j)
+            Magic32(p.out_dims[j], p.magic[j], p.shift[j]);
+        Magic32(p.size, p.size_magic, p.size_shift);
+    }
 }
 
 // ---------------------------------------------------------------------------
