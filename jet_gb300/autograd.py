@@ -179,3 +179,47 @@ def contract_network(leaves: Sequence[torch.Tensor], labels: Sequence[Sequence[s
     if plan is None:
         plan = ContractionPlan(labels, [list(l.shape) for l in leaves], path)
     return _NetworkContraction.apply(plan, precision, *leaves)
+
+
+class GraphedStep:
+    """A loss-and-gradient evaluation captured once in a CUDA graph and
+    replayed: `loss_fn()` must build its inputs from fixed tensors (the
+    parameters) and return a real scalar; `params` are the leaf tensors whose
+    `.grad` the backward fills.
+
+    Every contraction, conjugation and transpose of the network (and torch's
+    own kernels around it) is a node of one graph, so a replay costs no
+    per-step host work: the per-step Python and launch overhead of the eager
+    path (several launches per contraction, hundreds of steps) disappears.
+    Shapes and the path are fixed at capture; to evaluate at new parameter
+    values, copy them into `params` (in place) before `step()`.
+
+    Capture happens after `warmup` eager evaluations on a side stream (the
+    first launches of each kernel configure it, which must not happen inside
+    a capture)."""
+
+    def __init__(self, loss_fn, params: Sequence[torch.Tensor], warmup: int = 2):
+        self.loss_fn = loss_fn
+        self.params = list(params)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(max(1, warmup)):
+                for p in self.params:
+                    p.grad = None
+                loss_fn().backward()
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        for p in self.params:
+            p.grad = None
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = loss_fn()
+            self.loss.backward()
+        self.grads = [p.grad for p in self.params]
+
+    def step(self):
+        """Replays the graph: returns the loss tensor; the gradients are in
+        `self.grads` (the params' `.grad`, overwritten by every replay)."""
+        self.graph.replay()
+        return self.loss
