@@ -749,8 +749,10 @@ def run_grad(args, rank, world, local_rank):
 
     # The same evaluation captured once in a CUDA graph (autograd.GraphedStep)
     # and replayed: no per-step host work.
+    consts = {}
+
     def loss_fn():
-        lv = ex.build_leaves(spec, t, p, dtype=torch.complex64, device=dev)
+        lv = ex.build_leaves(spec, t, p, dtype=torch.complex64, device=dev, const_cache=consts)
         return autograd.contract_network(lv, labels, path, precision=jet.PREC_AUTO,
                                          plan=plan).real
 

@@ -105,16 +105,26 @@ def numeric_network(leaves: Sequence[Leaf], thetas: np.ndarray, phis: np.ndarray
     return circuits.Network(out)
 
 
-def build_leaves(leaves: Sequence[Leaf], thetas, phis, dtype=None, device=None):
-    """torch leaves as differentiable functions of the angle tensors."""
+def build_leaves(leaves: Sequence[Leaf], thetas, phis, dtype=None, device=None,
+                 const_cache=None):
+    """torch leaves as differentiable functions of the angle tensors.
+
+    const_cache (a dict, optional) keeps the angle-independent leaves on the
+    device between calls, so a call makes no host-to-device copy (required
+    inside a CUDA graph capture)."""
     import torch
 
     dtype = dtype or torch.complex64
     real = torch.float32 if dtype == torch.complex64 else torch.float64
     out = []
-    for lf in leaves:
+    for i, lf in enumerate(leaves):
         if lf.kind == "const":
-            t = torch.as_tensor(lf.data, dtype=dtype, device=device).reshape(lf.shape)
+            key = (i, str(dtype), str(device))
+            t = None if const_cache is None else const_cache.get(key)
+            if t is None:
+                t = torch.as_tensor(lf.data, dtype=dtype, device=device).reshape(lf.shape)
+                if const_cache is not None:
+                    const_cache[key] = t
         else:
             ang = (thetas if lf.kind == "rx" else phis)[lf.layer, lf.qubit].to(real)
             c, s = torch.cos(ang / 2), torch.sin(ang / 2)

@@ -121,8 +121,10 @@ def test_graphed_step_matches_eager(cuda):
     t = torch.tensor(th, dtype=torch.float32, device=cuda, requires_grad=True)
     p = torch.tensor(ph, dtype=torch.float32, device=cuda, requires_grad=True)
 
+    consts = {}
+
     def loss_fn():
-        lv = ex.build_leaves(spec, t, p, dtype=torch.complex64, device=cuda)
+        lv = ex.build_leaves(spec, t, p, dtype=torch.complex64, device=cuda, const_cache=consts)
         return autograd.contract_network(lv, labels, path, precision=2, plan=plan).real
 
     def eager():
