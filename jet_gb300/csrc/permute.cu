@@ -125,41 +125,43 @@ __device__ __forceinline__ uint32_t DivMagic(uint32_t n, uint32_t m, uint32_t s)
     return (t + ((n - t) >> 1)) >> s;
 }
 
+// Input offset of output element idx: the mixed-radix walk over the output
+// dims, in 32-bit indices with multiply-shift division when the tensor has
+// fewer than 2^32 elements, else in 64 bits.
+__device__ __forceinline__ uint64_t GatherSrc(const GatherParams &p, uint64_t idx)
+{
+    if (p.narrow) {
+        uint32_t o = (uint32_t)idx;
+        const uint32_t b = DivMagic(o, p.size_magic, p.size_shift);
+        o -= b * (uint32_t)p.size;
+        uint32_t src = b * (uint32_t)p.size;
+        for (int j = p.rank - 1; j >= 0; --j) {
+            const uint32_t q = DivMagic(o, p.magic[j], p.shift[j]);
+            src += (o - q * (uint32_t)p.out_dims[j]) * (uint32_t)p.in_strides[j];
+            o = q;
+        }
+        return src;
+    }
+    const uint64_t b = idx / p.size;
+    uint64_t o = idx - b * p.size;
+    uint64_t src = b * p.size;
+    for (int j = p.rank - 1; j >= 0; --j) {
+        const uint64_t d = p.out_dims[j];
+        const uint64_t q = o / d;
+        src += (o - q * d) * p.in_strides[j];
+        o = q;
+    }
+    return src;
+}
+
 template <typename E>
 __global__ void __launch_bounds__(kThreads)
     gather_kernel(const __grid_constant__ GatherParams p,
                   const E *__restrict__ in, E *__restrict__ out)
 {
-    if (p.narrow) {
-        // Same walk with 32-bit indices and no hardware division.
-        for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.total;
-             idx += (uint64_t)gridDim.x * blockDim.x) {
-            uint32_t o = (uint32_t)idx;
-            const uint32_t b = DivMagic(o, p.size_magic, p.size_shift);
-            o -= b * (uint32_t)p.size;
-            uint32_t src = b * (uint32_t)p.size;
-            for (int j = p.rank - 1; j >= 0; --j) {
-                const uint32_t q = DivMagic(o, p.magic[j], p.shift[j]);
-                src += (o - q * (uint32_t)p.out_dims[j]) * (uint32_t)p.in_strides[j];
-                o = q;
-            }
-            out[idx] = in[src];
-        }
-        return;
-    }
-    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-         idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t b = idx / p.size;
-        uint64_t o = idx - b * p.size;
-        uint64_t src = b * p.size;
-        for (int j = p.rank - 1; j >= 0; --j) {
-            uint64_t d = p.out_dims[j];
-            uint64_t q = o / d;
-            src += (o - q * d) * p.in_strides[j];
-            o = q;
-        }
-        out[idx] = in[src];
-    }
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.total;
+         idx += (uint64_t)gridDim.x * blockDim.x)
+        out[idx] = in[GatherSrc(p, idx)];
 }
 
 // TF32 rounding to nearest (ties away from zero) by adding half a unit in the
@@ -278,19 +280,9 @@ __global__ void __launch_bounds__(kThreads)
     gather_split_kernel(const __grid_constant__ GatherParams p,
                         const float2 *__restrict__ in, SplitOut so)
 {
-    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-         idx < p.total; idx += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t b = idx / p.size;
-        uint64_t o = idx - b * p.size;
-        uint64_t src = b * p.size;
-        for (int j = p.rank - 1; j >= 0; --j) {
-            uint64_t d = p.out_dims[j];
-            uint64_t q = o / d;
-            src += (o - q * d) * p.in_strides[j];
-            o = q;
-        }
-        WriteSplit(so, idx, in[src]);
-    }
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.total;
+         idx += (uint64_t)gridDim.x * blockDim.x)
+        WriteSplit(so, idx, in[GatherSrc(p, idx)]);
 }
 
 // Multiplier and shift for dividing 32-bit values by d (d = 1: magic 0):
