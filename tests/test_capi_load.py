@@ -152,3 +152,25 @@ def test_tuned_precision_accepted_and_workspace_covers_every_form():
     assert rc == capi.ERR_INVALID and b"bad precision" in capi.lib.jetgpu_last_error()
     assert capi.lib.jetgpu_autotune_count() == 0
     assert capi.lib.jetgpu_autotune_entry(0, None, None, None, None, None) == capi.ERR_INVALID
+
+
+def test_group_offset_tables_match_numpy_views():
+    """capi.view_offsets (the grouped launch's batch / row / column tables):
+    element (b, i, j) of a view is the tensor's flat element at
+    bat[b] + row[i] + col[j], as numpy's transpose + reshape says."""
+    import numpy as np
+
+    from jet_gb300 import capi
+
+    rng = np.random.default_rng(4)
+    for shape in ([3, 2, 4, 5], [2, 2, 2, 2, 2, 2], [7, 1, 3], [6]):
+        x = np.arange(int(np.prod(shape))).reshape(shape)
+        axes = list(rng.permutation(len(shape)))
+        cut1 = int(rng.integers(0, len(axes) + 1))
+        cut2 = int(rng.integers(cut1, len(axes) + 1))
+        g = [axes[:cut1], axes[cut1:cut2], axes[cut2:]]
+        bat, row, col = (capi.view_offsets(shape, a) for a in g)
+        view = np.transpose(x, g[0] + g[1] + g[2]).reshape(len(bat), len(row), len(col))
+        flat = x.reshape(-1)
+        got = flat[bat[:, None, None] + row[None, :, None] + col[None, None, :]]
+        assert np.array_equal(got, view)
