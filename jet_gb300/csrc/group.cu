@@ -52,8 +52,8 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16; // 2 x 2 outputs each
+    int t = 0; // this CTA's tiles come in increasing order: the task only advances
     for (uint64_t g = blockIdx.x; g < total_tiles; g += gridDim.x) {
-        int t = 0;
         while (t + 1 < n_tasks && first_tile[t + 1] <= g)
             ++t;
         const jetgpu_group_task &q = tasks[t];
