@@ -4,8 +4,8 @@
 // The reference runs every path step as its own ContractTensors call
 // (Tensor.hpp:708-752: two transposes, then one BLAS call). For the many small
 // slice-dependent steps of a sliced network that is one to three launches per
-// step, each too small to fill the GPU. Here the steps of one level of the
-// path's dependency tree (no step reads another's output) go into one launch.
+// step, each too small to fill the GPU. Here a run of such steps that do not
+// read each other's outputs goes into one launch.
 // Each operand is read through offset tables instead of a transpose pass:
 // element (b, i, j) of the product's view of A is A[a_bat[b] + a_row[i] +
 // a_col[j]], so any permutation of the operand's axes and any placement of
