@@ -174,3 +174,40 @@ def test_group_offset_tables_match_numpy_views():
         flat = x.reshape(-1)
         got = flat[bat[:, None, None] + row[None, :, None] + col[None, None, :]]
         assert np.array_equal(got, view)
+
+
+def test_batched_operand_forms_are_checked_on_the_host():
+    """a_batched / b_batched take 0, 1 or 2; in form 2 the permutation must
+    lead with axes whose extents multiply to the batch (host checks, no
+    device work)."""
+    from jet_gb300 import capi
+
+    shape = [2, 4, 3, 5]  # batch 2 at axis 0 in the layout below
+    a_perm_ok = [0, 1, 2, 3]
+    args = lambda a_batched, a_perm: (2, None, 4, capi.u64(shape), capi.i32(a_perm), a_batched,
+                                      None, 2, capi.u64([5, 6]), capi.i32([0, 1]), 0, None,
+                                      12, 6, 5, capi.C64, 0, capi.ALGO_4M, 0, 0, None, 0, None)
+    rc = capi.lib.jetgpu_contract_batched(*args(3, a_perm_ok))
+    assert rc == capi.ERR_INVALID and b"batched flags" in capi.lib.jetgpu_last_error()
+    # Form 2 with a permutation that leads with the 4-axis: no batch split.
+    rc = capi.lib.jetgpu_contract_batched(*args(2, [1, 0, 2, 3]))
+    assert rc == capi.ERR_INVALID
+
+
+def test_tensor_core_settings_reject_out_of_range_values():
+    from jet_gb300 import capi
+
+    assert capi.lib.jetgpu_set_tc_group_m(0) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_set_tc_group_m(1025) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_set_tc_persistent(2) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_set_tc_group_m(8) == capi.OK
+    assert capi.lib.jetgpu_set_tc_persistent(1) == capi.OK
+
+
+def test_group_launch_checks_on_the_host():
+    from jet_gb300 import capi
+
+    assert capi.lib.jetgpu_contract_group(None, 257, 1, capi.C64, None) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_contract_group(None, 0, 0, capi.C64, None) == capi.OK
+    assert capi.lib.jetgpu_contract_group(None, 1, 1, 7, None) == capi.ERR_INVALID
+    assert capi.lib.jetgpu_group_tiles(3, 33, 64) == 3 * 2 * 2
