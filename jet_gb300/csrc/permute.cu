@@ -285,6 +285,231 @@ __global__ void __launch_bounds__(kThreads)
         WriteSplit(so, idx, in[GatherSrc(p, idx)]);
 }
 
+// ---------------------------------------------------------------------------
+// Tiled permute for any dims (the non-power-of-2 path).
+//
+// A tile is every index combination of a set U of axes: the innermost input
+// axes (I) until their extent reaches a threshold, joined with the input
+// axes that become the innermost output axes (O), so T = prod_{a in U} dim(a)
+// elements (at most kTileMax). The other axes (and the batch) enumerate the
+// tiles. A CTA reads its tile in input order, where the I axes vary fastest
+// (runs of at least the threshold's contiguous elements), places each element
+// at its output-order position in shared memory, and writes the tile in
+// output order, where the O axes vary fastest. in_off[e] / out_off[f] are the
+// element offsets of tile element e (input order) / f (output order) from the
+// tile's bases; pos[e] is e's output-order position. The gather kernel reads
+// one scattered element per output element; this reads and writes runs.
+// ---------------------------------------------------------------------------
+constexpr int kTileMax = 1024;
+
+struct TileParams {
+    int nr;          // tile-enumerating axes (batch first)
+    int T;           // elements per tile
+    int G;           // tiles per pass of a CTA (G * T elements fill at most 32 KB)
+    uint32_t t_magic, t_shift; // division by T (DivMagic)
+    uint64_t tiles;
+    uint64_t r_dims[kMaxRank + 1];
+    uint64_t r_in[kMaxRank + 1];  // input element stride of each
+    uint64_t r_out[kMaxRank + 1]; // output element stride of each
+    uint32_t r_magic[kMaxRank + 1], r_shift[kMaxRank + 1]; // division by r_dims
+    int narrow;                   // tiles < 2^32: 32-bit tile decode
+    int32_t in_off[kTileMax];
+    int32_t out_off[kTileMax];
+    uint16_t pos[kTileMax];
+};
+
+constexpr int kTileGroupMax = kThreads; // tiles per pass (one base per thread)
+constexpr int kTileSlotBytes = 32768;    // shared memory for one pass's elements
+
+// Tile bases: tile t decoded over the enumerating axes (last fastest).
+__device__ __forceinline__ void TileBases(const TileParams &p, uint64_t t, uint64_t &bi,
+                                          uint64_t &bo)
+{
+    bi = 0;
+    bo = 0;
+    if (p.narrow) {
+        uint32_t x = (uint32_t)t;
+        for (int a = p.nr - 1; a >= 0; --a) {
+            const uint32_t q = DivMagic(x, p.r_magic[a], p.r_shift[a]);
+            const uint64_t c = x - q * (uint32_t)p.r_dims[a];
+            bi += c * p.r_in[a];
+            bo += c * p.r_out[a];
+            x = q;
+        }
+        return;
+    }
+    for (int a = p.nr - 1; a >= 0; --a) {
+        const uint64_t d = p.r_dims[a];
+        const uint64_t q = t / d;
+        const uint64_t c = t - q * d;
+        bi += c * p.r_in[a];
+        bo += c * p.r_out[a];
+        t = q;
+    }
+}
+
+template <typename E> struct TilePlainStore {
+    E *out;
+    __device__ __forceinline__ void operator()(uint64_t o, const E &v) const { out[o] = v; }
+};
+
+struct TileSplitStore {
+    SplitOut so;
+    __device__ __forceinline__ void operator()(uint64_t o, const uint2 &v) const
+    {
+        WriteSplit(so, o, make_float2(__uint_as_float(v.x), __uint_as_float(v.y)));
+    }
+};
+
+// Each pass moves G consecutive tiles (G * T elements, up to 32 KB) through
+// shared memory: slot u holds element u mod T of the pass's tile u / T.
+template <typename E, typename Store>
+__global__ void __launch_bounds__(kThreads)
+    tile_permute_kernel(const __grid_constant__ TileParams p, const E *__restrict__ in, Store store)
+{
+    __shared__ E tile[kTileSlotBytes / sizeof(E)];
+    __shared__ uint64_t base_in[kTileGroupMax], base_out[kTileGroupMax];
+    // The offset tables move to shared memory once: indexed per thread, a
+    // kernel-parameter array would serialise every warp's load.
+    __shared__ int32_t in_off[kTileMax], out_off[kTileMax];
+    __shared__ uint16_t pos[kTileMax];
+    for (int e = threadIdx.x; e < p.T; e += blockDim.x) {
+        in_off[e] = p.in_off[e];
+        out_off[e] = p.out_off[e];
+        pos[e] = p.pos[e];
+    }
+    const uint64_t passes = (p.tiles + p.G - 1) / p.G;
+    for (uint64_t ps = blockIdx.x; ps < passes; ps += gridDim.x) {
+        const uint64_t t0 = ps * p.G;
+        const int g = (int)min((uint64_t)p.G, p.tiles - t0);
+        if ((int)threadIdx.x < g)
+            TileBases(p, t0 + threadIdx.x, base_in[threadIdx.x], base_out[threadIdx.x]);
+        __syncthreads();
+        const int n = g * p.T;
+#pragma unroll 4
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
+            const int e = u - j * p.T;
+            tile[j * p.T + pos[e]] = in[base_in[j] + (uint64_t)in_off[e]];
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
+            const int f = u - j * p.T;
+            store(base_out[j] + (uint64_t)out_off[f], tile[u]);
+        }
+        __syncthreads();
+    }
+}
+
+void Magic32(uint64_t d, uint32_t &m, uint32_t &sh);
+
+// The tile plan of a simplified permutation (false: no tile of at most
+// kTileMax elements, or offsets past 32 bits; the gather kernel then runs).
+bool BuildTile(const Simplified &s, uint64_t batch, size_t elem_bytes, TileParams &p)
+{
+    const int r = (int)s.dims.size();
+    if (r < 2)
+        return false;
+    std::vector<uint64_t> in_stride(r, 1);
+    for (int i = r - 2; i >= 0; --i)
+        in_stride[i] = in_stride[i + 1] * s.dims[i + 1];
+    std::vector<uint64_t> out_stride(r); // output stride of input axis a
+    {
+        uint64_t st = 1;
+        for (int j = r - 1; j >= 0; --j) {
+            out_stride[s.perm[j]] = st;
+            st *= s.dims[s.perm[j]];
+        }
+    }
+    for (uint64_t thr : {32ull, 16ull, 8ull}) {
+        std::vector<char> in_u(r, 0);
+        uint64_t pi = 1;
+        for (int a = r - 1; a >= 0 && pi < thr; --a) {
+            in_u[a] = 1;
+            pi *= s.dims[a];
+        }
+        uint64_t po = 1;
+        for (int j = r - 1; j >= 0 && po < thr; --j) {
+            in_u[s.perm[j]] = 1;
+            po *= s.dims[s.perm[j]];
+        }
+        uint64_t T = 1;
+        for (int a = 0; a < r; ++a)
+            if (in_u[a])
+                T *= s.dims[a];
+        if (T > (uint64_t)kTileMax)
+            continue;
+        std::vector<int> u_in, u_out;
+        for (int a = 0; a < r; ++a)
+            if (in_u[a])
+                u_in.push_back(a);
+        for (int j = 0; j < r; ++j)
+            if (in_u[s.perm[j]])
+                u_out.push_back(s.perm[j]);
+        std::vector<uint64_t> fstride(r, 0);
+        {
+            uint64_t st = 1;
+            for (int i = (int)u_out.size() - 1; i >= 0; --i) {
+                fstride[u_out[i]] = st;
+                st *= s.dims[u_out[i]];
+            }
+        }
+        std::memset(&p, 0, sizeof(p));
+        p.T = (int)T;
+        std::vector<uint64_t> c(r, 0);
+        for (uint64_t e = 0; e < T; ++e) {
+            uint64_t x = e, io = 0, oo = 0, f = 0;
+            for (int i = (int)u_in.size() - 1; i >= 0; --i) {
+                const int a = u_in[i];
+                const uint64_t ca = x % s.dims[a];
+                x /= s.dims[a];
+                io += ca * in_stride[a];
+                oo += ca * out_stride[a];
+                f += ca * fstride[a];
+            }
+            if (io > 0x7fffffffull || oo > 0x7fffffffull)
+                return false;
+            p.in_off[e] = (int32_t)io;
+            p.pos[e] = (uint16_t)f;
+            p.out_off[f] = (int32_t)oo;
+        }
+        int nr = 0;
+        if (batch > 1) {
+            p.r_dims[nr] = batch;
+            p.r_in[nr] = s.size;
+            p.r_out[nr] = s.size;
+            ++nr;
+        }
+        for (int a = 0; a < r; ++a)
+            if (!in_u[a]) {
+                p.r_dims[nr] = s.dims[a];
+                p.r_in[nr] = in_stride[a];
+                p.r_out[nr] = out_stride[a];
+                ++nr;
+            }
+        p.nr = nr;
+        p.tiles = (s.size / T) * batch;
+        p.narrow = p.tiles < (1ull << 32) ? 1 : 0;
+        for (int a = 0; a < nr; ++a)
+            Magic32(p.r_dims[a], p.r_magic[a], p.r_shift[a]);
+        p.G = (int)std::min<uint64_t>(
+            {(uint64_t)kTileSlotBytes / elem_bytes / T, (uint64_t)kTileGroupMax, p.tiles});
+        Magic32(T, p.t_magic, p.t_shift);
+        return true;
+    }
+    return false;
+}
+
+template <typename E, typename Store>
+int LaunchTile(const TileParams &p, const void *in, Store store, cudaStream_t stream)
+{
+    const unsigned grid = GridFor((p.tiles + p.G - 1) / p.G, 4);
+    tile_permute_kernel<E, Store><<<grid, kThreads, 0, stream>>>(p, (const E *)in, store);
+    return CheckLaunch("tile_permute_kernel");
+}
+
 // Multiplier and shift for dividing 32-bit values by d (d = 1: magic 0):
 // l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, s = l - 1.
 void Magic32(uint64_t d, uint32_t &m, uint32_t &sh)
@@ -642,6 +867,13 @@ int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
                                            PlainStore<uint4>{(uint4 *)out},
                                            stream);
     }
+    {
+        static thread_local TileParams tp; // ~12 KB: keep off the stack
+        if (BuildTile(s, batch, dtype == JETGPU_C64 ? 8 : 16, tp))
+            return dtype == JETGPU_C64
+                       ? LaunchTile<uint2>(tp, in, TilePlainStore<uint2>{(uint2 *)out}, stream)
+                       : LaunchTile<uint4>(tp, in, TilePlainStore<uint4>{(uint4 *)out}, stream);
+    }
     GatherParams gp;
     BuildGather(s, batch, gp);
     unsigned grid = GridFor((gp.total + kThreads - 1) / kThreads, 8);
@@ -706,6 +938,11 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
     static thread_local BitParams bp;
     if (aligned && IsPow2(cols) && cols >= 2 && BuildBitParams(s, batch, 1, bp))
         return LaunchBitperm<uint2, 1>(bp, in, SplitStore{so}, stream);
+    {
+        static thread_local TileParams tp;
+        if (BuildTile(s, batch, 8, tp))
+            return LaunchTile<uint2>(tp, in, TileSplitStore{so}, stream);
+    }
     GatherParams gp;
     BuildGather(s, batch, gp);
     unsigned grid = GridFor((gp.total + kThreads - 1) / kThreads, 8);
