@@ -318,6 +318,10 @@ struct TileParams {
     uint16_t pos[kTileMax];
 };
 
+// Below this many elements (per launch) the gather kernel runs: a small
+// permute is bound by its launch, and the tile plan's 12 KB parameter block and
+// host-side tables would only add to that.
+constexpr uint64_t kTileMinElements = 1ull << 15;
 constexpr int kTileGroupMax = kThreads; // tiles per pass (one base per thread)
 constexpr int kTileSlotBytes = 32768;    // shared memory for one pass's elements
 
@@ -869,7 +873,8 @@ int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
     }
     {
         static thread_local TileParams tp; // ~12 KB: keep off the stack
-        if (BuildTile(s, batch, dtype == JETGPU_C64 ? 8 : 16, tp))
+        if (s.size * batch >= kTileMinElements &&
+            BuildTile(s, batch, dtype == JETGPU_C64 ? 8 : 16, tp))
             return dtype == JETGPU_C64
                        ? LaunchTile<uint2>(tp, in, TilePlainStore<uint2>{(uint2 *)out}, stream)
                        : LaunchTile<uint4>(tp, in, TilePlainStore<uint4>{(uint4 *)out}, stream);
@@ -940,7 +945,7 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
         return LaunchBitperm<uint2, 1>(bp, in, SplitStore{so}, stream);
     {
         static thread_local TileParams tp;
-        if (BuildTile(s, batch, 8, tp))
+        if (s.size * batch >= kTileMinElements && BuildTile(s, batch, 8, tp))
             return LaunchTile<uint2>(tp, in, TileSplitStore{so}, stream);
     }
     GatherParams gp;

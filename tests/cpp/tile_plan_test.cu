@@ -1,0 +1,139 @@
+// Host-side check of the tiled permute's plan (jet_gb300/csrc/permute.cu):
+// the kernel's passes are replayed on the CPU over random shapes (dims 1..10,
+// ranks 1..6, batches 1..3) and both element sizes, with input element i
+// holding i, and the result compared with the plain row-major permutation
+// (output axis j = input axis perm[j], the convention of the reference's
+// Permuter, include/jet/permute/Permuter.hpp:36-80). The replay checks every
+// shared-memory slot and global offset against its buffer, that no output is
+// written twice, and that the 32-bit multiply-shift divisions the kernel uses
+// equal plain division.
+#include "../../jet_gb300/csrc/permute.cu"
+
+#include <cstdio>
+#include <random>
+
+using namespace jetgpu;
+
+namespace {
+
+uint32_t Div(uint32_t n, uint32_t m, uint32_t s)
+{
+    if (m == 0)
+        return n;
+    const uint32_t t = (uint32_t)(((uint64_t)n * m) >> 32);
+    return (t + ((n - t) >> 1)) >> s;
+}
+
+#define FAIL(...)                                                                                  \
+    do {                                                                                           \
+        std::printf(__VA_ARGS__);                                                                  \
+        return 1;                                                                                  \
+    } while (0)
+
+int Replay(const TileParams &tp, size_t eb, uint64_t total, std::vector<uint64_t> &got)
+{
+    const size_t slots = kTileSlotBytes / eb;
+    if (tp.T < 1 || tp.T > kTileMax || tp.G < 1 || tp.G > kTileGroupMax ||
+        (size_t)tp.G * tp.T > slots)
+        FAIL("bad tile shape T=%d G=%d\n", tp.T, tp.G);
+    if (!tp.narrow)
+        FAIL("expected the 32-bit tile decode\n");
+    std::vector<uint64_t> tile(slots), bin(tp.G), bout(tp.G);
+    const uint64_t passes = (tp.tiles + tp.G - 1) / tp.G;
+    for (uint64_t ps = 0; ps < passes; ++ps) {
+        const uint64_t t0 = ps * tp.G;
+        const int g = (int)std::min<uint64_t>(tp.G, tp.tiles - t0);
+        for (int j = 0; j < g; ++j) {
+            uint64_t bi = 0, bo = 0;
+            uint32_t x = (uint32_t)(t0 + j);
+            for (int a = tp.nr - 1; a >= 0; --a) {
+                const uint32_t q = Div(x, tp.r_magic[a], tp.r_shift[a]);
+                if (q != x / tp.r_dims[a])
+                    FAIL("tile decode division\n");
+                const uint64_t c = x - q * (uint32_t)tp.r_dims[a];
+                bi += c * tp.r_in[a];
+                bo += c * tp.r_out[a];
+                x = q;
+            }
+            bin[j] = bi;
+            bout[j] = bo;
+        }
+        const int n = g * tp.T;
+        for (int u = 0; u < n; ++u) {
+            const int j = (int)Div((uint32_t)u, tp.t_magic, tp.t_shift);
+            if (j != u / tp.T)
+                FAIL("slot division\n");
+            const int e = u - j * tp.T;
+            const uint64_t src = bin[j] + (uint64_t)tp.in_off[e];
+            const size_t slot = (size_t)j * tp.T + tp.pos[e];
+            if (src >= total || tp.pos[e] >= tp.T || slot >= slots)
+                FAIL("read out of range\n");
+            tile[slot] = src;
+        }
+        for (int u = 0; u < n; ++u) {
+            const int j = (int)Div((uint32_t)u, tp.t_magic, tp.t_shift);
+            const int f = u - j * tp.T;
+            const uint64_t dst = bout[j] + (uint64_t)tp.out_off[f];
+            if (dst >= total)
+                FAIL("write out of range\n");
+            if (got[dst] != ~0ull)
+                FAIL("output %llu written twice\n", (unsigned long long)dst);
+            got[dst] = tile[u];
+        }
+    }
+    return 0;
+}
+
+} // namespace
+
+int main()
+{
+    std::mt19937_64 rng(7);
+    int planned = 0, cases = 0;
+    static TileParams tp;
+    for (int trial = 0; trial < 3000; ++trial) {
+        const int rank = 1 + (int)(rng() % 6);
+        std::vector<uint64_t> shape(rank);
+        uint64_t size = 1;
+        for (auto &d : shape) {
+            d = 1 + rng() % 10;
+            size *= d;
+        }
+        if (size > 200000)
+            continue;
+        std::vector<int32_t> perm(rank);
+        for (int i = 0; i < rank; ++i)
+            perm[i] = i;
+        std::shuffle(perm.begin(), perm.end(), rng);
+        const uint64_t batch = 1 + rng() % 3;
+        const size_t eb = (trial & 1) ? 8 : 16;
+        Simplified s;
+        if (Simplify(rank, shape.data(), perm.data(), s))
+            FAIL("simplify failed\n");
+        ++cases;
+        if (!BuildTile(s, batch, eb, tp))
+            continue;
+        ++planned;
+        std::vector<uint64_t> ref(size * batch), got(size * batch, ~0ull);
+        std::vector<uint64_t> stride(rank, 1);
+        for (int i = rank - 2; i >= 0; --i)
+            stride[i] = stride[i + 1] * shape[i + 1];
+        for (uint64_t b = 0; b < batch; ++b)
+            for (uint64_t o = 0; o < size; ++o) {
+                uint64_t x = o, src = 0;
+                for (int j = rank - 1; j >= 0; --j) {
+                    src += (x % shape[perm[j]]) * stride[perm[j]];
+                    x /= shape[perm[j]];
+                }
+                ref[b * size + o] = b * size + src;
+            }
+        if (Replay(tp, eb, size * batch, got))
+            FAIL("  (trial %d)\n", trial);
+        if (got != ref)
+            FAIL("mismatch in trial %d\n", trial);
+    }
+    if (planned < cases / 2)
+        FAIL("only %d of %d cases planned\n", planned, cases);
+    std::printf("ok %d of %d cases tiled\n", planned, cases);
+    return 0;
+}

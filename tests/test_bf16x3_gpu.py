@@ -81,11 +81,13 @@ def _config1_data(rng, rows, cols):
 
 
 @pytest.mark.parametrize("shape,perm", [([2] * 12, None), ([3, 5, 7, 4], [2, 0, 3, 1]),
-                                        ([16, 8], [1, 0])])
+                                        ([16, 8], [1, 0]), ([3] * 10, None),
+                                        ([6, 9, 5, 7, 20], [3, 1, 4, 0, 2])])
 def test_split_bf16_bit_exact(cuda, shape, perm):
     """Planes equal the rounding model word for word, on random values,
     exact rounding ties (low 16 bits 0x8000), zeros and FP32 subnormals; both
-    the bit-permutation kernel (power-of-2 shapes) and the gather kernel."""
+    the bit-permutation kernel (power-of-2 shapes) and the tiled kernel
+    (other dims)."""
     import torch
 
     from jet_gb300 import capi

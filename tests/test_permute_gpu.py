@@ -80,6 +80,34 @@ def test_mixed_shapes_vs_oracle(cuda, shape):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("shape,batch,dtype", [([3] * 12, 1, np.complex64), ([3] * 11, 1, np.complex128),
+                                               ([9, 5, 7, 3, 11, 4], 1, np.complex64),
+                                               ([6] * 7, 1, np.complex128), ([3] * 10, 3, np.complex64),
+                                               ([5, 2, 9, 2, 3, 7, 2], 4, np.complex128),
+                                               ([1000, 3, 7, 2], 1, np.complex64),
+                                               ([3] * 8, 3, np.complex64)])
+def test_non_pow2_tiled_vs_oracle(cuda, shape, batch, dtype):
+    """Non-power-of-2 dims of at least 2^15 elements per launch take the tiled
+    kernel (several tiles per pass of a CTA, batches enumerated with the
+    tiles); smaller ones, and shapes whose innermost axes are too long for a
+    tile of at most 1024 elements, take the gather kernel. Bit-exact against
+    the oracle's transpose for each batch item."""
+    from jet_gb300 import capi
+
+    r = len(shape)
+    lab = cases.labels(r)
+    size = int(np.prod(shape))
+    for rep in range(2):
+        seed = 61000 + 13 * r + rep
+        perm = cases.permutation(seed, r)
+        x = cases.tensor_data(seed, [batch * size], dtype)
+        got = capi.permute(_to_dev(x, cuda), shape, perm, batch=batch).cpu().numpy()
+        for b in range(batch):
+            want = jo.transpose(jo.OTensor.make(lab, shape, x[b * size:(b + 1) * size], dtype),
+                                [lab[i] for i in perm]).data
+            assert np.array_equal(got[b * size:(b + 1) * size], want), b
+
+
 def test_batched_permute(cuda):
     from jet_gb300 import capi
 
