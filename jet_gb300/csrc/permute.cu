@@ -313,15 +313,15 @@ struct TileParams {
     uint64_t r_out[kMaxRank + 1]; // output element stride of each
     uint32_t r_magic[kMaxRank + 1], r_shift[kMaxRank + 1]; // division by r_dims
     int narrow;                   // tiles < 2^32: 32-bit tile decode
-    int32_t in_off[kTileMax];
-    int32_t out_off[kTileMax];
-    uint16_t pos[kTileMax];
+    alignas(16) int32_t in_off[kTileMax];
+    alignas(16) int32_t out_off[kTileMax];
+    alignas(16) uint16_t pos[kTileMax];
 };
 
 // Below this many elements (per launch) the gather kernel runs: a small
 // permute is bound by its launch, and the tile plan's 12 KB parameter block and
 // host-side tables would only add to that.
-constexpr uint64_t kTileMinElements = 1ull << 15;
+constexpr uint64_t kTileMinElements = 1ull << 18;
 constexpr int kTileGroupMax = kThreads; // tiles per pass (one base per thread)
 constexpr int kTileSlotBytes = 32768;    // shared memory for one pass's elements
 
@@ -373,14 +373,23 @@ __global__ void __launch_bounds__(kThreads)
 {
     __shared__ E tile[kTileSlotBytes / sizeof(E)];
     __shared__ uint64_t base_in[kTileGroupMax], base_out[kTileGroupMax];
-    // The offset tables move to shared memory once: indexed per thread, a
-    // kernel-parameter array would serialise every warp's load.
-    __shared__ int32_t in_off[kTileMax], out_off[kTileMax];
-    __shared__ uint16_t pos[kTileMax];
-    for (int e = threadIdx.x; e < p.T; e += blockDim.x) {
-        in_off[e] = p.in_off[e];
-        out_off[e] = p.out_off[e];
-        pos[e] = p.pos[e];
+    // The offset tables move to shared memory once, in 16-byte words: indexed
+    // per thread, a kernel-parameter array serialises every warp's load, so
+    // the tile loops read them from shared memory instead.
+    __shared__ alignas(16) int32_t in_off[kTileMax];
+    __shared__ alignas(16) int32_t out_off[kTileMax];
+    __shared__ alignas(16) uint16_t pos[kTileMax];
+    {
+        const int n4 = (p.T + 3) / 4, n8 = (p.T + 7) / 8; // within the 1024-entry arrays
+        const int4 *src_in = reinterpret_cast<const int4 *>(p.in_off);
+        const int4 *src_out = reinterpret_cast<const int4 *>(p.out_off);
+        const int4 *src_pos = reinterpret_cast<const int4 *>(p.pos);
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+            reinterpret_cast<int4 *>(in_off)[i] = src_in[i];
+            reinterpret_cast<int4 *>(out_off)[i] = src_out[i];
+        }
+        for (int i = threadIdx.x; i < n8; i += blockDim.x)
+            reinterpret_cast<int4 *>(pos)[i] = src_pos[i];
     }
     const uint64_t passes = (p.tiles + p.G - 1) / p.G;
     for (uint64_t ps = blockIdx.x; ps < passes; ps += gridDim.x) {

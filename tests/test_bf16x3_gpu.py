@@ -81,8 +81,8 @@ def _config1_data(rng, rows, cols):
 
 
 @pytest.mark.parametrize("shape,perm", [([2] * 12, None), ([3, 5, 7, 4], [2, 0, 3, 1]),
-                                        ([16, 8], [1, 0]), ([3] * 10, None),
-                                        ([6, 9, 5, 7, 20], [3, 1, 4, 0, 2])])
+                                        ([16, 8], [1, 0]), ([3] * 12, None),
+                                        ([6, 9, 5, 7, 20, 8], [3, 5, 1, 4, 0, 2])])
 def test_split_bf16_bit_exact(cuda, shape, perm):
     """Planes equal the rounding model word for word, on random values,
     exact rounding ties (low 16 bits 0x8000), zeros and FP32 subnormals; both

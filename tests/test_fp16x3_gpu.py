@@ -75,7 +75,7 @@ def _data(rng, rows, cols, scale=2**-10):
 
 
 @pytest.mark.parametrize("shape,perm,scale", [([2] * 12, None, 1.0), ([3, 5, 7, 4], [2, 0, 3, 1], 2.0**-70),
-                                              ([16, 8], [1, 0], 2.0**50), ([3] * 10, None, 1.0)])
+                                              ([16, 8], [1, 0], 2.0**50), ([3] * 12, None, 1.0)])
 def test_split_fp16_bit_exact(cuda, shape, perm, scale):
     """Planes equal the model word for word, with exact rounding ties, zeros,
     and values 2^-20 and 2^-30 below the maximum (FP16 subnormal lo words);

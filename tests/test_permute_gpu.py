@@ -80,14 +80,14 @@ def test_mixed_shapes_vs_oracle(cuda, shape):
         assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("shape,batch,dtype", [([3] * 12, 1, np.complex64), ([3] * 11, 1, np.complex128),
-                                               ([9, 5, 7, 3, 11, 4], 1, np.complex64),
-                                               ([6] * 7, 1, np.complex128), ([3] * 10, 3, np.complex64),
-                                               ([5, 2, 9, 2, 3, 7, 2], 4, np.complex128),
+@pytest.mark.parametrize("shape,batch,dtype", [([3] * 12, 1, np.complex64), ([3] * 12, 1, np.complex128),
+                                               ([9, 5, 7, 3, 11, 4, 7], 1, np.complex64),
+                                               ([6] * 7, 1, np.complex128), ([3] * 11, 3, np.complex64),
+                                               ([5, 2, 9, 2, 3, 7, 2, 5], 4, np.complex128),
                                                ([1000, 3, 7, 2], 1, np.complex64),
                                                ([3] * 8, 3, np.complex64)])
 def test_non_pow2_tiled_vs_oracle(cuda, shape, batch, dtype):
-    """Non-power-of-2 dims of at least 2^15 elements per launch take the tiled
+    """Non-power-of-2 dims of at least 2^18 elements per launch take the tiled
     kernel (several tiles per pass of a CTA, batches enumerated with the
     tiles); smaller ones, and shapes whose innermost axes are too long for a
     tile of at most 1024 elements, take the gather kernel. Bit-exact against
