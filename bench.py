@@ -810,6 +810,65 @@ def run_grad(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def _parse_shape(text):
+    """'3^16' -> [3] * 16; '9,5,7,3' -> [9, 5, 7, 3]."""
+    if "^" in text:
+        d, r = text.split("^")
+        return [int(d)] * int(r)
+    return [int(v) for v in text.split(",")]
+
+
+def run_permute(args):
+    """One permute (jetgpu_permute) of a seeded random permutation, timed with
+    CUDA events on the launching stream over --steps launches after --warmup;
+    the output is compared bit for bit with torch's permute of the same
+    tensor. Algorithmic traffic: one read and one write of every element."""
+    import numpy as np
+    import torch
+
+    from jet_gb300 import capi
+
+    dev = torch.device("cuda:0")
+    shape = _parse_shape(args.permute_shape)
+    perm = [int(v) for v in np.random.default_rng(SEED).permutation(len(shape))]
+    tdt = torch.complex128 if args.permute_dtype == "c128" else torch.complex64
+    n = int(np.prod(shape))
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED)
+    x = torch.randn(n, dtype=tdt, device=dev, generator=g)
+    y = torch.empty_like(x)
+    for _ in range(args.warmup):
+        capi.permute(x, shape, perm, out=y)
+    torch.cuda.synchronize()
+    exact = bool(torch.equal(y, x.view(shape).permute(perm).contiguous().view(-1)))
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            capi.permute(x, shape, perm, out=y)
+        e1.record(st)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    ms = e0.elapsed_time(e1) / args.steps
+    nbytes = 2 * n * x.element_size()
+    gbs = nbytes / ms / 1e6
+    hbm, _, src = measured_peaks()
+    print(json.dumps({
+        "metric": "permute_bandwidth", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "dtype": args.permute_dtype, "data": "synthetic (seeded)",
+        "config": {"workload": "permute %s %s, perm %s" % (args.permute_shape, args.permute_dtype,
+                                                           perm),
+                   "elements": n, "l2": "input and output each larger than L2" if nbytes // 2 > 129e6
+                   else "fits L2 (launch-bound case)"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": gbs / hbm, "peak_source": src, "traffic_algorithmic": nbytes},
+        "exact": exact, "clocks": clocks}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -849,7 +908,16 @@ def main():
     ap.add_argument("--config", default="1",
                     help="1 (default): the pairwise contraction; 0, 2, 4, 4q (qutrits): sliced "
                          "circuit amplitudes through the sliced executor; 3: gradients")
+    ap.add_argument("--permute-shape", default=None,
+                    help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
+                         "permutation)")
+    ap.add_argument("--permute-dtype", default="c64", choices=["c64", "c128"])
     args = ap.parse_args()
+    if args.permute_shape:
+        if args.warmup < 3:
+            args.warmup = 3
+        run_permute(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
