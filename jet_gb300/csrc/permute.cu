@@ -365,6 +365,17 @@ struct TileSplitStore {
     }
 };
 
+// Asynchronous copy of one element from global to shared memory: a thread
+// issues all its loads of a pass without holding them in registers.
+template <typename E> __device__ __forceinline__ void CopyAsync(E *dst, const E *src)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(E) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
 // Each pass moves G consecutive tiles (G * T elements, up to 32 KB) through
 // shared memory: slot u holds element u mod T of the pass's tile u / T.
 template <typename E, typename Store>
@@ -403,8 +414,9 @@ __global__ void __launch_bounds__(kThreads)
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
             const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
             const int e = u - j * p.T;
-            tile[j * p.T + pos[e]] = in[base_in[j] + (uint64_t)in_off[e]];
+            CopyAsync(&tile[j * p.T + pos[e]], in + base_in[j] + (uint64_t)in_off[e]);
         }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
         __syncthreads();
 #pragma unroll 4
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
@@ -882,8 +894,9 @@ int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
     }
     {
         static thread_local TileParams tp; // ~12 KB: keep off the stack
-        if (s.size * batch >= kTileMinElements &&
-            BuildTile(s, batch, dtype == JETGPU_C64 ? 8 : 16, tp))
+        const size_t eb = dtype == JETGPU_C64 ? 8 : 16;
+        if (s.size * batch >= kTileMinElements && (uintptr_t)in % eb == 0 &&
+            BuildTile(s, batch, eb, tp))
             return dtype == JETGPU_C64
                        ? LaunchTile<uint2>(tp, in, TilePlainStore<uint2>{(uint2 *)out}, stream)
                        : LaunchTile<uint4>(tp, in, TilePlainStore<uint4>{(uint4 *)out}, stream);
@@ -954,7 +967,8 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
         return LaunchBitperm<uint2, 1>(bp, in, SplitStore{so}, stream);
     {
         static thread_local TileParams tp;
-        if (s.size * batch >= kTileMinElements && BuildTile(s, batch, 8, tp))
+        if (s.size * batch >= kTileMinElements && (uintptr_t)in % 8 == 0 &&
+            BuildTile(s, batch, 8, tp))
             return LaunchTile<uint2>(tp, in, TileSplitStore{so}, stream);
     }
     GatherParams gp;
