@@ -30,18 +30,19 @@ def _case(seed, nl, nc, nr, dtype, batch, a_b, b_b, dev):
                 m=2 ** nl, n=2 ** nr, k=2 ** nc, na=na, nb=nb)
 
 
+# (dtype, precision, tensor-core main-loop variant): variant 0 for every form;
+# variant 1 shapes only the TF32x3 main loop and variant 2 only the BF16x3 one.
+_FORMS = [("complex64", 0, 0), ("complex64", 1, 0), ("complex64", 3, 0), ("complex64", 4, 0),
+          ("complex128", 0, 0), ("complex64", 1, 1), ("complex64", 3, 2)]
+
+
 @pytest.mark.parametrize("a_b,b_b", [(1, 0), (0, 1), (1, 1)])
-@pytest.mark.parametrize("dtype,precision", [("complex64", 0), ("complex64", 1),
-                                             ("complex64", 3), ("complex64", 4),
-                                             ("complex128", 0)])
+@pytest.mark.parametrize("dtype,precision,variant", _FORMS)
 @pytest.mark.parametrize("shape", [(7, 6, 8), (1, 9, 3), (4, 10, 1), (0, 5, 0), (8, 8, 8),
                                    (6, 14, 0), (0, 16, 3), (0, 18, 0)])
-@pytest.mark.parametrize("variant", [0, 1, 2])
-def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, shape, variant):
+def test_batched_matches_single(cuda, a_b, b_b, dtype, precision, variant, shape):
     from jet_gb300 import capi
 
-    if (variant == 1 and precision != 1) or (variant == 2 and precision != 3):
-        pytest.skip("variant 1 shapes the TF32x3 main loop, variant 2 the BF16x3 one")
     capi.set_tc_variant(variant)
 
     batch = 5
