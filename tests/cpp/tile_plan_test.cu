@@ -1,6 +1,7 @@
 // Host-side check of the tiled permute's plan (jet_gb300/csrc/permute.cu):
 // the kernel's passes are replayed on the CPU over random shapes (dims 1..10,
-// ranks 1..6, batches 1..3) and both element sizes, with input element i
+// ranks 1..6, batches 1..3; then fixed qutrit-sized shapes up to 3^12 with
+// batches of 2) and both element sizes, with input element i
 // holding i, and the result compared with the plain row-major permutation
 // (output axis j = input axis perm[j], the convention of the reference's
 // Permuter, include/jet/permute/Permuter.hpp:36-80). The replay checks every
@@ -86,11 +87,48 @@ int Replay(const TileParams &tp, size_t eb, uint64_t total, std::vector<uint64_t
 
 } // namespace
 
+// 1: planned and replayed equal to the plain permutation; 0: no plan; -1: failure.
+int Check(const std::vector<uint64_t> &shape, const std::vector<int32_t> &perm, uint64_t batch,
+          size_t eb)
+{
+    static TileParams tp;
+    const int rank = (int)shape.size();
+    uint64_t size = 1;
+    for (uint64_t d : shape)
+        size *= d;
+    Simplified s;
+    if (Simplify(rank, shape.data(), perm.data(), s)) {
+        std::printf("simplify failed\n");
+        return -1;
+    }
+    if (!BuildTile(s, batch, eb, tp))
+        return 0;
+    std::vector<uint64_t> ref(size * batch), got(size * batch, ~0ull);
+    std::vector<uint64_t> stride(rank, 1);
+    for (int i = rank - 2; i >= 0; --i)
+        stride[i] = stride[i + 1] * shape[i + 1];
+    for (uint64_t b = 0; b < batch; ++b)
+        for (uint64_t o = 0; o < size; ++o) {
+            uint64_t x = o, src = 0;
+            for (int j = rank - 1; j >= 0; --j) {
+                src += (x % shape[perm[j]]) * stride[perm[j]];
+                x /= shape[perm[j]];
+            }
+            ref[b * size + o] = b * size + src;
+        }
+    if (Replay(tp, eb, size * batch, got))
+        return -1;
+    if (got != ref) {
+        std::printf("mismatch\n");
+        return -1;
+    }
+    return 1;
+}
+
 int main()
 {
     std::mt19937_64 rng(7);
     int planned = 0, cases = 0;
-    static TileParams tp;
     for (int trial = 0; trial < 3000; ++trial) {
         const int rank = 1 + (int)(rng() % 6);
         std::vector<uint64_t> shape(rank);
@@ -107,33 +145,38 @@ int main()
         std::shuffle(perm.begin(), perm.end(), rng);
         const uint64_t batch = 1 + rng() % 3;
         const size_t eb = (trial & 1) ? 8 : 16;
-        Simplified s;
-        if (Simplify(rank, shape.data(), perm.data(), s))
-            FAIL("simplify failed\n");
         ++cases;
-        if (!BuildTile(s, batch, eb, tp))
-            continue;
-        ++planned;
-        std::vector<uint64_t> ref(size * batch), got(size * batch, ~0ull);
-        std::vector<uint64_t> stride(rank, 1);
-        for (int i = rank - 2; i >= 0; --i)
-            stride[i] = stride[i + 1] * shape[i + 1];
-        for (uint64_t b = 0; b < batch; ++b)
-            for (uint64_t o = 0; o < size; ++o) {
-                uint64_t x = o, src = 0;
-                for (int j = rank - 1; j >= 0; --j) {
-                    src += (x % shape[perm[j]]) * stride[perm[j]];
-                    x /= shape[perm[j]];
-                }
-                ref[b * size + o] = b * size + src;
-            }
-        if (Replay(tp, eb, size * batch, got))
+        const int rc = Check(shape, perm, batch, eb);
+        if (rc < 0)
             FAIL("  (trial %d)\n", trial);
-        if (got != ref)
-            FAIL("mismatch in trial %d\n", trial);
+        planned += rc;
     }
     if (planned < cases / 2)
         FAIL("only %d of %d cases planned\n", planned, cases);
-    std::printf("ok %d of %d cases tiled\n", planned, cases);
+    // Sizes the GPU runs take: qutrit and other uniform radices (729- and
+    // 81-element tiles, several per pass), random permutations, both
+    // element sizes, with and without a batch. Axes that stay adjacent and in
+    // order are merged first, so a permutation can leave no tile of at most
+    // 1024 elements (the gather kernel then runs); most must be planned.
+    const std::vector<std::vector<uint64_t>> big = {
+        std::vector<uint64_t>(12, 3), std::vector<uint64_t>(6, 9), std::vector<uint64_t>(8, 5),
+        std::vector<uint64_t>(7, 6), {9, 5, 7, 3, 11, 4, 7}};
+    int big_cases = 0, big_planned = 0;
+    for (const auto &shape : big)
+        for (int rep = 0; rep < 4; ++rep) {
+            std::vector<int32_t> perm(shape.size());
+            for (size_t i = 0; i < perm.size(); ++i)
+                perm[i] = (int32_t)i;
+            std::shuffle(perm.begin(), perm.end(), rng);
+            const int rc = Check(shape, perm, 1 + (rep & 1), (rep & 2) ? 16 : 8);
+            if (rc < 0)
+                FAIL("large case %d of shape %zu axes failed\n", rep, shape.size());
+            ++big_cases;
+            big_planned += rc;
+        }
+    if (2 * big_planned < big_cases)
+        FAIL("only %d of %d large cases planned\n", big_planned, big_cases);
+    std::printf("ok %d of %d cases tiled, %d of %d large cases\n", planned, cases, big_planned,
+                big_cases);
     return 0;
 }
