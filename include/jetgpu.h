@@ -29,7 +29,7 @@ extern "C" {
 #define JETGPU_OK 0
 #define JETGPU_ERR_INVALID 1     /* bad argument (shape, permutation, size) */
 #define JETGPU_ERR_CUDA 2        /* a CUDA runtime/driver call failed */
-#define JETGPU_ERR_UNSUPPORTED 3 /* valid request this build cannot serve */
+#define JETGPU_ERR_UNSUPPORTED 3 /* valid request the library does not serve */
 #define JETGPU_ERR_WORKSPACE 4   /* workspace missing or too small */
 #define JETGPU_ERR_TIMEOUT 5     /* a bounded device wait gave up */
 #define JETGPU_ERR_MEMORY 6      /* the device memory pool limit (jetgpu_set_pool_limit) */
