@@ -527,6 +527,39 @@ bool BuildTile(const Simplified &s, uint64_t batch, size_t elem_bytes, TileParam
     return false;
 }
 
+// The permutation with unit axes dropped and no axes merged. Merging shortens
+// the rank, but a merged axis can be too long for a tile on both sides (e.g.
+// 81 innermost in the input, 729 innermost in the output); the original axes
+// then still give one. `perm` must already have passed Simplify's checks.
+void Unmerged(int rank, const uint64_t *shape, const int32_t *perm, Simplified &u)
+{
+    std::vector<int> keep_id(rank, -1);
+    u.dims.clear();
+    u.perm.clear();
+    u.size = 1;
+    for (int i = 0; i < rank; ++i)
+        if (shape[i] != 1) {
+            keep_id[i] = (int)u.dims.size();
+            u.dims.push_back(shape[i]);
+            u.size *= shape[i];
+        }
+    for (int j = 0; j < rank; ++j)
+        if (keep_id[perm[j]] >= 0)
+            u.perm.push_back(keep_id[perm[j]]);
+}
+
+// A tile plan for the simplified permutation `s` of (rank, shape, perm):
+// first on the merged axes, then on the original ones.
+bool PlanTile(const Simplified &s, int rank, const uint64_t *shape, const int32_t *perm,
+              uint64_t batch, size_t elem_bytes, TileParams &p)
+{
+    if (BuildTile(s, batch, elem_bytes, p))
+        return true;
+    Simplified u;
+    Unmerged(rank, shape, perm, u);
+    return u.dims.size() > s.dims.size() && BuildTile(u, batch, elem_bytes, p);
+}
+
 template <typename E, typename Store>
 int LaunchTile(const TileParams &p, const void *in, Store store, cudaStream_t stream)
 {
@@ -894,9 +927,8 @@ int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
     }
     {
         static thread_local TileParams tp; // ~12 KB: keep off the stack
-        const size_t eb = dtype == JETGPU_C64 ? 8 : 16;
         if (s.size * batch >= kTileMinElements && (uintptr_t)in % eb == 0 &&
-            BuildTile(s, batch, eb, tp))
+            PlanTile(s, rank, shape, perm, batch, eb, tp))
             return dtype == JETGPU_C64
                        ? LaunchTile<uint2>(tp, in, TilePlainStore<uint2>{(uint2 *)out}, stream)
                        : LaunchTile<uint4>(tp, in, TilePlainStore<uint4>{(uint4 *)out}, stream);
@@ -968,7 +1000,7 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
     {
         static thread_local TileParams tp;
         if (s.size * batch >= kTileMinElements && (uintptr_t)in % 8 == 0 &&
-            BuildTile(s, batch, 8, tp))
+            PlanTile(s, rank, shape, perm, batch, 8, tp))
             return LaunchTile<uint2>(tp, in, TileSplitStore{so}, stream);
     }
     GatherParams gp;
