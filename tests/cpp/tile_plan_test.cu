@@ -183,7 +183,32 @@ int main()
             ++big_cases;
             big_planned += rc;
         }
-    std::printf("ok %d of %d cases tiled, %d of %d large cases\n", planned, cases, big_planned,
-                big_cases);
+    // Blocks of axes that stay in order: merged, they are too long for a tile
+    // on both sides, so the plan comes from the original axes (the cases of
+    // the GPU test test_merged_axes_tiled_on_original_axes_vs_oracle).
+    struct Fixed {
+        std::vector<uint64_t> shape;
+        std::vector<int32_t> perm;
+        uint64_t batch;
+        size_t eb;
+    };
+    const std::vector<Fixed> fixed = {
+        {std::vector<uint64_t>(12, 3), {8, 9, 10, 11, 4, 5, 6, 7, 0, 1, 2, 3}, 1, 8},
+        {std::vector<uint64_t>(12, 3), {8, 9, 10, 11, 4, 5, 6, 7, 0, 1, 2, 3}, 2, 16},
+        {std::vector<uint64_t>(12, 3), {6, 7, 8, 9, 10, 11, 0, 1, 2, 3, 4, 5}, 1, 8},
+        {std::vector<uint64_t>(6, 9), {3, 4, 5, 0, 1, 2}, 1, 8}};
+    for (size_t c = 0; c < fixed.size(); ++c) {
+        const Fixed &f = fixed[c];
+        Simplified s;
+        if (Simplify((int)f.shape.size(), f.shape.data(), f.perm.data(), s))
+            FAIL("simplify failed\n");
+        static TileParams merged;
+        if (BuildTile(s, f.batch, f.eb, merged))
+            FAIL("fixed case %zu: expected no tile on the merged axes\n", c);
+        if (Check(f.shape, f.perm, f.batch, f.eb) != 1)
+            FAIL("fixed case %zu: no plan or failed\n", c);
+    }
+    std::printf("ok %d of %d cases tiled, %d of %d large cases, %zu merged-axes cases\n", planned,
+                cases, big_planned, big_cases, fixed.size());
     return 0;
 }
