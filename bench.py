@@ -6,8 +6,10 @@ M = 2^14, N = 2^12, K = 2^13. Both operands' labels are seeded-randomly
 permuted, so both need a transpose. Entries are complex64 with real and
 imaginary parts i.i.d. N(0, 1/2), scaled by 2^-10 (synthetic, seeded).
 
-One step = Tensor::ContractTensors on the device in the TF32x3 tensor-core
-form: permute+split A, permute+split B, tcgen05 GEMM. Metric: effective
+One step = Tensor::ContractTensors on the device in a split-precision
+tensor-core form: permute+split A, permute+split B, tcgen05 product. The
+TF32x3, BF16x3 and FP16x3 forms are all timed; the headline is the fastest
+whose error on the step is within 1e-5 of complex128. Metric: effective
 TFLOP/s = 4 x PathInfo flops / step time = 8 M N K / t. Inputs (1.34 GB) are
 larger than L2 (129 MB), so no flush is needed between steps.
 
@@ -433,8 +435,9 @@ def run_ours(args, rank, world, local_rank):
     # FP16 also reads A once more for its max exponent.
     split_bytes = {"tf32x3": 24.0, "bf16x3": 16.0, "fp16x3": 24.0}[head] * m * k
     achieved = flops / (gemm_ms * 1e-3) / 1e12
-    # DRAM bytes (read + write) per launch of the product at this size, from
-    # one ncu capture (profiles/tc_gemm_split_bf16_config1_launches.md).
+    # DRAM bytes (read + write) per launch of the product at this size: a
+    # constant taken from one ncu capture of this workload, not measured in
+    # this run (CUDA events cannot count DRAM bytes).
     traffic = 14.77e9 if head == "tf32x3" else 7.67e9
     form_names = {"tf32x3": "TF32x3 4M (tcgen05 kind::tf32, hi/lo split, 3 products)",
                   "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)",
@@ -468,6 +471,9 @@ def run_ours(args, rank, world, local_rank):
                      if head != "tf32x3" else
                      ("TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak)),
                      "traffic": traffic,
+                     "traffic_source": "constant from one ncu capture of this workload "
+                                       "(dram__bytes_read.sum + dram__bytes_write.sum), not "
+                                       "measured in this run",
                      "traffic_algorithmic": (32.0 if head == "tf32x3" else 16.0) * (m + n) * k
                      / 2.0 + 8.0 * m * n},
         "roofline_split": {"bound": "hbm",

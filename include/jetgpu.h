@@ -293,8 +293,11 @@ int jetgpu_contract_group(const jetgpu_group_task *tasks, int n_tasks, uint64_t 
  * device address (cudaGetSymbolAddress) with that device current; make that
  * first call before any stream capture. All calls share the one array: calls
  * whose executions overlap on the GPU (different streams, or concurrent
- * graphs) race on it and must be serialised by the caller. Arguments and
- * results are those of jetgpu_contract.
+ * graphs) race on it and must be serialised by the caller. The looked-up
+ * address is cached per device for the life of the process: after a
+ * cudaDeviceReset the module is loaded again and the array may move, so a
+ * process that resets a device must not call this entry point on it again.
+ * Arguments and results are those of jetgpu_contract.
  */
 int jetgpu_contract_noalloc(const void *A, int a_rank, const uint64_t *a_shape,
                             const int32_t *a_perm, const void *B, int b_rank,

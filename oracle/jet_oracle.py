@@ -269,8 +269,14 @@ class OTensorNetwork:
         for lab in indices:
             self.edges.pop(lab, None)
 
-    def contract(self, path: Sequence[Tuple[int, int]], dtype=None) -> OTensor:
-        """TensorNetwork.hpp:301-328 -> ContractNodes_ :394-421."""
+    def contract(self, path: Sequence[Tuple[int, int]], dtype=None,
+                 release: bool = False) -> OTensor:
+        """TensorNetwork.hpp:301-328 -> ContractNodes_ :394-421.
+
+        release=True drops each node's tensor once it has been contracted
+        (the reference keeps every intermediate in nodes_); the arithmetic
+        and the result are the same, only the memory held differs, which
+        lets large networks (53-qubit slices, m12) run in host memory."""
         if not self.nodes:
             raise ValueError("An empty tensor network cannot be contracted.")
         for a, b in path:
@@ -281,6 +287,11 @@ class OTensorNetwork:
             n1, n2 = self.nodes[a], self.nodes[b]
             t3 = contract_tensors(n1.tensor, n2.tensor, dtype=dtype)
             n1.contracted = n2.contracted = True
+            if release:
+                n1.tensor = OTensor(list(n1.tensor.indices), list(n1.tensor.shape),
+                                    np.zeros(0, dtype=t3.data.dtype))
+                n2.tensor = OTensor(list(n2.tensor.indices), list(n2.tensor.shape),
+                                    np.zeros(0, dtype=t3.data.dtype))
             idx3 = vector_disjunctive_union(n1.indices, n2.indices)
             n3 = ONode(len(self.nodes), _node_name(idx3), idx3,
                        vector_union(n1.tags, n2.tags), False, t3)

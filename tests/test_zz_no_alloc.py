@@ -7,7 +7,8 @@ where an allocation would synchronise the device. Its scratch is one 32 MiB
 array inside the library, shared by every call.
 
 The test calls it through the C ABI twice in a row on different inputs and
-compares each result with jetgpu_contract (caller-provided workspace) under
+compares each result with jetgpu_contract (caller-provided workspace) and
+with the complex128 oracle contraction of the same labelled tensors, under
 the tolerances of the other contraction tests: 1e-5 relative for complex64,
 1e-12 for complex128. It also checks that a contraction needing more scratch
 than the array holds is refused with a clear error. This file is collected
@@ -53,6 +54,8 @@ def _noalloc(capi, lib, a, a_shape, a_perm, b, b_shape, b_perm, m, n, k, precisi
 def _operands(seed, dtype, nl, nc, nr, dev):
     import torch
 
+    from oracle import jet_oracle as jo
+
     left = ["l%d" % i for i in range(nl)]
     common = ["c%d" % i for i in range(nc)]
     right = ["r%d" % i for i in range(nr)]
@@ -63,7 +66,10 @@ def _operands(seed, dtype, nl, nc, nr, dev):
     lft = [x for x in a_lab if x not in b_lab]
     com = [x for x in a_lab if x in b_lab]
     rgt = [x for x in b_lab if x not in a_lab]
-    return dict(a=torch.from_numpy(a).to(dev), a_shape=[2] * (nl + nc),
+    want = jo.contract_tensors(jo.OTensor.make(a_lab, [2] * (nl + nc), a, np.complex128),
+                               jo.OTensor.make(b_lab, [2] * (nc + nr), b, np.complex128))
+    return dict(oracle=np.asarray(want.data).reshape(-1),
+                a=torch.from_numpy(a).to(dev), a_shape=[2] * (nl + nc),
                 a_perm=[a_lab.index(x) for x in lft + com],
                 b=torch.from_numpy(b).to(dev), b_shape=[2] * (nc + nr),
                 b_perm=[b_lab.index(x) for x in com + rgt],
@@ -92,6 +98,7 @@ def test_noalloc_matches_contract_twice(cuda, dtype, precision):
         w = want.cpu().numpy()
         assert np.all(np.isfinite(g)), call
         assert _rel(g, w) <= tol, (call, _rel(g, w))
+        assert _rel(g, o["oracle"]) <= tol, (call, _rel(g, o["oracle"]))
     assert capi.take_device_status() == 0
 
 
