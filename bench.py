@@ -244,15 +244,42 @@ def run_ours(args, rank, world, local_rank):
         return float(np.linalg.norm(got - ref_rows) / np.linalg.norm(ref_rows))
 
     def run_form(form):
-        """Times `args.steps` steps of split A, split B, split product."""
-        bf, hf = form == "bf16x3", form == "fp16x3"
+        """Times `args.steps` steps of split A, split B, split product (forms
+        ending in _3m: the 3M product on six planes per operand)."""
+        base, _, algo = form.partition("_")
+        three_m = algo == "3m"
+        bf, hf = base == "bf16x3", base == "fp16x3"
+        fmt = capi.FMT_BF16 if bf else capi.FMT_FP16 if hf else capi.FMT_TF32
         word = torch.int16 if (bf or hf) else torch.float32
-        bplanes = 4 if (bf or hf) else capi.tc_b_planes()
-        pa = torch.empty(4 * m * kp, dtype=word, device=dev)
+        aplanes = 6 if three_m else 4
+        bplanes = 6 if three_m else 4 if (bf or hf) else capi.tc_b_planes()
+        pa = torch.empty(aplanes * m * kp, dtype=word, device=dev)
         pb = torch.empty(bplanes * n * kp, dtype=word, device=dev)
         e2 = torch.empty(2, dtype=torch.int32, device=dev)  # FP16: max exponents of A, B
 
+        def step3m(events=None):
+            if events:
+                events[0].record(stream)
+            if hf:
+                capi.max_exponent(A, stream=stream, out=e2[0:1])
+            capi.split_planes(A, w["a_shape"], w["a_perm"], m, k, kp, pa, fmt,
+                              extra=capi.SPLIT_SUM, e_max=e2[0:1] if hf else None, stream=stream)
+            if events:
+                events[1].record(stream)
+            if hf:
+                capi.max_exponent(B, stream=stream, out=e2[1:2])
+            capi.split_planes(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, fmt,
+                              extra=capi.SPLIT_SUM, e_max=e2[1:2] if hf else None, stream=stream)
+            if events:
+                events[2].record(stream)
+            capi.gemm_split(pa, pb, m, n, k, kp, C, fmt, algo=capi.ALGO_3M,
+                            e_max2=e2 if hf else None, stream=stream)
+            if events:
+                events[3].record(stream)
+
         def step(events=None):
+            if three_m:
+                return step3m(events)
             if events:
                 events[0].record(stream)
             if hf:
@@ -317,7 +344,8 @@ def run_ours(args, rank, world, local_rank):
         del pa, pb
         return out
 
-    forms = ["tf32x3", "bf16x3", "fp16x3"] if args.form == "auto" else [args.form]
+    forms = (["tf32x3", "bf16x3", "fp16x3", "bf16x3_3m", "fp16x3_3m"] if args.form == "auto"
+             else [args.form])
     results = {f: run_form(f) for f in forms}
     if args.form == "auto":
         # The fastest form whose error on this step meets the 1e-5 bound
@@ -334,8 +362,10 @@ def run_ours(args, rank, world, local_rank):
         return
     ms_step, value, rel_err = hr["ms_per_step"], hr["value"], hr["rel_err_vs_fp64"]
     clocks, wall = hr["clocks"], hr["wall_s_timed"]
+    head_base, _, head_algo = head.partition("_")
     head_prec = {"tf32x3": capi.PREC_TF32X3, "bf16x3": capi.PREC_BF16X3,
-                 "fp16x3": capi.PREC_FP16X3}[head]
+                 "fp16x3": capi.PREC_FP16X3}[head_base]
+    head_algo = capi.ALGO_3M if head_algo == "3m" else capi.ALGO_4M
 
     # Plain FP32 form of the same step (permute + SIMT complex GEMM), 2 runs.
     ws_need = capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
@@ -382,7 +412,7 @@ def run_ours(args, rank, world, local_rank):
                   hc=torch.empty(C.shape, dtype=C.dtype).pin_memory()) for _ in range(n_slots)]
     ws_tc = torch.empty(capi.contract_workspace_size(w["a_shape"], w["a_perm"], w["b_shape"],
                                                      w["b_perm_kn"], m, n, k, capi.C64,
-                                                     head_prec),
+                                                     head_prec, head_algo),
                         dtype=torch.uint8, device=dev)
     cs_in = torch.cuda.Stream(dev)
     cs_out = torch.cuda.Stream(dev)
@@ -403,7 +433,7 @@ def run_ours(args, rank, world, local_rank):
         stream.wait_event(ev["out"][j])           # slot j's C read back by step i-3
         capi.contract(sl["a"], w["a_shape"], w["a_perm"], sl["b"], w["b_shape"], w["b_perm_kn"],
                       m, n, k, precision=head_prec, out=sl["c"], workspace=ws_tc,
-                      stream=stream)
+                      stream=stream, algo=head_algo)
         ev["comp"][j].record(stream)
         with torch.cuda.stream(cs_out):
             cs_out.wait_event(ev["comp"][j])
@@ -428,21 +458,36 @@ def run_ours(args, rank, world, local_rank):
     hbm_peak, bf16_peak, peak_src = measured_peaks()
     # Dense tensor rate of the headline form's operand type: BF16 = measured
     # bf16, TF32 = half of it.
-    tc_peak = bf16_peak / 2.0 if head == "tf32x3" else bf16_peak
+    tf32 = head_base == "tf32x3"
+    three_m = head_algo == capi.ALGO_3M
+    tc_peak = bf16_peak / 2.0 if tf32 else bf16_peak
     gemm_ms = hr["stages_ms"]["gemm"]
     split_ms = hr["stages_ms"]["split_a"]
-    # A per element: read 8 B, write 4 planes x (2 B BF16 / FP16 | 4 B TF32);
-    # FP16 also reads A once more for its max exponent.
-    split_bytes = {"tf32x3": 24.0, "bf16x3": 16.0, "fp16x3": 24.0}[head] * m * k
+    # A per element: read 8 B, write 4 planes (3M: 6) x (2 B BF16 / FP16 |
+    # 4 B TF32); FP16 also reads A once more for its max exponent.
+    planes = 6 if three_m else 4
+    word = 4.0 if tf32 else 2.0
+    split_bytes = (8.0 + planes * word + (8.0 if head_base == "fp16x3" else 0.0)) * m * k
     achieved = flops / (gemm_ms * 1e-3) / 1e12
     # DRAM bytes (read + write) per launch of the product at this size: a
     # constant taken from one ncu capture of this workload, not measured in
-    # this run (CUDA events cannot count DRAM bytes).
-    traffic = 14.77e9 if head == "tf32x3" else 7.67e9
+    # this run (CUDA events cannot count DRAM bytes); null where none was taken.
+    traffic = {"tf32x3": 14.77e9, "bf16x3": 7.67e9}.get(head)
     form_names = {"tf32x3": "TF32x3 4M (tcgen05 kind::tf32, hi/lo split, 3 products)",
                   "bf16x3": "BF16x3 4M (tcgen05 kind::f16 on BF16, hi/lo split, 3 products)",
                   "fp16x3": "FP16x3 4M (tcgen05 kind::f16 on FP16 hi/lo of power-of-two "
-                            "scaled operands, 3 products)"}
+                            "scaled operands, 3 products)",
+                  "bf16x3_3m": "BF16x3 3M (Gauss: 3 real products, each hi/lo split "
+                               "3 products, kind::f16 on BF16)",
+                  "fp16x3_3m": "FP16x3 3M (Gauss: 3 real products, each hi/lo split "
+                               "3 products, kind::f16 on scaled FP16)",
+                  "tf32x3_3m": "TF32x3 3M (Gauss: 3 real products, kind::tf32)"}
+    kernel_v = {("tf32x3", False): 0, ("bf16x3", False): 2, ("fp16x3", False): 4,
+                ("tf32x3", True): 5, ("bf16x3", True): 6, ("fp16x3", True): 7}[(head_base,
+                                                                                 three_m)]
+    # Tensor-pipe flops per algorithmic flop: 3 split products of each real
+    # product; 3M does 3 real products where the algorithmic count has 4.
+    pipe_factor = 3.0 * (0.75 if three_m else 1.0)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -462,23 +507,22 @@ def run_ours(args, rank, world, local_rank):
                        "value": world * flops / (plain_ms * 1e-3) / 1e12,
                        "rel_err_vs_fp64": plain_err},
         "roofline": {"bound": "tensor",
-                     "kernel": "tc_gemm_split_kernel<%d>" % {"tf32x3": 0, "bf16x3": 2,
-                                                             "fp16x3": 4}[head],
+                     "kernel": "tc_gemm_split_kernel<%d>" % kernel_v,
                      "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
                      "frac": achieved / tc_peak,
-                     "tensor_pipe_frac": 3 * achieved / tc_peak,
+                     "tensor_pipe_frac": pipe_factor * achieved / tc_peak,
                      "peak_source": ("%s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak))
-                     if head != "tf32x3" else
+                     if not tf32 else
                      ("TF32 dense = 1/2 of %s bf16 (%.0f TFLOP/s)" % (peak_src, bf16_peak)),
                      "traffic": traffic,
-                     "traffic_source": "constant from one ncu capture of this workload "
-                                       "(dram__bytes_read.sum + dram__bytes_write.sum), not "
-                                       "measured in this run",
-                     "traffic_algorithmic": (32.0 if head == "tf32x3" else 16.0) * (m + n) * k
-                     / 2.0 + 8.0 * m * n},
+                     "traffic_source": ("constant from one ncu capture of this workload "
+                                        "(dram__bytes_read.sum + dram__bytes_write.sum), not "
+                                        "measured in this run") if traffic else
+                                       "no ncu capture of this form's product at this size",
+                     "traffic_algorithmic": planes * word * (m + n) * k + 8.0 * m * n},
         "roofline_split": {"bound": "hbm",
                            "kernel": "max_exp_kernel + bitperm_kernel (split store)"
-                           if head == "fp16x3" else "bitperm_kernel (split store)",
+                           if head_base == "fp16x3" else "bitperm_kernel (split store)",
                            "achieved": split_bytes / (split_ms * 1e-3) / 1e9, "peak": hbm_peak,
                            "unit": "GB/s",
                            "frac": split_bytes / (split_ms * 1e-3) / 1e9 / hbm_peak,
@@ -495,10 +539,12 @@ def run_ours(args, rank, world, local_rank):
                             "the contractions"},
         # per step: 2 splits + 1 product (FP16: + one max-exponent kernel per
         # operand, each after a 4-byte memset)
-        "gpu_launches": (5 if head == "fp16x3" else 3) * args.steps,
+        "gpu_launches": (5 if head_base == "fp16x3" else 3) * args.steps,
         "wall_s_timed": wall,
         "clocks": clocks,
     }
+    if not args.no_sliced and world == 1:
+        line["sliced"] = run_config4_leg()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_sample()
@@ -519,6 +565,96 @@ SLICED_CONFIGS = {
     "4q": (5, 5, 8, (), 4, 9, 9, 16),
 }
 QUDIT_DIM = {"4q": 3}
+
+
+def time_sliced_form(jet, tn, path, sliced, prec, batch, chunks, start=None, after=None):
+    """Slices/s of one form through Jet::SlicedContractor: one eager warm-up
+    chunk (prefix, tuning, graph capture), then `chunks` chunks of `batch`
+    slices replayed from the captured graph, timed on the host around the
+    synchronous Contract call (it returns the FP64 sum read back from the
+    device); runs under 0.2 s are repeated and the median kept."""
+    import torch
+
+    sc = jet.SlicedContractorC64(tn, path, sliced, prec)
+    sc.set_batch_size(batch)
+    n_all = sc.num_slices
+    sc.contract(0, batch)
+    count = min(n_all, batch * chunks)
+    if start is None:
+        start = 0 if count == n_all else batch
+    if start + count > n_all:
+        start = 0
+    torch.cuda.synchronize()
+    reps = []
+    amp = None
+    while not reps or sum(reps) < 0.2:
+        t1 = time.perf_counter()
+        amp = sc.contract(start, count)[0]
+        reps.append(time.perf_counter() - t1)
+    dt = statistics.median(reps)
+    if after is not None:
+        after(sc, start)
+    out = {"slices_per_s": count / dt, "s_per_slice": dt / count,
+           "eff_tflops": 4.0 * sc.slice_dependent_flops * count / dt / 1e12,
+           "slices_timed": count, "first_slice": start, "runs": len(reps),
+           "arena_gb": sc.arena_bytes / 1e9}
+    info = {"amp": amp, "slice_flops": sc.slice_flops,
+            "slice_dependent_flops": sc.slice_dependent_flops, "num_slices": n_all}
+    del sc
+    return out, info
+
+
+def config4_golden():
+    """The 53-qubit config-4 record of the golden fixtures: circuit, path,
+    sliced bonds and complex128 amplitudes of two slices (made on the CPU by
+    tests/golden/make_network_fixtures.py)."""
+    with open(os.path.join(REPO, "tests", "golden", "network_amplitudes.json")) as f:
+        return json.load(f)["config4"]
+
+
+def run_config4_leg(batch=16, chunks=2, fp32_chunks=1):
+    """The spec workload beside the config-1 line: config 4 (53 qubits,
+    6 x 9 grid minus one site, 12 cycles, 64 slices of 1011 steps) in the
+    tensor-core AUTO form and in plain FP32, slices/s of each and their
+    ratio, plus each form's error on two single slices against the
+    complex128 oracle amplitudes of the golden fixture."""
+    import jet_gb300 as jet
+    from jet_gb300 import capi, circuits
+
+    ent = config4_golden()
+    net = circuits.random_circuit_network(ent["rows"], ent["cols"], ent["cycles"],
+                                          seed=ent["seed"], removed=tuple(ent["removed"]))
+    path = [tuple(p) for p in ent["path"]]
+    sliced = ent["sliced"]
+    tn = jet.TensorNetwork(dtype="complex64")
+    for lab, sh, d in net.tensors:
+        tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
+    capi.set_auto_form(capi.PREC_FP16X3)
+    forms, errs = {}, {}
+    for name, prec, ch in (("auto", jet.PREC_AUTO, chunks), ("fp32", jet.PREC_FP32, fp32_chunks)):
+        forms[name], info = time_sliced_form(jet, tn, path, sliced, prec, batch, ch)
+        one = jet.SlicedContractorC64(tn, path, sliced, prec)
+        one.set_batch_size(1)
+        errs[name] = {}
+        for v, rec in ent["slices"].items():
+            got = one.contract(int(v), 1)[0]
+            want = complex(*rec["oracle_c128"])
+            errs[name]["slice_%s" % v] = abs(got - want) / abs(want)
+        del one
+    for name in forms:
+        forms[name]["rel_err_vs_fp64"] = max(errs[name].values())
+        forms[name]["rel_err_per_slice"] = errs[name]
+    return {"workload": "config 4: 6x9 grid minus site %d, %d cycles, %d qubits, %d sliced bonds "
+                        "(%d slices), greedy path of %d steps, %d slices per batch"
+                        % (ent["removed"][0], ent["cycles"], ent["rows"] * ent["cols"] - 1,
+                           len(sliced), info["num_slices"], len(path), batch),
+            "unit": "slices/s", "slice_pathinfo_flops": info["slice_flops"],
+            "forms": forms,
+            "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
+            "error_reference": "complex128 oracle amplitudes of slices %s (golden fixture)"
+                               % ", ".join(sorted(ent["slices"], key=int)),
+            "timing": "host clock around each synchronous chunk replay (graph launch + FP64 "
+                      "read-back); warm-up chunk excluded"}
 
 
 def run_sliced(args, rank, world, local_rank):
@@ -547,14 +683,7 @@ def run_sliced(args, rank, world, local_rank):
         net = circuits.qudit_circuit_network(rows, cols, cycles, d=qd, seed=SEED)
     else:
         net = circuits.random_circuit_network(rows, cols, cycles, seed=SEED, removed=removed)
-    best = None
-    for s in range(restarts):
-        for temp in (0.0, 0.2):
-            p = circuits.greedy_path(net, seed=s, temperature=temp, score="gain")
-            f, big = circuits.path_cost(net, p)
-            if best is None or (f, big) < best[0]:
-                best = ((f, big), p)
-    path = best[1]
+    path = circuits.best_gain_path(net, restarts)
     sliced = circuits.choose_slices(net, path, n_sliced) if n_sliced else []
     plan_s = time.perf_counter() - t0
     full_flops, log2_big = circuits.path_cost(net, path)
@@ -604,28 +733,13 @@ def run_sliced(args, rank, world, local_rank):
             amps[name] = complex(res.data[0]) if hasattr(res, "data") else complex(res[0])
             slice_flops = dep_flops = flops
             continue
-        sc = jet.SlicedContractorC64(tn, path, sliced, prec)
-        sc.set_batch_size(batch)
-        n_all = sc.num_slices
-        first = 0
-        sc.contract(first, batch)  # warm-up: prefix, capture, one chunk
-        count = min(n_all, batch * chunks)
-        start = 0 if count == n_all else batch
-        if start + count > n_all:
-            start = 0
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        amp = sc.contract(start, count)[0]
-        dt = time.perf_counter() - t1
-        # Runs this short are timed again until 0.2 s have passed: the median.
-        reps = [dt]
-        while sum(reps) < 0.2:
-            t1 = time.perf_counter()
-            sc.contract(start, count)
-            reps.append(time.perf_counter() - t1)
-        dt = statistics.median(reps)
-        if args.profile_chunk and rank == 0:
-            profiles[name] = sc.profile_chunk(start)
+
+        def profile(sc, start, name=name):
+            if args.profile_chunk and rank == 0:
+                profiles[name] = sc.profile_chunk(start)
+
+        forms[name], info = time_sliced_form(jet, tn, path, sliced, prec, batch, chunks,
+                                             after=profile)
         tuned = None
         if prec == jet.PREC_TUNED:
             table = capi.autotune_table()
@@ -635,16 +749,11 @@ def run_sliced(args, rank, world, local_rank):
             if args.autotune_dump and rank == 0:
                 with open(args.autotune_dump, "w") as f:
                     json.dump(table, f, indent=1)
-        forms[name] = {"slices_per_s": count / dt, "s_per_slice": dt / count,
-                       "eff_tflops": 4.0 * sc.slice_dependent_flops * count / dt / 1e12,
-                       "slices_timed": count, "runs": len(reps),
-                       "arena_gb": sc.arena_bytes / 1e9}
         if tuned is not None:
             forms[name]["autotune"] = tuned
-        amps[name] = amp
-        slice_flops = sc.slice_flops
-        dep_flops = sc.slice_dependent_flops
-        del sc
+        amps[name] = info["amp"]
+        slice_flops = info["slice_flops"]
+        dep_flops = info["slice_dependent_flops"]
     if profiles:
         with open(args.profile_chunk, "w") as f:
             json.dump(profiles, f, indent=1)
@@ -882,6 +991,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sliced", action="store_true",
+                    help="config 1: skip the config-4 sliced leg (AUTO vs plain FP32 slices/s)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: rank-25 x rank-25 (M = N = 2^12, K = 2^13)")
     ap.add_argument("--kernels-only", action="store_true",

@@ -55,6 +55,8 @@ extern "C" {
 
 /* Complex product algorithms for the tensor-core form. */
 #define JETGPU_ALGO_4M 0 /* Cr = ArBr - AiBi, Ci = ArBi + AiBr */
+#define JETGPU_ALGO_3M 1 /* P1 = ArBr, P2 = AiBi, P3 = (Ar+Ai)(Br+Bi): Cr = P1 - P2,
+                            Ci = P3 - P1 - P2 (split forms only) */
 
 /* ---------------------------------------------------------------------------
  * Memory, streams and graphs: the runtime under the C++ host API.
@@ -179,7 +181,9 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
  *
  * precision: JETGPU_PREC_FP32, JETGPU_PREC_TF32X3, JETGPU_PREC_BF16X3 or
  * JETGPU_PREC_FP16X3 (complex64 only; shapes with m or n below 2 take the
- * plain form), JETGPU_PREC_AUTO or JETGPU_PREC_TUNED. algo: JETGPU_ALGO_4M. FP16X3 needs
+ * plain form), JETGPU_PREC_AUTO or JETGPU_PREC_TUNED. algo: JETGPU_ALGO_4M, or
+ * JETGPU_ALGO_3M with TF32X3, BF16X3 or FP16X3 (three real products instead
+ * of four; its workspace is jetgpu_contract_workspace_size_algo's). FP16X3 needs
  * |scale_a + scale_b| <= 126.
  * scale_a, scale_b: power-of-two exponents applied exactly to A and B before
  * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
@@ -199,6 +203,18 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
                     uint64_t m, uint64_t n, uint64_t k, int dtype,
                     int precision, int algo, int scale_a, int scale_b,
                     void *workspace, size_t workspace_bytes, void *stream);
+
+/*
+ * jetgpu_contract_workspace_size for a complex product algorithm: the 3M
+ * split forms keep six planes per operand (the split adds hi, lo of re + im)
+ * instead of four. The cblas_cgemm call this product stands in for is
+ * TensorHelpers.hpp:47-61 (the reference has one complex algorithm).
+ */
+size_t jetgpu_contract_workspace_size_algo(int a_rank, const uint64_t *a_shape,
+                                           const int32_t *a_perm, int b_rank,
+                                           const uint64_t *b_shape, const int32_t *b_perm,
+                                           uint64_t m, uint64_t n, uint64_t k, int dtype,
+                                           int precision, int algo);
 
 /*
  * Batched contraction: C[b] = contract(A[b], B[b]) for b < batch, C packed as
@@ -446,6 +462,30 @@ int jetgpu_split_fp16(const void *in, int rank, const uint64_t *shape,
 int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C,
                        uint64_t m, uint64_t n, uint64_t k, uint64_t kpitch,
                        const int *e_max_dev, float out_scale, void *stream);
+
+/*
+ * The two stages of any split form, with either complex product algorithm.
+ *
+ * jetgpu_split_planes: fmt 0 TF32 (float words, pitch % 4 == 0), 1 BF16,
+ * 2 FP16 (uint16 words, pitch % 8 == 0); planes 0-3 as above; extra 2
+ * (JETGPU_ALGO_3M's operands) also writes plane 4 = hi and plane 5 = lo of
+ * re + im, and for FP16 scales by 2^(s - 1) instead of 2^s so the sums stay
+ * below 2^15. extra 0 writes four planes. e_max_dev: FP16 only.
+ *
+ * jetgpu_gemm_split: C = A * B^T from the planes of A (m x k) and B (n x k):
+ * algo JETGPU_ALGO_4M reads four planes per operand, JETGPU_ALGO_3M six
+ * (written with extra 2) and forms P1 = ArBr, P2 = AiBi,
+ * P3 = (Ar + Ai)(Br + Bi), Cr = P1 - P2, Ci = P3 - P1 - P2. e_max_dev: two
+ * device ints (A, B) for FP16. Replaces the cblas_cgemm call of
+ * TensorHelpers.hpp:47-61.
+ */
+int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
+                        uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                        int fmt, int extra, const int *e_max_dev, void *planes, void *stream);
+
+int jetgpu_gemm_split(const void *a_planes, const void *b_planes, void *C, uint64_t m,
+                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo,
+                      const int *e_max_dev, float out_scale, void *stream);
 
 /*
  * Element-wise sum C = A + B of equal-size tensors whose data are already in

@@ -47,6 +47,13 @@ PREC_FP16X3 = 4
 PREC_TUNED = 5
 
 ALGO_4M = 0
+ALGO_3M = 1
+
+# Word formats of the split stages (jetgpu_split_planes / jetgpu_gemm_split).
+FMT_TF32 = 0
+FMT_BF16 = 1
+FMT_FP16 = 2
+SPLIT_SUM = 2  # extra planes 4, 5: hi, lo of re + im (3M operands)
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _i32p = ctypes.POINTER(ctypes.c_int32)
@@ -57,6 +64,16 @@ lib.jetgpu_contract_workspace_size.restype = ctypes.c_size_t
 lib.jetgpu_contract_workspace_size.argtypes = [ctypes.c_int, _u64p, _i32p, ctypes.c_int, _u64p,
                                                _i32p, ctypes.c_uint64, ctypes.c_uint64,
                                                ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+lib.jetgpu_contract_workspace_size_algo.restype = ctypes.c_size_t
+lib.jetgpu_contract_workspace_size_algo.argtypes = [
+    ctypes.c_int, _u64p, _i32p, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64, ctypes.c_uint64,
+    ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+lib.jetgpu_split_planes.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_uint64,
+                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                    ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
+lib.jetgpu_gemm_split.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                  _vp, ctypes.c_float, _vp]
 lib.jetgpu_permute.argtypes = [_vp, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp]
 lib.jetgpu_permute_batched.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _u64p, _i32p,
                                        ctypes.c_int, _vp]
@@ -213,27 +230,30 @@ def multiply(a, b, m: int, n: int, k: int, out=None, stream=None):
     return out
 
 
-def contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dtype_c, precision) -> int:
-    return int(lib.jetgpu_contract_workspace_size(len(a_shape), u64(a_shape), i32(a_perm),
-                                                  len(b_shape), u64(b_shape), i32(b_perm),
-                                                  m, n, k, dtype_c, precision))
+def contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dtype_c, precision,
+                            algo=ALGO_4M) -> int:
+    return int(lib.jetgpu_contract_workspace_size_algo(len(a_shape), u64(a_shape), i32(a_perm),
+                                                       len(b_shape), u64(b_shape), i32(b_perm),
+                                                       m, n, k, dtype_c, precision, algo))
 
 
 def contract(a, a_shape, a_perm, b, b_shape, b_perm, m, n, k, precision=PREC_FP32,
-             out=None, workspace=None, scale_a=0, scale_b=0, stream=None):
-    """C[m x n] = permute(A)[m x k] permute(B)[k x n] through jetgpu_contract."""
+             out=None, workspace=None, scale_a=0, scale_b=0, stream=None, algo=ALGO_4M):
+    """C[m x n] = permute(A)[m x k] permute(B)[k x n] through jetgpu_contract
+    (algo ALGO_3M: three real products, split forms only)."""
     import torch
 
     dc = dtype_code(a.dtype)
     if out is None:
         out = torch.empty(max(m * n, 1), dtype=a.dtype, device=a.device)
-    need = contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dc, precision)
+    need = contract_workspace_size(a_shape, a_perm, b_shape, b_perm, m, n, k, dc, precision,
+                                   algo)
     if workspace is None and need:
         workspace = torch.empty(need, dtype=torch.uint8, device=a.device)
     ws_bytes = 0 if workspace is None else workspace.numel() * workspace.element_size()
     check(lib.jetgpu_contract(_ptr(a), len(a_shape), u64(a_shape), i32(a_perm), _ptr(b),
                               len(b_shape), u64(b_shape), i32(b_perm), _ptr(out), m, n, k, dc,
-                              precision, ALGO_4M, scale_a, scale_b, _ptr(workspace), ws_bytes,
+                              precision, algo, scale_a, scale_b, _ptr(workspace), ws_bytes,
                               _stream(stream)))
     return out
 
@@ -397,6 +417,26 @@ def gemm_fp16x3(a_planes, b_planes, m, n, k, kpitch, out, e_max2, out_scale=1.0,
     exponents of A and B."""
     check(lib.jetgpu_gemm_fp16x3(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
                                  _ptr(e_max2), out_scale, _stream(stream)))
+    return out
+
+
+def split_planes(x, shape, perm, rows, cols, pitch, planes, fmt, extra=0, e_max=None,
+                 stream=None):
+    """Permute + hi/lo split in any word format (FMT_TF32 / FMT_BF16 / FMT_FP16)
+    into 4 planes, or 6 with extra=SPLIT_SUM (hi, lo of re + im: 3M operands;
+    FP16 then scales by 2^(13 - *e_max))."""
+    check(lib.jetgpu_split_planes(_ptr(x), len(shape), u64(shape), i32(perm), rows, cols, pitch,
+                                  rows * pitch, int(fmt), int(extra), _ptr(e_max), _ptr(planes),
+                                  _stream(stream)))
+    return planes
+
+
+def gemm_split(a_planes, b_planes, m, n, k, kpitch, out, fmt, algo=ALGO_4M, e_max2=None,
+               out_scale=1.0, stream=None):
+    """Split-precision product of planes written by split_planes (ALGO_3M
+    reads six planes per operand)."""
+    check(lib.jetgpu_gemm_split(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
+                                int(fmt), int(algo), _ptr(e_max2), out_scale, _stream(stream)))
     return out
 
 

@@ -343,6 +343,20 @@ def find_path(net: Network, restarts: int = 16, seed: int = 0,
     return best[1]
 
 
+def best_gain_path(net: Network, restarts: int) -> List[Tuple[int, int]]:
+    """Best (total flops, then largest intermediate) of the "gain"-score
+    greedy runs with seeds 0 .. restarts-1, each without and with Gumbel
+    noise at temperature 0.2: the path of the sliced benchmark circuits."""
+    best = None
+    for s in range(restarts):
+        for temp in (0.0, 0.2):
+            p = greedy_path(net, seed=s, temperature=temp, score="gain")
+            f, big = path_cost(net, p)
+            if best is None or (f, big) < best[0]:
+                best = ((f, big), p)
+    return best[1]
+
+
 def path_cost(net: Network, path: Sequence[Tuple[int, int]], sliced: Sequence[str] = ()):
     """(total flops as PathInfo counts them, log2 of the largest intermediate)
     with the sliced indices at dimension 1 (PathInfo.hpp:157-224)."""

@@ -125,13 +125,18 @@ __host__ __device__ inline float Pow2f(int e)
     return v.f;
 }
 
-// PermuteSplitTf32Batched for any word format (neg_im with TF32 only). For
-// FP16, `e_max_dev` points at the operand's max exponent on the device and
-// sets the scale (Fp16ScaleExp); scale_exp is then ignored.
+// Extra plane pair (planes 4 and 5) of a split: none; -im_hi, -im_lo (the
+// N = 256 TF32 main loop); hi, lo of re + im (the 3M product's sums).
+constexpr int kSplitNone = 0, kSplitNegIm = 1, kSplitSum = 2;
+
+// PermuteSplitTf32Batched for any word format (kSplitNegIm with TF32 only).
+// For FP16, `e_max_dev` points at the operand's max exponent on the device
+// and sets the scale (Fp16ScaleExp, one less with kSplitSum so the sums stay
+// in range); scale_exp is then ignored.
 int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
                        const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
                        uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
-                       int neg_im, cudaStream_t stream, const int *e_max_dev = nullptr);
+                       int extra, cudaStream_t stream, const int *e_max_dev = nullptr);
 
 // Device max exponent of `size` complex elements into *e_dev (stream-ordered).
 int MaxExponent(const void *x, uint64_t size, int dtype, int *e_dev, cudaStream_t stream);
@@ -172,20 +177,24 @@ int GemmTf32x3PlanarBatched(const float *a_planes, int a_batched, const float *b
 // the epilogue undoes their scales. `group_m`: tile rows per group of the
 // tile order (0: the jetgpu_set_tc_group_m setting). `tile_counter`: device
 // word of the caller's workspace for the persistent launch's tile counter
-// (null: a slot of a library-wide ring).
+// (null: a slot of a library-wide ring). `algo`: JETGPU_ALGO_4M (four planes
+// per operand) or JETGPU_ALGO_3M (six: the split's kSplitSum pair added; FP16
+// planes scaled one power of two lower, which the epilogue undoes).
 int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_planes,
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant = -1,
                            const int *e_max_dev = nullptr, int group_m = 0,
-                           int *out_emax = nullptr, unsigned int *tile_counter = nullptr);
+                           int *out_emax = nullptr, unsigned int *tile_counter = nullptr,
+                           int algo = JETGPU_ALGO_4M);
 
 // Workspace bytes of a (batched) contraction in `precision` (JETGPU_PREC_TUNED:
 // the largest of its candidates' and AUTO's).
 size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
                          const int32_t *a_perm, int a_batched, int b_rank,
                          const uint64_t *b_shape, const int32_t *b_perm, int b_batched, uint64_t m,
-                         uint64_t n, uint64_t k, int dtype, int precision);
+                         uint64_t n, uint64_t k, int dtype, int precision,
+                         int algo = JETGPU_ALGO_4M);
 
 // Max-exponent hints of one contraction (device ints; each may be null):
 // `a` / `b` hold the operands' exponents when the kernels that wrote them
@@ -207,7 +216,7 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
                  int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m = 0,
-                 const ExpHints *hints = nullptr);
+                 const ExpHints *hints = nullptr, int algo = JETGPU_ALGO_4M);
 
 // JETGPU_PREC_TUNED: the form the autotuner measured fastest for this
 // contraction's key, timing the candidates on first use (autotune.cu).

@@ -30,11 +30,13 @@ inline size_t AlignUp(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 struct SplitLayout {
     SplitFormat fmt;
     int variant;      // main-loop variant, read once
+    int algo;         // JETGPU_ALGO_4M or JETGPU_ALGO_3M
     uint64_t kp;      // row pitch in words
     uint64_t word;    // bytes per word
-    int b_planes;     // 4, or 6 for the N = 256 TF32 main loop
+    int a_planes;     // 4, or 6 for 3M (re + im hi, lo)
+    int b_planes;     // 4, or 6 for the N = 256 TF32 main loop and for 3M
     int group_m;      // tile order (0: the setting)
-    size_t a_bytes(uint64_t rows) const { return AlignUp(4 * rows * kp * word); }
+    size_t a_bytes(uint64_t rows) const { return AlignUp(a_planes * rows * kp * word); }
     size_t b_bytes(uint64_t rows) const { return AlignUp(b_planes * rows * kp * word); }
     // After the planes: the operands' max exponents (two ints, FP16) and the
     // product's tile counter (one unsigned int at byte 16).
@@ -54,7 +56,7 @@ std::atomic<int> g_auto_form{JETGPU_PREC_FP16X3};
 constexpr double kAutoFp16MinWork = 1073741824.0; // 2^30
 
 SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1,
-                      int group_m = 0)
+                      int group_m = 0, int algo = JETGPU_ALGO_4M)
 {
     if (precision == JETGPU_PREC_AUTO) {
         precision = g_auto_form.load(std::memory_order_relaxed);
@@ -69,7 +71,11 @@ SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1,
     l.kp = (k + al - 1) / al * al;
     l.word = SplitWordBytes(l.fmt);
     l.variant = variant >= 0 ? variant : TcVariant();
-    l.b_planes = (l.fmt == SplitFormat::kTf32 && l.variant == 1) ? 6 : 4;
+    l.algo = algo;
+    l.a_planes = algo == JETGPU_ALGO_3M ? 6 : 4;
+    l.b_planes = (algo == JETGPU_ALGO_3M || (l.fmt == SplitFormat::kTf32 && l.variant == 1))
+                     ? 6
+                     : 4;
     l.group_m = group_m;
     return l;
 }
@@ -160,17 +166,19 @@ int SplitProduct(const SplitLayout &l, uint64_t batch, const void *A, int a_rank
         bt[j] = b_perm[nb + (j - nb + nc - nb) % (b_rank - nb)];
     // Mode 1: `ba` tensors back to back; mode 2: one tensor whose leading
     // permuted axes are the batch, i.e. ba * m rows of one split.
+    const bool three_m = l.algo == JETGPU_ALGO_3M;
     if ((rc = PermuteSplitPlanes(A, pa, a_mode == 1 ? ba : 1, a_rank, a_shape, a_perm,
                                  (a_mode == 2 ? ba : 1) * m, k, l.kp, ba * m * l.kp, scale_a,
-                                 l.fmt, 0, st, e_dev)))
+                                 l.fmt, three_m ? kSplitSum : kSplitNone, st, e_dev)))
         return rc;
+    const int b_extra = three_m ? kSplitSum : (l.b_planes == 6 ? kSplitNegIm : kSplitNone);
     if ((rc = PermuteSplitPlanes(B, pb, b_mode == 1 ? bb : 1, b_rank, b_shape, bt.data(),
                                  (b_mode == 2 ? bb : 1) * n, k, l.kp, bb * n * l.kp, scale_b,
-                                 l.fmt, l.b_planes == 6 ? 1 : 0, st, e_dev ? e_dev + 1 : nullptr)))
+                                 l.fmt, b_extra, st, e_dev ? e_dev + 1 : nullptr)))
         return rc;
     return GemmSplitPlanarBatched(pa, ba > 1, pb, bb > 1, C, batch, m, n, k, l.kp, out_scale,
                                   l.fmt, st, l.variant, e_dev, l.group_m,
-                                  hints ? hints->c : nullptr, tile_counter);
+                                  hints ? hints->c : nullptr, tile_counter, l.algo);
 }
 
 } // namespace
@@ -264,6 +272,37 @@ int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void 
                                   SplitFormat::kFp16, AsStream(stream), -1, e_max_dev);
 }
 
+int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
+                        uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
+                        int fmt, int extra, const int *e_max_dev, void *planes, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(fmt >= 0 && fmt <= 2, "fmt must be 0 (TF32), 1 (BF16) or 2 (FP16)");
+    JETGPU_REQUIRE(extra == kSplitNone || extra == kSplitSum, "extra must be 0 or 2");
+    const SplitFormat f = static_cast<SplitFormat>(fmt);
+    JETGPU_REQUIRE(pitch >= cols && pitch % SplitPitchAlign(f) == 0,
+                   "pitch must be >= cols and span a multiple of 16 bytes");
+    JETGPU_REQUIRE(plane_stride >= rows * pitch, "plane stride too small");
+    JETGPU_REQUIRE(f != SplitFormat::kFp16 || e_max_dev != nullptr, "null exponent pointer");
+    if (rows * cols == 0)
+        return JETGPU_OK;
+    JETGPU_REQUIRE(in != nullptr && planes != nullptr, "null pointer");
+    return PermuteSplitPlanes(in, planes, 1, rank, shape, perm, rows, cols, pitch, plane_stride,
+                              0, f, extra, AsStream(stream), e_max_dev);
+}
+
+int jetgpu_gemm_split(const void *a_planes, const void *b_planes, void *C, uint64_t m,
+                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo,
+                      const int *e_max_dev, float out_scale, void *stream)
+{
+    ClearError();
+    JETGPU_REQUIRE(fmt >= 0 && fmt <= 2, "fmt must be 0 (TF32), 1 (BF16) or 2 (FP16)");
+    JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
+    return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
+                                  static_cast<SplitFormat>(fmt), AsStream(stream), 0, e_max_dev,
+                                  0, nullptr, nullptr, algo);
+}
+
 int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C, uint64_t m,
                        uint64_t n, uint64_t k, uint64_t kpitch, float out_scale, void *stream)
 {
@@ -312,7 +351,8 @@ void FoldShape(int rank, const uint64_t *shape, const int32_t *perm, uint64_t ba
 // Workspace of one form (precision FP32, TF32X3, BF16X3, FP16X3 or AUTO).
 size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_perm,
                      int a_batched, int b_rank, const uint64_t *b_shape, const int32_t *b_perm,
-                     int b_batched, uint64_t m, uint64_t n, uint64_t k, int dtype, int precision)
+                     int b_batched, uint64_t m, uint64_t n, uint64_t k, int dtype, int precision,
+                     int algo = JETGPU_ALGO_4M)
 {
     if (batch <= 1 || (!a_batched && !b_batched)) {
         batch = 1;
@@ -322,19 +362,18 @@ size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const 
     if (p.fold) {
         if (a_batched == 2) // the batch axes already lead A's permutation
             return FormWorkspace(1, a_rank, a_shape, a_perm, 0, b_rank, b_shape, b_perm, 0,
-                                 batch * m, n, k, dtype, precision);
+                                 batch * m, n, k, dtype, precision, algo);
         std::vector<uint64_t> s;
         std::vector<int32_t> pm;
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
         return FormWorkspace(1, a_rank + 1, s.data(), pm.data(), 0, b_rank, b_shape, b_perm, 0,
-                             batch * m, n, k, dtype, precision);
+                             batch * m, n, k, dtype, precision, algo);
     }
     if (p.tc) {
         // Sized for six TF32 B planes whatever the main-loop variant.
-        const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k);
-        return l.a_bytes(p.ba * m) +
-               AlignUp((l.fmt == SplitFormat::kTf32 ? 6 : 4) * p.bb * n * l.kp * l.word) +
-               l.exp_bytes();
+        const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k, -1, 0, algo);
+        const int bpl = (l.fmt == SplitFormat::kTf32 || algo == JETGPU_ALGO_3M) ? 6 : 4;
+        return l.a_bytes(p.ba * m) + AlignUp(bpl * p.bb * n * l.kp * l.word) + l.exp_bytes();
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
@@ -352,11 +391,11 @@ size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const 
 size_t ContractWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape,
                          const int32_t *a_perm, int a_batched, int b_rank,
                          const uint64_t *b_shape, const int32_t *b_perm, int b_batched, uint64_t m,
-                         uint64_t n, uint64_t k, int dtype, int precision)
+                         uint64_t n, uint64_t k, int dtype, int precision, int algo)
 {
     if (precision != JETGPU_PREC_TUNED)
         return FormWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm,
-                             b_batched, m, n, k, dtype, precision);
+                             b_batched, m, n, k, dtype, precision, algo);
     // Any candidate of the tuner, and AUTO (untuned steps).
     size_t ws = 0;
     for (int prec : {JETGPU_PREC_FP32, JETGPU_PREC_AUTO, JETGPU_PREC_TF32X3, JETGPU_PREC_FP16X3}) {
@@ -374,7 +413,7 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                  const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                  uint64_t m, uint64_t n, uint64_t k, int dtype, int precision, int variant,
                  int scale_a, int scale_b, void *workspace, cudaStream_t st, int group_m,
-                 const ExpHints *hints)
+                 const ExpHints *hints, int algo)
 {
     if (batch <= 1 || (!a_batched && !b_batched)) {
         batch = 1;
@@ -385,17 +424,18 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
         if (a_batched == 2) // the batch axes already lead A's permutation
             return ContractForm(1, A, a_rank, a_shape, a_perm, 0, B, b_rank, b_shape, b_perm, 0,
                                 C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
-                                workspace, st, group_m, hints);
+                                workspace, st, group_m, hints, algo);
         std::vector<uint64_t> s;
         std::vector<int32_t> pm;
         FoldShape(a_rank, a_shape, a_perm, batch, s, pm);
         return ContractForm(1, A, a_rank + 1, s.data(), pm.data(), 0, B, b_rank, b_shape, b_perm,
                             0, C, batch * m, n, k, dtype, precision, variant, scale_a, scale_b,
-                            workspace, st, group_m, hints);
+                            workspace, st, group_m, hints, algo);
     }
     uint8_t *ws = static_cast<uint8_t *>(workspace);
     if (k > 0 && p.tc)
-        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant, group_m),
+        return SplitProduct(LayoutFor(precision, k, (double)batch * m * n * k, variant, group_m,
+                                      algo),
                             batch, A, a_rank, a_shape, a_perm, p.ba, p.ba > 1 ? a_batched : 0, B,
                             b_rank, b_shape, b_perm, p.bb, p.bb > 1 ? b_batched : 0, C, m, n, k,
                             dtype, scale_a, scale_b, ws, st, hints);
@@ -441,11 +481,15 @@ int CheckContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
     JETGPU_REQUIRE(precision >= JETGPU_PREC_FP32 && precision <= JETGPU_PREC_TUNED,
                    "bad precision");
-    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M, "bad algorithm");
-    if ((precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
-         precision == JETGPU_PREC_FP16X3) &&
-        dtype != JETGPU_C64)
+    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M || algo == JETGPU_ALGO_3M, "bad algorithm");
+    const bool split_form = precision == JETGPU_PREC_TF32X3 || precision == JETGPU_PREC_BF16X3 ||
+                            precision == JETGPU_PREC_FP16X3;
+    if (split_form && dtype != JETGPU_C64)
         return SetError(JETGPU_ERR_UNSUPPORTED, "split precision needs complex64 operands");
+    if (algo == JETGPU_ALGO_3M && (!split_form || batch > 1))
+        return SetError(JETGPU_ERR_UNSUPPORTED,
+                        "the 3M product is available for single contractions in the TF32X3, "
+                        "BF16X3 and FP16X3 forms");
     JETGPU_REQUIRE(a_batched >= 0 && a_batched <= 2 && b_batched >= 0 && b_batched <= 2,
                    "batched flags must be 0, 1 or 2");
     // Mode 2: the operand is one tensor whose permutation leads with axes of
@@ -468,7 +512,8 @@ int CheckContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
     JETGPU_REQUIRE(C != nullptr, "null output");
     JETGPU_REQUIRE(k == 0 || (A != nullptr && B != nullptr), "null operand");
     const size_t need = ContractWorkspace(batch, a_rank, a_shape, a_perm, a_batched, b_rank,
-                                          b_shape, b_perm, b_batched, m, n, k, dtype, precision);
+                                          b_shape, b_perm, b_batched, m, n, k, dtype, precision,
+                                          algo);
     if (need > 0 && (workspace == nullptr || workspace_bytes < need))
         return SetError(JETGPU_ERR_WORKSPACE,
                         "workspace too small: need " + std::to_string(need) + " bytes");
@@ -498,7 +543,7 @@ int Contract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
                              st, hints);
     return ContractForm(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape, b_perm,
                         b_batched, C, m, n, k, dtype, precision, -1, scale_a, scale_b, workspace,
-                        st, 0, hints);
+                        st, 0, hints, algo);
 }
 
 } // namespace
@@ -528,6 +573,16 @@ int jetgpu_contract(const void *A, int a_rank, const uint64_t *a_shape,
     return Contract(1, A, a_rank, a_shape, a_perm, 0, B, b_rank, b_shape, b_perm, 0, C, m, n, k,
                     dtype, precision, algo, scale_a, scale_b, workspace, workspace_bytes,
                     AsStream(stream));
+}
+
+size_t jetgpu_contract_workspace_size_algo(int a_rank, const uint64_t *a_shape,
+                                           const int32_t *a_perm, int b_rank,
+                                           const uint64_t *b_shape, const int32_t *b_perm,
+                                           uint64_t m, uint64_t n, uint64_t k, int dtype,
+                                           int precision, int algo)
+{
+    return ContractWorkspace(1, a_rank, a_shape, a_perm, 0, b_rank, b_shape, b_perm, 0, m, n, k,
+                             dtype, precision, algo);
 }
 
 size_t jetgpu_contract_batched_workspace_size(uint64_t batch, int a_rank, const uint64_t *a_shape,

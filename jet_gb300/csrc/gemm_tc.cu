@@ -20,6 +20,12 @@
 // TMEM accumulator sets (Cr, Ci: 2 x 256 columns) and releases stages with
 // tcgen05.commit; eight accumulator warps fold each finished K chunk into
 // FP32 registers (see the kernel comment) and write C.
+// The 3M ("Gauss") form uses three real products instead of four:
+//   P1 = Ar Br,  P2 = Ai Bi,  P3 = (Ar + Ai)(Br + Bi),
+//   Cr = P1 - P2,  Ci = P3 - P1 - P2,
+// each again as hi*hi + hi*lo + lo*hi, on six planes per operand (the split
+// also writes hi/lo of re + im). 9 tensor-core products per K step instead
+// of 12; Ci's error grows with |P3| ~ 2|A||B| (see the kernel comment).
 // Every mbarrier wait is bounded: on timeout the kernel records
 // JETGPU_ERR_TIMEOUT in a device status word, skips the remaining work,
 // frees its TMEM and returns.
@@ -62,28 +68,44 @@ constexpr int kTileRing = 4;                  // tile indices in flight between 
 //                 half-size stages.
 // A chunk is the K extent accumulated in TMEM before the FP32 fold, in
 // stages (a kernel argument; see the kernel comment).
+//  5, 6, 7 3M:    TF32 / BF16 / FP16 planes, 64-byte rows, 2 stages of six A
+//                 plane boxes (re, im, re + im; hi, lo) and six B boxes;
+//                 9 MMAs of N = 128 per k step, each product into its own
+//                 TMEM slot (see the kernel comment).
 template <int V> struct TcCfg;
 // Operand formats: 0 TF32 (kind::tf32), 1 BF16, 2 FP16 (both kind::f16).
 constexpr int kFmtTf32 = 0, kFmtBf16 = 1, kFmtFp16 = 2;
 template <> struct TcCfg<0> {
-    static constexpr bool Wide = false;
+    static constexpr bool Wide = false, ThreeM = false;
     static constexpr int Fmt = kFmtTf32, Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <> struct TcCfg<1> {
-    static constexpr bool Wide = true;
+    static constexpr bool Wide = true, ThreeM = false;
     static constexpr int Fmt = kFmtTf32, Stages = 2, Tiles = 10, RowBytes = 64;
 };
 template <> struct TcCfg<2> {
-    static constexpr bool Wide = false;
+    static constexpr bool Wide = false, ThreeM = false;
     static constexpr int Fmt = kFmtBf16, Stages = 3, Tiles = 8, RowBytes = 64;
 };
 template <> struct TcCfg<3> {
-    static constexpr bool Wide = false;
+    static constexpr bool Wide = false, ThreeM = false;
     static constexpr int Fmt = kFmtBf16, Stages = 6, Tiles = 8, RowBytes = 32;
 };
 template <> struct TcCfg<4> {
-    static constexpr bool Wide = false;
+    static constexpr bool Wide = false, ThreeM = false;
     static constexpr int Fmt = kFmtFp16, Stages = 3, Tiles = 8, RowBytes = 64;
+};
+template <> struct TcCfg<5> {
+    static constexpr bool Wide = false, ThreeM = true;
+    static constexpr int Fmt = kFmtTf32, Stages = 2, Tiles = 12, RowBytes = 64;
+};
+template <> struct TcCfg<6> {
+    static constexpr bool Wide = false, ThreeM = true;
+    static constexpr int Fmt = kFmtBf16, Stages = 2, Tiles = 12, RowBytes = 64;
+};
+template <> struct TcCfg<7> {
+    static constexpr bool Wide = false, ThreeM = true;
+    static constexpr int Fmt = kFmtFp16, Stages = 2, Tiles = 12, RowBytes = 64;
 };
 template <int V> constexpr int TileBytes() { return kBM * TcCfg<V>::RowBytes; }
 template <int V> constexpr int ElemBytes() { return TcCfg<V>::Fmt == kFmtTf32 ? 4 : 2; }
@@ -307,6 +329,14 @@ __device__ __forceinline__ void TmemWaitLoad()
 // Register budget: the ten warps spread over the SM's four register-file
 // partitions (16K registers each) three to a partition at most, so a thread
 // gets at most 168 registers (a few bytes of the epilogue spill).
+// 3M variants: three accumulators (P1, P2, P3) of 128 columns do not fit
+// twice in the 512 TMEM columns, so the products rotate through four
+// 128-column slots instead: product q = 3 g + p (stage g, product p) goes to
+// slot q mod 4, and the MMA warp waits for that slot's previous product to be
+// folded (two products' MMA time later) before reusing it. The chunk is one
+// stage; the fold adds P1 to Cr and subtracts it from Ci, subtracts P2 from
+// both and adds P3 to Ci. The error of Ci grows with |P3| ~ 2 |A| |B|, about
+// twice the 4M form's; Cr's is the 4M form's.
 template <int V>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_split_kernel(const __grid_constant__ CUtensorMap tmA,
@@ -318,6 +348,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 {
     using Cfg = TcCfg<V>;
     constexpr bool kWide = Cfg::Wide;
+    constexpr bool kThreeM = Cfg::ThreeM;
+    constexpr int kAPlanes = kThreeM ? 6 : 4;
     constexpr int kFmt = Cfg::Fmt;
     constexpr bool kHalf = kFmt != kFmtTf32;
     constexpr int kBK = BlockK<V>();
@@ -328,8 +360,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
-    __shared__ __align__(8) uint64_t acc_full[2];
-    __shared__ __align__(8) uint64_t acc_empty[2];
+    __shared__ __align__(8) uint64_t acc_full[4];  // 4M: two sets; 3M: four slots
+    __shared__ __align__(8) uint64_t acc_empty[4];
     __shared__ __align__(8) uint64_t tile_full[kTileRing];
     __shared__ __align__(8) uint64_t tile_empty[kTileRing];
     __shared__ int tile_ring[kTileRing];
@@ -377,7 +409,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             MbarInit(SmemAddr(&full_bar[s]), 1);
             MbarInit(SmemAddr(&empty_bar[s]), 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < 4; ++b) {
             MbarInit(SmemAddr(&acc_full[b]), 1);
             MbarInit(SmemAddr(&acc_empty[b]), kAccWarps);
         }
@@ -431,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t base = SmemAddr(smem + s * kStageBytes);
                 const int k0 = kt * kBK;
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
+                for (int p = 0; p < kAPlanes; ++p) {
                     if (a_batched)
                         TmaLoad4d(base + p * kTileBytes, &tmA, k0, m0, bz, p, fb);
                     else
@@ -439,17 +471,19 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 // B tiles: narrow {Br_hi, Br_lo, Bi_hi, Bi_lo}; wide
                 // {-Bi_hi, Br_hi, Bi_hi, -Bi_lo, Br_lo, Bi_lo} (plane numbers
-                // 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo, 4 -im_hi, 5 -im_lo).
-                constexpr int kBTiles = Cfg::Tiles - 4;
+                // 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo, 4 -im_hi, 5 -im_lo);
+                // 3M {Br_hi, Br_lo, Bi_hi, Bi_lo, Bs_hi, Bs_lo} (4, 5: re + im).
+                constexpr int kBTiles = Cfg::Tiles - kAPlanes;
 #pragma unroll
                 for (int t = 0; t < kBTiles; ++t) {
                     const int plane = kWide ? (t == 0 ? 4 : t == 1 ? 0 : t == 2 ? 2
                                                : t == 3 ? 5 : t == 4 ? 1 : 3)
                                             : t;
                     if (b_batched)
-                        TmaLoad4d(base + (4 + t) * kTileBytes, &tmB, k0, n0, bz, plane, fb);
+                        TmaLoad4d(base + (kAPlanes + t) * kTileBytes, &tmB, k0, n0, bz, plane,
+                                  fb);
                     else
-                        TmaLoad3d(base + (4 + t) * kTileBytes, &tmB, k0, n0, plane, fb);
+                        TmaLoad3d(base + (kAPlanes + t) * kTileBytes, &tmB, k0, n0, plane, fb);
                 }
             }
             }
@@ -472,6 +506,50 @@ __global__ void __launch_bounds__(kThreads, 1)
                          : "memory");
             if (t >= total_tiles)
                 break;
+            if constexpr (kThreeM) {
+            for (int kt = 0; kt < ktiles && ok; ++kt) {
+                const long long g = (long long)i * ktiles + kt;
+                const int s = (int)(g % kStages);
+                const uint32_t phase = (uint32_t)(g / kStages) & 1u;
+                if (!MbarWait(SmemAddr(&full_bar[s]), phase)) {
+                    ok = false;
+                    break;
+                }
+                FenceAfterSync();
+                const uint32_t base = SmemAddr(smem + s * kStageBytes);
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {
+                    // Product p of stage g into slot q mod 4, free once the
+                    // product four back has been folded.
+                    const long long q = 3 * g + p;
+                    const int slot = (int)(q & 3);
+                    if (!MbarWait(SmemAddr(&acc_empty[slot]), ((uint32_t)(q >> 2) & 1u) ^ 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    FenceAfterSync();
+                    const uint32_t d = tmem + slot * kBN;
+#pragma unroll
+                    for (int kk = 0; kk < kRowBytes / 32; ++kk) {
+                        const uint32_t koff = kk * 32; // 32 bytes of K per MMA
+                        // Planes 2p (hi), 2p + 1 (lo) of A (tiles 0..5) and B (6..11).
+                        const uint64_t ah = SmemDesc<kRowBytes>(base + (2 * p) * kTileBytes + koff);
+                        const uint64_t al =
+                            SmemDesc<kRowBytes>(base + (2 * p + 1) * kTileBytes + koff);
+                        const uint64_t bh =
+                            SmemDesc<kRowBytes>(base + (6 + 2 * p) * kTileBytes + koff);
+                        const uint64_t bl =
+                            SmemDesc<kRowBytes>(base + (7 + 2 * p) * kTileBytes + koff);
+                        Mma<kHalf>(d, ah, bh, kIdesc, kk == 0 ? 0u : 1u);
+                        Mma<kHalf>(d, ah, bl, kIdesc, 1u);
+                        Mma<kHalf>(d, al, bh, kIdesc, 1u);
+                    }
+                    MmaCommit(SmemAddr(&acc_full[slot]));
+                }
+                MmaCommit(SmemAddr(&empty_bar[s]));
+            }
+            }
+            else
             for (int kt = 0; kt < ktiles && ok; ++kt) {
                 const int chunk = kt / chunk_stages;
                 // Accumulator set: chunks alternate across tiles too.
@@ -568,7 +646,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         // multiplies (each factor inside the float range).
         float f1 = 1.f, f2 = 1.f;
         if (scale_exps != nullptr) {
-            const int e = -(Fp16ScaleExp(scale_exps[0]) + Fp16ScaleExp(scale_exps[1]));
+            // 3M planes were scaled one power of two lower (sum headroom).
+            const int e = -(Fp16ScaleExp(scale_exps[0]) + Fp16ScaleExp(scale_exps[1])) +
+                          (kThreeM ? 2 : 0);
             f1 = Pow2f(e / 2);
             f2 = Pow2f(e - e / 2);
         }
@@ -595,6 +675,52 @@ __global__ void __launch_bounds__(kThreads, 1)
             acc_re[j] = 0.f;
             acc_im[j] = 0.f;
         }
+        if constexpr (kThreeM) {
+        for (int kt = 0; kt < ktiles && ok; ++kt) {
+            const long long g = (long long)i * ktiles + kt;
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                const long long q = 3 * g + p;
+                const int slot = (int)(q & 3);
+                ok = MbarWait(SmemAddr(&acc_full[slot]), (uint32_t)(q >> 2) & 1u);
+                __syncwarp();
+                if (!ok)
+                    break;
+                FenceAfterSync();
+                const uint32_t col0 = tmem + lane_base + slot * kBN + half * 64;
+#pragma unroll
+                for (int c = 0; c < 64; c += 32) {
+                    float v0[16], v1[16];
+                    TmemLoad16(col0 + c, v0);
+                    TmemLoad16(col0 + c + 16, v1);
+                    TmemWaitLoad();
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) {
+                        // P1: Cr += P1, Ci -= P1; P2: Cr -= P2, Ci -= P2; P3: Ci += P3.
+                        if (p != 2) {
+                            const float sr = p == 0 ? 1.f : -1.f;
+                            AddF32x2(acc_re[c + j], acc_re[c + j + 1], sr * v0[j], sr * v0[j + 1]);
+                            AddF32x2(acc_re[c + 16 + j], acc_re[c + 17 + j], sr * v1[j],
+                                     sr * v1[j + 1]);
+                            AddF32x2(acc_im[c + j], acc_im[c + j + 1], -v0[j], -v0[j + 1]);
+                            AddF32x2(acc_im[c + 16 + j], acc_im[c + 17 + j], -v1[j], -v1[j + 1]);
+                        }
+                        else {
+                            AddF32x2(acc_im[c + j], acc_im[c + j + 1], v0[j], v0[j + 1]);
+                            AddF32x2(acc_im[c + 16 + j], acc_im[c + 17 + j], v1[j], v1[j + 1]);
+                        }
+                    }
+                }
+                FenceBeforeSync();
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                     SmemAddr(&acc_empty[slot]))
+                                 : "memory");
+            }
+        }
+        }
+        else
         for (int chunk = 0; chunk < nchunks; ++chunk) {
             const long long gc = (long long)i * nchunks + chunk;
             const int buf = (int)(gc & 1);
@@ -895,8 +1021,10 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
                            int b_batched, void *C, uint64_t batch, uint64_t m, uint64_t n,
                            uint64_t k, uint64_t kpitch, float out_scale, SplitFormat fmt,
                            cudaStream_t stream, int variant, const int *e_max_dev, int group_m,
-                           int *out_emax, unsigned int *tile_counter)
+                           int *out_emax, unsigned int *tile_counter, int algo)
 {
+    JETGPU_REQUIRE(algo == JETGPU_ALGO_4M || algo == JETGPU_ALGO_3M, "bad algorithm");
+    const bool three_m = algo == JETGPU_ALGO_3M;
     JETGPU_REQUIRE(batch >= 1 && batch <= 65535, "batch out of range");
     if (batch == 1) {
         a_batched = 0;
@@ -921,19 +1049,31 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (variant < 0)
         variant = TcVariant();
-    const bool wide = !half && variant == 1;
-    const bool deep = bf16 && variant == 2;
+    const bool wide = !half && variant == 1 && !three_m;
+    const bool deep = bf16 && variant == 2 && !three_m;
     const int row_bytes = deep ? TcCfg<3>::RowBytes : TcCfg<0>::RowBytes;
+    const int aplanes = three_m ? 6 : 4;
     CUtensorMap ta, tb;
     if ((rc = a_batched
-                  ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, half, 4, row_bytes)
-                  : EncodePlanes(&ta, a_planes, m, k, kpitch, half, 4, row_bytes)))
+                  ? EncodePlanesBatched(&ta, a_planes, m, k, kpitch, batch, half, aplanes,
+                                        row_bytes)
+                  : EncodePlanes(&ta, a_planes, m, k, kpitch, half, aplanes, row_bytes)))
         return rc;
-    const int bplanes = wide ? 6 : 4;
+    const int bplanes = (wide || three_m) ? 6 : 4;
     if ((rc = b_batched
                   ? EncodePlanesBatched(&tb, b_planes, n, k, kpitch, batch, half, bplanes, row_bytes)
                   : EncodePlanes(&tb, b_planes, n, k, kpitch, half, bplanes, row_bytes)))
         return rc;
+    if (three_m) {
+        if (fp16)
+            return LaunchTc<7>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
+                               stream, e_max_dev, group_m, out_emax, tile_counter);
+        if (bf16)
+            return LaunchTc<6>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched,
+                               stream, nullptr, group_m, out_emax, tile_counter);
+        return LaunchTc<5>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           nullptr, group_m, out_emax, tile_counter);
+    }
     if (fp16)
         return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
                            e_max_dev, group_m, out_emax, tile_counter);

@@ -219,12 +219,13 @@ __device__ __forceinline__ void SplitF16x2(float x0, float x1, uint32_t &hi, uin
 }
 
 struct SplitOut {
-    void *planes;          // 4 planes, or 6 with the negated imaginary pair
+    void *planes;          // 4 planes, or 6 with an extra pair (see `extra`)
     uint64_t plane_stride; // words between planes
     uint64_t cols;         // logical columns of the permuted view
     uint64_t pitch;        // words per row in a plane
     float scale;           // exact power of two
-    int neg_im;            // also write planes 4, 5 = -im_hi, -im_lo (TF32)
+    int extra;             // planes 4, 5: kSplitNegIm -im_hi, -im_lo (TF32);
+                           // kSplitSum hi, lo of re + im (the 3M product's sums)
     int bf16;              // 16-bit BF16 words instead of TF32-in-FP32 words
     int fp16;              // 16-bit FP16 words of the operand scaled by its FP16 scale
     const int *e_max_dev;  // FP16: the operand's max exponent (sets the scale)
@@ -233,7 +234,11 @@ struct SplitOut {
 
 __device__ __forceinline__ float SplitScale(const SplitOut &so)
 {
-    return so.fp16 ? Pow2f(Fp16ScaleExp(*so.e_max_dev)) : so.scale;
+    // With sum planes the FP16 scale is one power of two lower: the operand's
+    // largest |re| or |im| lies in [2^13, 2^14), so |re + im| < 2^15 stays
+    // below the FP16 maximum 65504.
+    return so.fp16 ? Pow2f(Fp16ScaleExp(*so.e_max_dev) - (so.extra == kSplitSum ? 1 : 0))
+                   : so.scale;
 }
 
 __device__ __forceinline__ void Split16x2(const SplitOut &so, float x0, float x1, uint32_t &hi,
@@ -261,6 +266,11 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
         pl[off + so.plane_stride] = (uint16_t)(l & 0xffffu);
         pl[off + 2 * so.plane_stride] = (uint16_t)(h >> 16);
         pl[off + 3 * so.plane_stride] = (uint16_t)(l >> 16);
+        if (so.extra == kSplitSum) {
+            Split16x2(so, re + im, 0.f, h, l);
+            pl[off + 4 * so.plane_stride] = (uint16_t)(h & 0xffffu);
+            pl[off + 5 * so.plane_stride] = (uint16_t)(l & 0xffffu);
+        }
         return;
     }
     float *planes = static_cast<float *>(so.planes);
@@ -270,9 +280,14 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
     planes[off + so.plane_stride] = rl;
     planes[off + 2 * so.plane_stride] = ih;
     planes[off + 3 * so.plane_stride] = il;
-    if (so.neg_im) {
+    if (so.extra == kSplitNegIm) {
         planes[off + 4 * so.plane_stride] = -ih;
         planes[off + 5 * so.plane_stride] = -il;
+    }
+    else if (so.extra == kSplitSum) {
+        const float sm = re + im, sh = RoundTf32(sm);
+        planes[off + 4 * so.plane_stride] = sh;
+        planes[off + 5 * so.plane_stride] = RoundTf32(sm - sh);
     }
 }
 
@@ -686,6 +701,12 @@ struct SplitStore {
             *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = rl;
             *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = ih;
             *reinterpret_cast<uint32_t *>(pl + base + 3 * so.plane_stride) = il;
+            if (so.extra == kSplitSum) {
+                uint32_t sh, sl;
+                Split16x2(so, ar + ai, br + bi, sh, sl);
+                *reinterpret_cast<uint32_t *>(pl + base + 4 * so.plane_stride) = sh;
+                *reinterpret_cast<uint32_t *>(pl + base + 5 * so.plane_stride) = sl;
+            }
             return;
         }
         float *planes = static_cast<float *>(so.planes);
@@ -699,11 +720,19 @@ struct SplitStore {
         *reinterpret_cast<float2 *>(planes + base + so.plane_stride) = rl;
         *reinterpret_cast<float2 *>(planes + base + 2 * so.plane_stride) = ih;
         *reinterpret_cast<float2 *>(planes + base + 3 * so.plane_stride) = il;
-        if (so.neg_im) {
+        if (so.extra == kSplitNegIm) {
             *reinterpret_cast<float2 *>(planes + base + 4 * so.plane_stride) =
                 make_float2(-ih.x, -ih.y);
             *reinterpret_cast<float2 *>(planes + base + 5 * so.plane_stride) =
                 make_float2(-il.x, -il.y);
+        }
+        else if (so.extra == kSplitSum) {
+            const float sa = ar + ai, sb = br + bi;
+            const float sah = RoundTf32(sa), sbh = RoundTf32(sb);
+            *reinterpret_cast<float2 *>(planes + base + 4 * so.plane_stride) =
+                make_float2(sah, sbh);
+            *reinterpret_cast<float2 *>(planes + base + 5 * so.plane_stride) =
+                make_float2(RoundTf32(sa - sah), RoundTf32(sb - sbh));
         }
     }
 };
@@ -960,15 +989,19 @@ int PermuteSplitTf32Batched(const void *in, float *planes, uint64_t batch, int r
                             int scale_exp, cudaStream_t stream, int neg_im)
 {
     return PermuteSplitPlanes(in, planes, batch, rank, shape, perm, rows, cols, pitch,
-                              plane_stride, scale_exp, SplitFormat::kTf32, neg_im, stream);
+                              plane_stride, scale_exp, SplitFormat::kTf32,
+                              neg_im ? kSplitNegIm : kSplitNone, stream);
 }
 
 int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
                        const uint64_t *shape, const int32_t *perm, uint64_t rows, uint64_t cols,
                        uint64_t pitch, uint64_t plane_stride, int scale_exp, SplitFormat fmt,
-                       int neg_im, cudaStream_t stream, const int *e_max_dev)
+                       int extra, cudaStream_t stream, const int *e_max_dev)
 {
-    JETGPU_REQUIRE(!(neg_im && fmt != SplitFormat::kTf32), "negated planes are TF32 only");
+    JETGPU_REQUIRE(extra == kSplitNone || extra == kSplitNegIm || extra == kSplitSum,
+                   "unknown extra plane pair");
+    JETGPU_REQUIRE(!(extra == kSplitNegIm && fmt != SplitFormat::kTf32),
+                   "negated planes are TF32 only");
     JETGPU_REQUIRE(fmt != SplitFormat::kFp16 || e_max_dev != nullptr,
                    "FP16 planes need the operand's max exponent");
     Simplified s;
@@ -987,7 +1020,7 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
     so.cols = cols;
     so.pitch = pitch;
     so.scale = ldexpf(1.0f, scale_exp);
-    so.neg_im = neg_im;
+    so.extra = extra;
     so.bf16 = fmt == SplitFormat::kBf16 ? 1 : 0;
     so.fp16 = fmt == SplitFormat::kFp16 ? 1 : 0;
     so.e_max_dev = e_max_dev;

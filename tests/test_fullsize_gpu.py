@@ -4,8 +4,13 @@ oracle to run the whole problem:
   * the permute is bit-exact: a round trip through the inverse permutation
     returns the input bytes, and 4096 sampled outputs match index arithmetic;
   * the BF16 split reconstructs every element: |x - (hi + lo)| <= 2^-16 |x|;
-  * the contraction (BF16x3, TF32x3) matches complex128 on 16 sampled rows of
-    C within 1e-5, and is linear in B within 2e-5."""
+  * the contraction (BF16x3, TF32x3, FP16x3; 4M and 3M) against complex128 products of
+    the oracle's CPU transposes of A and B: every 16th row of C (1024 rows,
+    a quarter of a billion entries) exactly, and all of C through a
+    Freivalds-style sketch U^T C V (U: M x 8, V: N x 8 complex Gaussian),
+    whose relative Frobenius difference from (U^T A')(B' V) estimates C's
+    normwise error; both within 1e-5;
+  * the contraction is linear in B within 2e-5."""
 import numpy as np
 import pytest
 
@@ -93,22 +98,52 @@ def test_bf16_split_reconstructs_every_element(data):
     assert bool((err_im <= im.abs() * 2.0**-16).all())
 
 
-@pytest.mark.parametrize("precision", ["bf16x3", "tf32x3"])
-def test_contraction_rows_match_fp64(data, precision):
+@pytest.fixture(scope="module")
+def oracle_operands(data):
+    """A' (M x K) and B' (K x N): the operands in ContractTensors' order,
+    transposed on the CPU by the oracle (numpy), complex64, plus the
+    complex128 sketch factors U^T A' (8 x K) and B' V (K x 8)."""
+    from oracle import jet_oracle as jo
+
+    w, a, b = data
+    m, n, k = w["m"], w["n"], w["k"]
+    r_a, r_b = len(w["a_shape"]), len(w["b_shape"])
+    a_lab = ["x%d" % i for i in range(r_a)]
+    b_lab = ["y%d" % i for i in range(r_b)]
+    at = jo.transpose(jo.OTensor(a_lab, list(w["a_shape"]), a.cpu().numpy()),
+                      [a_lab[i] for i in w["a_perm"]]).data.reshape(m, k)
+    bt = jo.transpose(jo.OTensor(b_lab, list(w["b_shape"]), b.cpu().numpy()),
+                      [b_lab[i] for i in w["b_perm"]]).data.reshape(k, n)
+    rng = np.random.default_rng(9)
+    u = (rng.standard_normal((m, 8)) + 1j * rng.standard_normal((m, 8))) / np.sqrt(2)
+    v = (rng.standard_normal((n, 8)) + 1j * rng.standard_normal((n, 8))) / np.sqrt(2)
+    uta = u.T @ at.astype(np.complex128)        # 8 x K
+    btv = bt.astype(np.complex128) @ v          # K x 8
+    return dict(at=at, bt=bt, u=u, v=v, sketch=uta @ btv)
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32x3", "fp16x3", "bf16x3_3m", "fp16x3_3m",
+                                       "tf32x3_3m"])
+def test_contraction_matches_fp64_every_16th_row_and_sketch(data, oracle_operands, precision):
     from jet_gb300 import capi
 
     w, a, b = data
     m, n, k = w["m"], w["n"], w["k"]
-    prec = capi.PREC_BF16X3 if precision == "bf16x3" else capi.PREC_TF32X3
+    form, _, algo = precision.partition("_")
+    prec = {"bf16x3": capi.PREC_BF16X3, "tf32x3": capi.PREC_TF32X3,
+            "fp16x3": capi.PREC_FP16X3}[form]
     c = capi.contract(a, w["a_shape"], w["a_perm"], b, w["b_shape"], w["b_perm"], m, n, k,
-                      precision=prec)
-    rows = np.random.default_rng(5).choice(m, 16, replace=False)
-    at = capi.permute(a, w["a_shape"], w["a_perm"]).view(m, k)[rows].cpu().numpy()
-    bt = capi.permute(b, w["b_shape"], w["b_perm"]).view(k, n).cpu().numpy()
-    want = at.astype(np.complex128) @ bt.astype(np.complex128)
-    got = c.view(m, n)[rows].cpu().numpy()
-    assert np.linalg.norm(got - want) <= 1e-5 * np.linalg.norm(want)
+                      precision=prec, algo=capi.ALGO_3M if algo == "3m" else capi.ALGO_4M)
+    got = c.view(m, n).cpu().numpy()
     assert capi.take_device_status() == 0
+    o = oracle_operands
+    rows = np.arange(0, m, 16)
+    want = o["at"][rows].astype(np.complex128) @ o["bt"].astype(np.complex128)
+    rel_rows = np.linalg.norm(got[rows] - want) / np.linalg.norm(want)
+    assert rel_rows <= 1e-5, rel_rows
+    sk = o["u"].T @ (got.astype(np.complex128) @ o["v"])
+    rel_sketch = np.linalg.norm(sk - o["sketch"]) / np.linalg.norm(o["sketch"])
+    assert rel_sketch <= 1e-5, rel_sketch
 
 
 def test_contraction_linear_in_b(data):

@@ -74,3 +74,35 @@ def test_benchmark_file_schema(jet):
     tnf = jet.TensorNetworkSerializer(dtype="complex64")(js)
     assert tnf.tensors.num_tensors == 4
     assert len(tnf.path.steps) == 7
+
+
+@pytest.mark.parametrize("name,tensors,steps", [("m10", 322, 321), ("m12", 410, 409)])
+def test_reference_benchmark_networks_load(jet, name, tensors, steps):
+    """The reference's m10 / m12 networks (golden npz form) rebuilt as JSON
+    text of the reference's schema load through the serializer with their
+    stored paths; where the reference tree is present, the npz holds exactly
+    the tensors of the reference's own file."""
+    import os
+
+    import numpy as np
+
+    import make_network_fixtures as mk
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    ts, path = mk.load_network_npz(os.path.join(here, name + "_network.npz"))
+    assert len(ts) == tensors and len(path) == steps
+    tnf = jet.TensorNetworkSerializer(dtype="complex64")(mk.network_json_text(ts, path))
+    assert tnf.tensors.num_tensors == tensors
+    assert tnf.path.path == path
+    node = tnf.tensors.nodes[7]
+    assert node.tensor.indices == ts[7][1] and node.tags == ts[7][0]
+    assert np.allclose(np.array(node.tensor.data, dtype=np.complex64), ts[7][3])
+    src = os.path.join(mk.reference_root(), "examples", "paper_benchmarks", "data_files",
+                       name + ".json")
+    if os.path.exists(src):
+        with open(src) as f:
+            js = json.load(f)
+        assert [tuple(p) for p in js["path"]] == path
+        for (tg, lb, sh, d), t in zip(ts, js["tensors"]):
+            assert tg == t[0] and lb == t[1] and sh == t[2]
+            assert np.array_equal(d, np.array([complex(*x) for x in t[3]], dtype=np.complex64))
