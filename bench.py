@@ -544,7 +544,8 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
     }
     if not args.no_sliced and world == 1:
-        line["sliced"] = run_config4_leg()
+        line["sliced"] = {"config4": run_sliced_leg("config4", batch=16, chunks=2),
+                          "config2": run_sliced_leg("config2", batch=2, chunks=2)}
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_sample()
@@ -555,16 +556,19 @@ def run_ours(args, rank, world, local_rank):
 
 
 SLICED_CONFIGS = {
-    # name: (rows, cols, cycles, removed sites, sliced bonds, slices per batch,
-    #        chunks timed, path restarts)
+    # name: (rows, cols, cycles, removed sites, sliced bonds (config 4: the
+    #        fewest), slices per batch, chunks timed, path restarts)
     "2": (7, 7, 14, (), 12, 2, 2, 48),
-    "4": (6, 9, 12, (5,), 6, 16, 4, 48),
+    "4": (6, 9, 12, (5,), 6, 64, 2, 48),
     "0": (4, 4, 8, (), 0, 1, 1, 8),
     # qutrit variant of config 4: 5x5 sites of dimension 3, 8 layers of Haar
     # unitaries (cycles = layers), 4 sliced bonds -> 81 slices
     "4q": (5, 5, 8, (), 4, 9, 9, 16),
 }
 QUDIT_DIM = {"4q": 3}
+# Configs sliced until a chunk of their slices per batch fits this much HBM
+# (the contractor's own plan: arena, workspace, slice-independent buffers).
+MEMORY_BUDGET = {"4": 120e9}
 
 
 def time_sliced_form(jet, tn, path, sliced, prec, batch, chunks, start=None, after=None):
@@ -604,24 +608,24 @@ def time_sliced_form(jet, tn, path, sliced, prec, batch, chunks, start=None, aft
     return out, info
 
 
-def config4_golden():
-    """The 53-qubit config-4 record of the golden fixtures: circuit, path,
-    sliced bonds and complex128 amplitudes of two slices (made on the CPU by
-    tests/golden/make_network_fixtures.py)."""
+def sliced_golden(name):
+    """The record of a sliced circuit in the golden fixtures (made on the CPU
+    by tests/golden/make_network_fixtures.py): circuit, path, sliced bonds
+    and, where the oracle could run one, complex128 amplitudes of slices."""
     with open(os.path.join(REPO, "tests", "golden", "network_amplitudes.json")) as f:
-        return json.load(f)["config4"]
+        return json.load(f)[name]
 
 
-def run_config4_leg(batch=16, chunks=2, fp32_chunks=1):
-    """The spec workload beside the config-1 line: config 4 (53 qubits,
-    6 x 9 grid minus one site, 12 cycles, 64 slices of 1011 steps) in the
-    tensor-core AUTO form and in plain FP32, slices/s of each and their
-    ratio, plus each form's error on two single slices against the
-    complex128 oracle amplitudes of the golden fixture."""
+def run_sliced_leg(name, batch, chunks, fp32_chunks=1):
+    """A sliced circuit of the golden fixtures beside the config-1 line, in
+    the tensor-core AUTO form and in plain FP32: slices/s of each and their
+    ratio (the benchmark spec's target is >= 3x), and each form's error on single
+    slices against the complex128 oracle amplitudes of the fixture where it
+    has them (config 4), else AUTO's difference from FP32 (config 2)."""
     import jet_gb300 as jet
     from jet_gb300 import capi, circuits
 
-    ent = config4_golden()
+    ent = sliced_golden(name)
     net = circuits.random_circuit_network(ent["rows"], ent["cols"], ent["cycles"],
                                           seed=ent["seed"], removed=tuple(ent["removed"]))
     path = [tuple(p) for p in ent["path"]]
@@ -630,31 +634,136 @@ def run_config4_leg(batch=16, chunks=2, fp32_chunks=1):
     for lab, sh, d in net.tensors:
         tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
     capi.set_auto_form(capi.PREC_FP16X3)
-    forms, errs = {}, {}
-    for name, prec, ch in (("auto", jet.PREC_AUTO, chunks), ("fp32", jet.PREC_FP32, fp32_chunks)):
-        forms[name], info = time_sliced_form(jet, tn, path, sliced, prec, batch, ch)
+    forms, errs, amps = {}, {}, {}
+    for fname, prec, ch in (("auto", jet.PREC_AUTO, chunks),
+                            ("fp32", jet.PREC_FP32, fp32_chunks)):
+        forms[fname], info = time_sliced_form(jet, tn, path, sliced, prec, batch, ch)
+        amps[fname] = info["amp"]
+        if not ent["slices"]:
+            continue
         one = jet.SlicedContractorC64(tn, path, sliced, prec)
         one.set_batch_size(1)
-        errs[name] = {}
+        errs[fname] = {}
         for v, rec in ent["slices"].items():
             got = one.contract(int(v), 1)[0]
             want = complex(*rec["oracle_c128"])
-            errs[name]["slice_%s" % v] = abs(got - want) / abs(want)
+            errs[fname]["slice_%s" % v] = abs(got - want) / abs(want)
         del one
-    for name in forms:
-        forms[name]["rel_err_vs_fp64"] = max(errs[name].values())
-        forms[name]["rel_err_per_slice"] = errs[name]
-    return {"workload": "config 4: 6x9 grid minus site %d, %d cycles, %d qubits, %d sliced bonds "
-                        "(%d slices), greedy path of %d steps, %d slices per batch"
-                        % (ent["removed"][0], ent["cycles"], ent["rows"] * ent["cols"] - 1,
-                           len(sliced), info["num_slices"], len(path), batch),
-            "unit": "slices/s", "slice_pathinfo_flops": info["slice_flops"],
-            "forms": forms,
-            "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
-            "error_reference": "complex128 oracle amplitudes of slices %s (golden fixture)"
-                               % ", ".join(sorted(ent["slices"], key=int)),
-            "timing": "host clock around each synchronous chunk replay (graph launch + FP64 "
-                      "read-back); warm-up chunk excluded"}
+    for fname in errs:
+        forms[fname]["rel_err_vs_fp64"] = max(errs[fname].values())
+        forms[fname]["rel_err_per_slice"] = errs[fname]
+    n_q = ent["rows"] * ent["cols"] - len(ent["removed"])
+    out = {"workload": "config %s: %dx%d grid%s, %d cycles, %d qubits, %d sliced bonds "
+                       "(%d slices), greedy path of %d steps, %d slices per batch"
+                       % (name[-1], ent["rows"], ent["cols"],
+                          " minus site %d" % ent["removed"][0] if ent["removed"] else "",
+                          ent["cycles"], n_q, len(sliced), info["num_slices"], len(path), batch),
+           "unit": "slices/s", "slice_pathinfo_flops": info["slice_flops"],
+           "forms": forms,
+           "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
+           "timing": "host clock around each synchronous chunk replay (graph launch + FP64 "
+                     "read-back); warm-up chunk excluded"}
+    if errs:
+        out["error_reference"] = ("complex128 oracle amplitudes of slices %s (golden fixture)"
+                                  % ", ".join(sorted(ent["slices"], key=int)))
+    else:
+        out["rel_diff_auto_vs_fp32"] = (abs(amps["auto"] - amps["fp32"]) /
+                                        max(abs(amps["fp32"]), 1e-300))
+        out["error_reference"] = ("none on the CPU (one slice is 3.6e13 PathInfo flops); "
+                                  "AUTO's difference from plain FP32 over the timed chunks")
+    return out
+
+
+def shared_flop_fraction(net, path, sliced, varying):
+    """PathInfo flops of the steps that depend neither on the leaves in
+    `varying` nor on a sliced bond, as a fraction of one slice's flops: the
+    work one run shares across the leaves' alternatives and the slices."""
+    dims = dict(net.index_dims())
+    for x in sliced:
+        dims[x] = 1
+    sl = set(sliced)
+    nodes = {i: (list(l), i in varying or any(x in sl for x in l))
+             for i, (l, _, _) in enumerate(net.tensors)}
+    nid = len(nodes)
+    total = shared = 0.0
+    for a, b in path:
+        la, va = nodes.pop(a)
+        lb, vb = nodes.pop(b)
+        out = [x for x in la if x not in lb] + [x for x in lb if x not in la]
+        fl = 2.0 * math.prod(dims[x] for x in out) * math.prod(dims[x] for x in la if x in lb)
+        total += fl
+        if not (va or vb):
+            shared += fl
+        nodes[nid] = (out, va or vb)
+        nid += 1
+    return shared / total
+
+
+def run_bitstrings(args, jet, net, path, sliced, rows, cols, cycles, removed):
+    """The second pass of config 2: seeded-uniform output bitstrings as
+    alternatives of the output-cap leaves ("$b"), so that one run yields
+    several bitstrings' amplitudes and computes every bitstring-independent
+    intermediate once. Timed on a sample (bitstrings per run x slices per
+    batch x chunks), reported as bitstring-slices/s with the extrapolated
+    time for all bitstrings and slices; the amplitudes of the sample's
+    first chunk are checked against separate single-bitstring runs."""
+    from jet_gb300 import circuits
+
+    n_q = rows * cols - len(removed)
+    n_t = len(net.tensors)
+    cap_ids = list(range(n_t - n_q, n_t))  # output caps close the network, one per qubit
+    bits = np.random.default_rng(SEED + 1).integers(0, 2, size=(args.bitstrings, n_q))
+    nb = args.bitstring_chunk
+    batch = args.sliced_batch or 1
+    tn = jet.TensorNetwork(dtype="complex64")
+    for lab, sh, d in net.tensors:
+        tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
+
+    def contractor(chunk_bits):
+        sc = jet.SlicedContractorC64(tn, path, sliced, jet.PREC_AUTO)
+        sc.set_batch_size(batch)
+        for q, node in enumerate(cap_ids):
+            vals = []
+            for b in chunk_bits:
+                vals += [1, 0] if b[q] == 0 else [0, 1]
+            sc.set_leaf_alternatives(node, vals, len(chunk_bits))
+        return sc
+
+    sc = contractor(bits[:nb])
+    sc.contract(0, batch)  # warm-up: prefix, tuning, capture
+    count = batch * max(1, args.sliced_chunks or 1)
+    reps = []
+    while not reps or sum(reps) < 0.2:
+        t1 = time.perf_counter()
+        amps = sc.contract(batch, count)
+        reps.append(time.perf_counter() - t1)
+    dt = statistics.median(reps)
+    arena = sc.arena_bytes
+    del sc
+    # Consistency: each bitstring of the chunk contracted on its own.
+    worst = 0.0
+    for i in range(min(nb, 2)):
+        net_b = circuits.random_circuit_network(rows, cols, cycles, seed=SEED, removed=removed,
+                                                bitstring=bits[i])
+        tb = jet.TensorNetwork(dtype="complex64")
+        for lab, sh, d in net_b.tensors:
+            tb.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
+        one = jet.SlicedContractorC64(tb, path, sliced, jet.PREC_AUTO)
+        one.set_batch_size(batch)
+        want = one.contract(batch, count)[0]
+        del one
+        worst = max(worst, abs(amps[i] - want) / max(abs(want), 1e-300))
+    rate = nb * count / dt
+    n_slices = 2 ** len(sliced)
+    return {"bitstrings": args.bitstrings, "bitstrings_per_run": nb, "slices_per_batch": batch,
+            "slices_timed": count, "bitstring_slices_per_s": rate,
+            "extrapolated_all_s": args.bitstrings * n_slices / rate,
+            "arena_gb": arena / 1e9,
+            "shared_flop_fraction": shared_flop_fraction(net, path, sliced, set(cap_ids)),
+            "rel_diff_vs_single_bitstring_runs": worst,
+            "sharing": "every intermediate that depends on no output cap (and the "
+                       "slice-independent prefix) is computed once per run for all its "
+                       "bitstrings"}
 
 
 def run_sliced(args, rank, world, local_rank):
@@ -684,12 +793,29 @@ def run_sliced(args, rank, world, local_rank):
     else:
         net = circuits.random_circuit_network(rows, cols, cycles, seed=SEED, removed=removed)
     path = circuits.best_gain_path(net, restarts)
-    sliced = circuits.choose_slices(net, path, n_sliced) if n_sliced else []
-    plan_s = time.perf_counter() - t0
-    full_flops, log2_big = circuits.path_cost(net, path)
     tn = jet.TensorNetwork(dtype="complex64")
     for lab, sh, d in net.tensors:
         tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d), dtype="complex64"))
+    budget = None
+    if args.config in MEMORY_BUDGET and not args.sliced_batch:
+        from jet_gb300 import slicing
+
+        # The bonds for both the tensor-core and the plain form's plans.
+        cap = MEMORY_BUDGET[args.config]
+        sliced, need, batch = slicing.choose_slices_for_memory(net, path, tn, batch, cap,
+                                                               jet.PREC_AUTO, min_count=n_sliced)
+        sliced, need_fp32, _ = slicing.choose_slices_for_memory(net, path, tn, batch, cap,
+                                                                jet.PREC_FP32,
+                                                                min_count=len(sliced))
+        n_sliced = len(sliced)
+        budget = {"hbm_budget_gb": cap / 1e9, "slices_per_batch": batch,
+                  "sliced_bonds": n_sliced,
+                  "planned_device_gb": {"auto": need / 1e9, "fp32": need_fp32 / 1e9},
+                  "rule": "fewest bonds (greedy slicer order) whose chunk plan fits the budget"}
+    else:
+        sliced = circuits.choose_slices(net, path, n_sliced) if n_sliced else []
+    plan_s = time.perf_counter() - t0
+    full_flops, log2_big = circuits.path_cost(net, path)
     forms = {}
     amps = {}
     # (name, precision, split form of AUTO's tensor-core steps)
@@ -809,6 +935,16 @@ def run_sliced(args, rank, world, local_rank):
         "slice_vs_fp64": slice_check,
         "plan_seconds": plan_s,
     }
+    if args.bitstrings and sliced:
+        line["bitstring_pass"] = run_bitstrings(args, jet, net, path, sliced, rows, cols, cycles,
+                                                removed)
+    if sliced:
+        pi_big = circuits.path_cost(net, path, sliced)[1]
+        line["slicing"] = dict(budget or {}, slices_total=qd ** n_sliced,
+                               log2_largest_intermediate_per_slice=pi_big,
+                               pathinfo_flops_per_slice=slice_flops)
+        line["extrapolated_full_amplitude_s"] = {
+            f: qd ** n_sliced / forms[f]["slices_per_s"] for f in forms}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -992,7 +1128,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sliced", action="store_true",
-                    help="config 1: skip the config-4 sliced leg (AUTO vs plain FP32 slices/s)")
+                    help="config 1: skip the sliced legs (configs 4 and 2: AUTO vs plain FP32 "
+                         "slices/s)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: rank-25 x rank-25 (M = N = 2^12, K = 2^13)")
     ap.add_argument("--kernels-only", action="store_true",
@@ -1011,6 +1148,11 @@ def main():
     ap.add_argument("--sliced-forms", default="auto,tuned,auto_tf32,fp32",
                     help="forms timed by the sliced configs (comma list of auto (FP16x3 on "
                          "the tensor-core steps), auto_tf32, bf16x3, fp32)")
+    ap.add_argument("--bitstrings", type=int, default=0,
+                    help="sliced configs: also run the bitstring pass over this many "
+                         "seeded-uniform output bitstrings (config 2: 256), timed on a sample")
+    ap.add_argument("--bitstring-chunk", type=int, default=4,
+                    help="bitstrings per run of the bitstring pass (alternatives of the caps)")
     ap.add_argument("--sliced-batch", type=int, default=0,
                     help="slices per batch of the sliced configs (0: the config's own)")
     ap.add_argument("--sliced-chunks", type=int, default=0,

@@ -527,6 +527,17 @@ int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
                         uint64_t n_values, void *out, int dtype, void *stream);
 
 /*
+ * Adjoint of jetgpu_slice_gather for one slice value: full[positions of
+ * slice `value`] += sliced, element for element (`sliced` holds out_size
+ * elements in the order jetgpu_slice_gather writes them; `full` has `shape`).
+ * The gradient of Tensor::SliceIndex (Tensor.hpp:493-526), used by the
+ * adjoint of sliced network contractions. No counterpart in the reference.
+ */
+int jetgpu_slice_scatter_add(const void *sliced, int rank, const uint64_t *shape, int n_axes,
+                             const int32_t *axes, const uint64_t *value_strides, uint64_t value,
+                             void *full, int dtype, void *stream);
+
+/*
  * jetgpu_slice_gather with the first slice value read from device memory
  * (*first_value_dev) when the kernel runs, so that one captured CUDA graph can
  * be replayed over successive chunks of slices; jetgpu_counter_add advances

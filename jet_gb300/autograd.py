@@ -19,12 +19,24 @@ keeps only the leaves: backward recomputes the intermediates (checkpointing),
 so memory stays at one forward's worth plus the gradients. Every contraction,
 conjugation and transpose runs in libjetgpu.so (jetgpu_contract,
 jetgpu_conj, jetgpu_permute).
+
+Sliced networks (`sliced` labels, TensorNetwork::SliceIndices semantics,
+TensorNetwork.hpp:210-284): the value is the sum over every slice value of
+the network with those bonds fixed. Forward and backward both run slice by
+slice, recomputing each slice's intermediates from the leaves, so the memory
+held is one slice's forward and gradients, not the whole network's. A
+slice's leaf gradients are added into the full leaves' gradients at that
+slice's positions (jetgpu_slice_scatter_add, the adjoint of the device
+SliceIndex gather). `memory_budget` (bytes) picks the sliced bonds: the
+greedy slicer's bonds are added until one slice's checkpointed forward plus
+the gradients fits.
 """
 from __future__ import annotations
 
 import dataclasses
 from typing import List, Sequence, Tuple
 
+import numpy as np
 import torch
 
 from . import capi
@@ -150,34 +162,157 @@ def _backward(plan: ContractionPlan, vals, grad_out, precision: int):
     return grads[: plan.num_leaves]
 
 
+class SlicedPlan:
+    """A path over the leaves with the `sliced` bonds fixed: per leaf the
+    sliced axes (jetgpu_slice_gather's value strides: row-major over the
+    sliced bonds, as SliceIndices unravels a slice value) and the plan of the
+    sliced network (each leaf keeps its other axes in their order)."""
+
+    def __init__(self, plan: ContractionPlan, path: Sequence[Tuple[int, int]],
+                 sliced: Sequence[str]):
+        self.full = plan
+        self.sliced = list(sliced)
+        dims = [plan.dims[x] for x in self.sliced]
+        strides = [1] * len(dims)
+        for j in range(len(dims) - 2, -1, -1):
+            strides[j] = strides[j + 1] * dims[j + 1]
+        self.num_slices = 1
+        for d in dims:
+            self.num_slices *= d
+        pos = {x: j for j, x in enumerate(self.sliced)}
+        self.leaf_axes: List[List[int]] = []
+        self.leaf_strides: List[List[int]] = []
+        labels, shapes = [], []
+        for i in range(plan.num_leaves):
+            lab, sh = plan.labels[i], plan.shapes[i]
+            axes = [a for a, x in enumerate(lab) if x in pos]
+            self.leaf_axes.append(axes)
+            self.leaf_strides.append([strides[pos[lab[a]]] for a in axes])
+            labels.append([x for x in lab if x not in pos])
+            shapes.append([d for x, d in zip(lab, sh) if x not in pos])
+        self.sub = ContractionPlan(labels, shapes, path)
+
+    def gather(self, leaves, v: int):
+        """The leaves of slice value v (flat device tensors)."""
+        out = []
+        for i, x in enumerate(leaves):
+            axes = self.leaf_axes[i]
+            if not axes:
+                out.append(x)
+                continue
+            out.append(capi.slice_gather(x, self.full.shapes[i], axes, self.leaf_strides[i], v,
+                                         1))
+        return out
+
+
+def checkpoint_bytes(plan: ContractionPlan, itemsize: int) -> int:
+    """Device bytes of one recomputing backward over `plan`: every node of
+    the forward kept for the reverse sweep, the largest intermediate's
+    gradient twice over (the gradient in flight and its transpose) and one
+    gradient per leaf."""
+    sizes = [1] * len(plan.shapes)
+    for i, sh in enumerate(plan.shapes):
+        for d in sh:
+            sizes[i] *= d
+    leaves = sum(sizes[: plan.num_leaves])
+    inter = sizes[plan.num_leaves:]
+    return itemsize * (sum(sizes) + 2 * (max(inter) if inter else 0) + leaves)
+
+
+def slices_for_budget(labels, shapes, path, budget_bytes: float, itemsize: int = 8,
+                      max_count: int = 24) -> List[str]:
+    """The fewest bonds, in the greedy slicer's order
+    (circuits.choose_slices), for which one slice's checkpointed backward fits
+    `budget_bytes` (checkpoint_bytes of the sliced plan, plus the full leaves'
+    gradients). Raises ValueError when `max_count` bonds do not fit."""
+    from . import circuits
+
+    net = circuits.Network([(list(l), list(s), None) for l, s in zip(labels, shapes)])
+    full = ContractionPlan(labels, shapes, path)
+    leaf_bytes = itemsize * sum(int(np.prod(s)) if len(s) else 1 for s in shapes)
+    for count in range(0, max_count + 1):
+        sliced = circuits.choose_slices(net, path, count) if count else []
+        sub = SlicedPlan(full, path, sliced).sub if sliced else full
+        if checkpoint_bytes(sub, itemsize) + leaf_bytes <= budget_bytes:
+            return sliced
+    raise ValueError("no slicing of up to %d bonds fits %.3g bytes" % (max_count, budget_bytes))
+
+
+def _sliced_forward(sp: SlicedPlan, leaves, precision: int):
+    total = None
+    for v in range(sp.num_slices):
+        out = _forward(sp.sub, sp.gather(leaves, v), precision, keep=False)[-1]
+        total = out if total is None else capi.add(total, out)
+    return total
+
+
+def _sliced_backward(sp: SlicedPlan, leaves, grad_out, precision: int):
+    grads = [None] * sp.full.num_leaves
+    for v in range(sp.num_slices):
+        vals = _forward(sp.sub, sp.gather(leaves, v), precision, keep=True)
+        g = _backward(sp.sub, vals, grad_out, precision)
+        for i, gi in enumerate(g):
+            if gi is None:
+                continue
+            if not sp.leaf_axes[i]:
+                grads[i] = gi if grads[i] is None else capi.add(grads[i], gi)
+                continue
+            if grads[i] is None:
+                grads[i] = torch.zeros_like(leaves[i])
+            capi.slice_scatter_add(gi, sp.full.shapes[i], sp.leaf_axes[i], sp.leaf_strides[i], v,
+                                   grads[i])
+    return grads
+
+
 class _NetworkContraction(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, plan: ContractionPlan, precision: int, *leaves):
+    def forward(ctx, plan, precision: int, *leaves):
         flat = [l.contiguous().reshape(-1) for l in leaves]
-        vals = _forward(plan, flat, precision, keep=False)
+        if isinstance(plan, SlicedPlan):
+            res = _sliced_forward(plan, flat, precision)
+            out_shape = plan.sub.out_shape
+        else:
+            res = _forward(plan, flat, precision, keep=False)[-1]
+            out_shape = plan.out_shape
         ctx.plan = plan
         ctx.precision = precision
         ctx.leaf_shapes = [tuple(l.shape) for l in leaves]
         ctx.save_for_backward(*leaves)
-        return vals[-1].reshape(plan.out_shape)
+        return res.reshape(out_shape)
 
     @staticmethod
     def backward(ctx, grad_out):
         leaves = [l.contiguous().reshape(-1) for l in ctx.saved_tensors]
-        vals = _forward(ctx.plan, leaves, ctx.precision, keep=True)
-        g = grad_out.contiguous().reshape(-1).to(vals[-1].dtype)
-        grads = _backward(ctx.plan, vals, g, ctx.precision)
+        g = grad_out.contiguous().reshape(-1).to(leaves[0].dtype)
+        if isinstance(ctx.plan, SlicedPlan):
+            grads = _sliced_backward(ctx.plan, leaves, g, ctx.precision)
+        else:
+            vals = _forward(ctx.plan, leaves, ctx.precision, keep=True)
+            grads = _backward(ctx.plan, vals, g, ctx.precision)
         out = [None if gr is None else gr.reshape(s) for gr, s in zip(grads, ctx.leaf_shapes)]
         return (None, None, *out)
 
 
 def contract_network(leaves: Sequence[torch.Tensor], labels: Sequence[Sequence[str]],
                      path: Sequence[Tuple[int, int]], precision: int = capi.PREC_AUTO,
-                     plan: ContractionPlan = None) -> torch.Tensor:
+                     plan=None, sliced: Sequence[str] = None,
+                     memory_budget: float = None) -> torch.Tensor:
     """Contracts CUDA complex tensors `leaves` (labels[i] per leaf) along
-    `path`; differentiable with respect to every leaf."""
+    `path`; differentiable with respect to every leaf.
+
+    sliced: bonds to slice; the value is the sum over their slice values,
+    and forward and backward run (and recompute) one slice at a time.
+    memory_budget: device bytes for one slice's checkpointed backward; picks
+    `sliced` (slices_for_budget) when `sliced` is not given. `plan` (a
+    ContractionPlan, or the SlicedPlan these build) skips the bookkeeping."""
     if plan is None:
-        plan = ContractionPlan(labels, [list(l.shape) for l in leaves], path)
+        shapes = [list(l.shape) for l in leaves]
+        if sliced is None and memory_budget is not None:
+            sliced = slices_for_budget(labels, shapes, path, memory_budget,
+                                       leaves[0].element_size())
+        plan = ContractionPlan(labels, shapes, path)
+        if sliced:
+            plan = SlicedPlan(plan, path, sliced)
     return _NetworkContraction.apply(plan, precision, *leaves)
 
 

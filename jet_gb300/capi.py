@@ -132,6 +132,8 @@ lib.jetgpu_slice_sum_f64.argtypes = [_vp, ctypes.c_uint64, ctypes.c_uint64, ctyp
 lib.jetgpu_slice_gather.argtypes = [_vp, ctypes.c_int, _u64p, ctypes.c_int, _i32p, _u64p,
                                     ctypes.c_uint64, ctypes.c_uint64, _vp, ctypes.c_int, _vp]
 lib.jetgpu_max_exponent.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, _vp]
+lib.jetgpu_slice_scatter_add.argtypes = [_vp, ctypes.c_int, _u64p, ctypes.c_int, _i32p, _u64p,
+                                         ctypes.c_uint64, _vp, ctypes.c_int, _vp]
 lib.jetgpu_take_device_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
 lib.jetgpu_probe_bounded_wait.argtypes = [ctypes.c_uint, _vp]
 lib.jetgpu_device_info.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
@@ -483,6 +485,15 @@ def slice_gather(x, shape, axes, value_strides, first_value, n_values, out=None,
                                   u64(value_strides), first_value, n_values, _ptr(out),
                                   dtype_code(x.dtype), _stream(stream)))
     return out
+
+
+def slice_scatter_add(sliced, shape, axes, value_strides, value, full, stream=None):
+    """full[positions of slice `value`] += sliced (adjoint of slice_gather for
+    one slice value); returns `full`."""
+    check(lib.jetgpu_slice_scatter_add(_ptr(sliced), len(shape), u64(shape), len(axes),
+                                       i32(axes), u64(value_strides), int(value), _ptr(full),
+                                       dtype_code(full.dtype), _stream(stream)))
+    return full
 
 
 def max_exponent(x, stream=None, out=None):

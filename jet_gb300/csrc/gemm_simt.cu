@@ -72,8 +72,11 @@ __global__ void __launch_bounds__(256)
 
     const int tid = threadIdx.x;
     const int tx = tid % kTX, ty = tid / kTX;
-    const int64_t m0 = (int64_t)blockIdx.y * BM;
-    const int64_t n0 = (int64_t)blockIdx.x * BN;
+    // Tiles in row-major order over one grid dimension (N tiles fastest), so
+    // M may exceed 65535 tiles (2^23 rows).
+    const int64_t tiles_n = (N + BN - 1) / BN;
+    const int64_t m0 = ((int64_t)blockIdx.x / tiles_n) * BM;
+    const int64_t n0 = ((int64_t)blockIdx.x % tiles_n) * BN;
 
     V acc[TM][kTN];
 #pragma unroll
@@ -445,8 +448,9 @@ int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename
             ? GemmSplits(tn * tm * batch, batch, K, batch * M * N * (int64_t)sizeof(V))
             : 1;
     const int64_t kchunk = (K + S - 1) / S;
-    const dim3 grid((unsigned)tn, (unsigned)tm, (unsigned)(batch * S));
-    JETGPU_REQUIRE(tm <= 65535 && batch * S <= 65535, "product too large for one launch");
+    JETGPU_REQUIRE(tn * tm <= 0x7fffffffLL && batch * S <= 65535,
+                   "product too large for one launch");
+    const dim3 grid((unsigned)(tn * tm), 1u, (unsigned)(batch * S));
     V *dst = S > 1 ? (V *)ws : C;
     if (GemmTM<T>(M) == 2)
         gemm_kernel<T, 2><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa, sb, (int)S,

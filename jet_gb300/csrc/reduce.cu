@@ -124,6 +124,34 @@ __global__ void slice_gather_kernel(const __grid_constant__ SliceParams p,
     }
 }
 
+// Adjoint of slice_gather_kernel for one slice value: full[src] += sliced[o]
+// at the same positions. Within one value every o has its own src, so the
+// read-modify-write needs no atomics and the result is deterministic.
+template <typename E, typename R>
+__global__ void slice_scatter_add_kernel(const __grid_constant__ SliceParams p,
+                                         const E *__restrict__ sliced, E *__restrict__ full)
+{
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < p.total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = p.first_value;
+        uint64_t o = idx;
+        uint64_t dst = 0;
+        for (int j = 0; j < p.n_axes; ++j)
+            dst += ((v / p.value_stride[j]) % p.fixed_dim[j]) * p.fixed_stride[j];
+        for (int j = p.free_rank - 1; j >= 0; --j) {
+            const uint64_t d = p.free_dims[j];
+            const uint64_t q = o / d;
+            dst += (o - q * d) * p.free_strides[j];
+            o = q;
+        }
+        const E g = sliced[idx];
+        E f = full[dst];
+        f.x = (R)(f.x + g.x);
+        f.y = (R)(f.y + g.y);
+        full[dst] = f;
+    }
+}
+
 __global__ void init_exp_kernel(int *e) { *e = kExpZero; }
 
 __global__ void counter_add_kernel(uint64_t *c, uint64_t delta) { *c += delta; }
@@ -266,7 +294,7 @@ int jetgpu_slice_sum_f64(const void *results, uint64_t n_slices, uint64_t size,
 static int SliceGatherImpl(const void *in, int rank, const uint64_t *shape, int n_axes,
                            const int32_t *axes, const uint64_t *value_strides,
                            uint64_t first_value, const uint64_t *first_dev, uint64_t n_values,
-                           void *out, int dtype, void *stream);
+                           void *out, int dtype, void *stream, bool scatter_add = false);
 
 int jetgpu_slice_gather(const void *in, int rank, const uint64_t *shape,
                         int n_axes, const int32_t *axes,
@@ -287,6 +315,14 @@ int jetgpu_slice_gather_at(const void *in, int rank, const uint64_t *shape, int 
                            n_values, out, dtype, stream);
 }
 
+int jetgpu_slice_scatter_add(const void *sliced, int rank, const uint64_t *shape, int n_axes,
+                             const int32_t *axes, const uint64_t *value_strides, uint64_t value,
+                             void *full, int dtype, void *stream)
+{
+    return SliceGatherImpl(sliced, rank, shape, n_axes, axes, value_strides, value, nullptr, 1,
+                           full, dtype, stream, true);
+}
+
 int jetgpu_counter_add(uint64_t *counter_dev, uint64_t delta, void *stream)
 {
     ClearError();
@@ -298,7 +334,7 @@ int jetgpu_counter_add(uint64_t *counter_dev, uint64_t delta, void *stream)
 static int SliceGatherImpl(const void *in, int rank, const uint64_t *shape, int n_axes,
                            const int32_t *axes, const uint64_t *value_strides,
                            uint64_t first_value, const uint64_t *first_dev, uint64_t n_values,
-                           void *out, int dtype, void *stream)
+                           void *out, int dtype, void *stream, bool scatter_add)
 {
     ClearError();
     JETGPU_REQUIRE(dtype == JETGPU_C64 || dtype == JETGPU_C128, "bad dtype");
@@ -334,6 +370,16 @@ static int SliceGatherImpl(const void *in, int rank, const uint64_t *shape, int 
         return JETGPU_OK;
     JETGPU_REQUIRE(in && out, "null pointer");
     unsigned grid = GridFor((p.total + kThreads - 1) / kThreads, 8);
+    if (scatter_add) {
+        // `in` is the sliced tensor, `out` the full one it is added into.
+        if (dtype == JETGPU_C64)
+            slice_scatter_add_kernel<float2, float><<<grid, kThreads, 0, AsStream(stream)>>>(
+                p, (const float2 *)in, (float2 *)out);
+        else
+            slice_scatter_add_kernel<double2, double><<<grid, kThreads, 0, AsStream(stream)>>>(
+                p, (const double2 *)in, (double2 *)out);
+        return CheckLaunch("slice_scatter_add_kernel");
+    }
     if (dtype == JETGPU_C64)
         slice_gather_kernel<uint2><<<grid, kThreads, 0, AsStream(stream)>>>(
             p, (const uint2 *)in, (uint2 *)out, first_dev);

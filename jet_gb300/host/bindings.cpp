@@ -267,7 +267,8 @@ template <class T> void BindSliced(py::module_ &m)
         .def_property_readonly("result_shape", &sc_t::GetResultShape)
         .def_property_readonly("slice_flops", &sc_t::GetSliceFlops)
         .def_property_readonly("slice_dependent_flops", &sc_t::GetSliceDependentFlops)
-        .def_property_readonly("arena_bytes", &sc_t::GetArenaBytes);
+        .def_property_readonly("arena_bytes", &sc_t::GetArenaBytes)
+        .def("estimate_device_bytes", &sc_t::EstimateDeviceBytes);
 }
 
 template <class T> void BindPathInfoCtor(py::class_<Jet::PathInfo> &c)

@@ -219,6 +219,33 @@ template <class T = std::complex<float>> class SlicedContractor {
         return arena_bytes_;
     }
 
+    // Device bytes a contraction at the current batch size holds: the chunk
+    // arena, the largest step's workspace, the slice-independent buffers and
+    // the prefix's peak of transient intermediates. Planned without
+    // allocating, so slice counts and batch sizes can be chosen against a
+    // memory budget before any of it is committed.
+    size_t EstimateDeviceBytes()
+    {
+        if (!planned_)
+            Plan(false);
+        size_t persistent = 0, transient = 0, peak = 0;
+        for (size_t i = 0; i < nodes_.size(); ++i)
+            if (!nodes_[i].chunk && persist_[i])
+                persistent += nodes_[i].bytes;
+        for (size_t i = 0; i < steps_.size(); ++i) {
+            const Step &st = steps_[i];
+            if (st.chunk)
+                continue;
+            if (!persist_[st.out])
+                transient += nodes_[st.out].bytes;
+            peak = std::max(peak, transient);
+            for (int id : {st.a, st.b})
+                if (!persist_[id] && prefix_last_use_[id] == (int)i)
+                    transient -= nodes_[id].bytes;
+        }
+        return arena_bytes_ + ws_bytes_ + persistent + peak + result_size_ * 16;
+    }
+
   private:
     struct Node {
         std::vector<std::string> labels;
@@ -334,7 +361,9 @@ template <class T = std::complex<float>> class SlicedContractor {
         graph_ = nullptr;
     }
 
-    void Plan()
+    // allocate = false computes the layout only (EstimateDeviceBytes); the
+    // contractor then stays unplanned.
+    void Plan(bool allocate = true)
     {
         using namespace Utilities;
         ReleaseGraph();
@@ -582,6 +611,10 @@ template <class T = std::complex<float>> class SlicedContractor {
                     }
         }
         arena_bytes_ = top;
+        if (!allocate) {
+            PlanPersistence();
+            return;
+        }
         arena_ = Gpu::DeviceBuffer(std::max<size_t>(arena_bytes_, 256));
         ws_ = Gpu::DeviceBuffer(ws_bytes_);
         acc_ = Gpu::DeviceBuffer(std::max<size_t>(result_size_ * 16, 16));
@@ -597,10 +630,21 @@ template <class T = std::complex<float>> class SlicedContractor {
             Gpu::Synchronize();
         }
         final_tmp_ = Gpu::DeviceBuffer(final_perm_needed_ ? nodes_[final_id_].bytes : 0);
-        // Slice-independent tensors that the captured graph reads (leaves,
-        // prefix outputs consumed by "$s" steps, the final result) keep one
-        // buffer for the contractor's lifetime; other prefix intermediates
-        // live only while the prefix runs.
+        PlanPersistence();
+        for (size_t i = 0; i < nodes_.size(); ++i)
+            if (!nodes_[i].chunk && persist_[i])
+                nodes_[i].own = Gpu::DeviceBuffer(nodes_[i].bytes);
+        BuildGroups();
+        prefix_done_ = false;
+        planned_ = true;
+    }
+
+    // Slice-independent tensors that the captured graph reads (leaves,
+    // prefix outputs consumed by "$s" steps, the final result) keep one
+    // buffer for the contractor's lifetime; other prefix intermediates live
+    // only while the prefix runs.
+    void PlanPersistence()
+    {
         persist_.assign(nodes_.size(), 0);
         for (size_t i = 0; i < num_leaves_; ++i)
             persist_[i] = 1;
@@ -615,12 +659,6 @@ template <class T = std::complex<float>> class SlicedContractor {
                 prefix_last_use_[steps_[i].a] = (int)i;
                 prefix_last_use_[steps_[i].b] = (int)i;
             }
-        for (size_t i = 0; i < nodes_.size(); ++i)
-            if (!nodes_[i].chunk && persist_[i])
-                nodes_[i].own = Gpu::DeviceBuffer(nodes_[i].bytes);
-        BuildGroups();
-        prefix_done_ = false;
-        planned_ = true;
     }
 
     // Tiny slice-dependent steps that AUTO and TUNED give to the plain

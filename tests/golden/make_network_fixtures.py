@@ -23,7 +23,10 @@ Writes into tests/golden/:
                the compiled reference in complex<float> for slice 0;
       config4: the 53-qubit circuit (6 x 9 grid minus site 5, 12 cycles,
                seed 20240601) with its greedy path and 6 sliced bonds, and
-               the complex128 oracle amplitudes of slices 0 and 37.
+               the amplitudes of slices 0 and 37 from the complex128 oracle
+               and from the compiled reference in complex<float>;
+      config2: the 49-qubit circuit (7 x 7 grid, 14 cycles) with its greedy
+               path and 12 sliced bonds (4096 slices).
 
   config3_gradient.json
       The 36-qubit parameterised circuit (6 x 6, 10 layers, 720 angles):
@@ -35,7 +38,7 @@ Usage (in a container with the reference tree; JET_REF overrides its
 location):
 
   make -C oracle/ref_build
-  python tests/golden/make_network_fixtures.py [--only m10,m12,config4,config3]
+  python tests/golden/make_network_fixtures.py [--only m10,m12,config4,config2,config3]
 """
 from __future__ import annotations
 
@@ -55,6 +58,7 @@ SEED = 20240601
 M12_SLICED = ["h5", "m", "H10", "w", "y", "J", "S", "G10", "P0"]
 C4 = dict(rows=6, cols=9, cycles=12, removed=[5], n_sliced=6, restarts=48, slices=[0, 37])
 C3 = dict(rows=6, cols=6, layers=10, restarts=8)
+C2 = dict(rows=7, cols=7, cycles=14, removed=[], n_sliced=12, restarts=48)
 
 
 def reference_root() -> str:
@@ -182,8 +186,26 @@ def make_config4(amps):
     for v in C4["slices"]:
         t0 = time.time()
         ent["slices"][str(v)] = {"oracle_c128": _pair(_oracle_amplitude(plain, path, sliced, v))}
+        ent["slices"][str(v)]["ref_c64"] = _pair(
+            _ref_amplitude(plain, path, np.complex64, sliced, v)[0])
         print("config4 slice", v, "%.1f s" % (time.time() - t0), flush=True)
     amps["config4"] = ent
+
+
+def make_config2(amps):
+    """The 49-qubit circuit's path and 12 sliced bonds (no amplitude: one
+    slice is 3.6e13 PathInfo flops with intermediates of 2^30 elements, too
+    large for the CPU oracle here)."""
+    from jet_gb300 import circuits
+
+    net = circuits.random_circuit_network(C2["rows"], C2["cols"], C2["cycles"], seed=SEED)
+    path = circuits.best_gain_path(net, C2["restarts"])
+    sliced = circuits.choose_slices(net, path, C2["n_sliced"])
+    flops, big = circuits.path_cost(net, path, sliced)
+    ent = {k: C2[k] for k in ("rows", "cols", "cycles", "removed")}
+    ent.update(seed=SEED, path=[list(p) for p in path], sliced=sliced,
+               slice_pathinfo_flops=flops, log2_largest=big, slices={})
+    amps["config2"] = ent
 
 
 def make_config3():
@@ -243,7 +265,7 @@ def einsum_along_path(leaves, labels, path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="m10,m12,config4,config3")
+    ap.add_argument("--only", default="m10,m12,config4,config2,config3")
     which = set(ap.parse_args().only.split(","))
     amp_path = os.path.join(HERE, "network_amplitudes.json")
     amps = {}
@@ -253,6 +275,8 @@ def main():
     make_m10_m12(which, amps)
     if "config4" in which:
         make_config4(amps)
+    if "config2" in which:
+        make_config2(amps)
     with open(amp_path, "w") as f:
         json.dump(amps, f)
     if "config3" in which:

@@ -132,6 +132,13 @@ def _config4_network(jet, ent):
 
 @pytest.mark.parametrize("precision", [2, 5, 0])
 def test_config4_slices_match_oracle(jet, amps, precision):
+    """AUTO and TUNED (tensor-core products on the large steps) within 1e-5 of
+    complex128. Plain FP32 -- complex64 with FP32 FMA, the arithmetic of the
+    reference's own complex<float> path -- within 1e-5, or where the
+    reference's own complex<float> result (compiled reference, golden) is
+    further than that from complex128, no further than it: on slice 37 the
+    reference's error is 2.05e-5 (the slice's amplitude is a quarter of slice
+    0's, with more cancellation)."""
     ent = amps["config4"]
     tn, path = _config4_network(jet, ent)
     sc = jet.SlicedContractorC64(tn, path, ent["sliced"], precision)
@@ -140,7 +147,10 @@ def test_config4_slices_match_oracle(jet, amps, precision):
     for v, rec in ent["slices"].items():
         got = sc.contract(int(v), 1)[0]
         want = _c(rec["oracle_c128"])
-        assert _rel(got, want) <= 1e-5, (v, _rel(got, want))
+        tol = 1e-5
+        if precision == 0:
+            tol = max(tol, _rel(_c(rec["ref_c64"]), want))
+        assert _rel(got, want) <= tol, (v, _rel(got, want), tol)
     from jet_gb300 import capi
 
     assert capi.take_device_status() == 0
