@@ -8,6 +8,9 @@ factories over the TensorC64/C128, ... classes) and the free functions
 slice runs as a CUDA kernel of libjetgpu.so (sm_103a). Importing the package
 fails when the native libraries are not built: there is no CPU fallback.
 
+The circuit front-end follows the reference's `jet.Circuit`, `jet.GateFactory`
+and state classes; `Circuit.tensor_network()` builds GPU tensors.
+
 Extras: `set_precision` (0 plain FP32, 1 TF32x3 tensor cores, 2 auto, 3 BF16x3, 4 FP16x3) and the
 raw C-ABI binding `jet_gb300.capi`.
 """
@@ -29,6 +32,9 @@ from ._jet_bindings import (  # noqa: F401
 )
 from .factory import *  # noqa: F401,F403
 from .io import TensorFileException, TensorNetworkFile, TensorNetworkSerializer  # noqa: F401
+from .gate import *  # noqa: F401,F403
+from .state import Qubit, QubitRegister, Qudit, QuditRegister, State  # noqa: F401
+from .circuit import Circuit, Operation, Wire  # noqa: F401
 
 PREC_FP32 = 0
 PREC_TF32X3 = 1

@@ -15,9 +15,16 @@
 // the stream-ordered allocator as soon as their last consumer is enqueued
 // (the deletion tasks), so peak device memory follows the path's liveness.
 // The reduction of equal-shaped results runs as an FP64 sum on the device.
+//
+// Repeated Contract() calls of the same tasks replay a CUDA graph: the first
+// call runs the tasks eagerly as above (keeping a copy of every leaf), the
+// second captures the contractions and result copies into one graph over an
+// arena planned from the tasks' liveness (PathInfo's step sizes), and that
+// call and every later one launch the graph, with no per-task host work.
 #pragma once
 
 #include <future>
+#include <map>
 #include <memory>
 #include <ostream>
 #include <string>
@@ -69,6 +76,7 @@ template <class TensorType> class TaskBasedContractor {
         const auto &steps = path_info.GetSteps();
         if (path.empty())
             return 0;
+        ResetReplay();
         const auto &nodes = tn.GetNodes();
         const size_t num_leaves = nodes.size();
         const size_t result_id = results_.size();
@@ -107,6 +115,7 @@ template <class TensorType> class TaskBasedContractor {
 
     size_t AddReductionTask() noexcept
     {
+        ResetReplay();
         if (reduced_)
             return 0;
         reduced_ = true;
@@ -116,6 +125,7 @@ template <class TensorType> class TaskBasedContractor {
 
     size_t AddDeletionTasks() noexcept
     {
+        ResetReplay();
         size_t count = 0;
         for (const auto &kv : name_to_parents_) {
             if (kv.second.empty())
@@ -129,10 +139,241 @@ template <class TensorType> class TaskBasedContractor {
     // Runs every task; the future is ready once the device work is complete.
     std::future<void> Contract()
     {
-        return std::async(std::launch::async, [this] { Run(); });
+        return std::async(std::launch::async, [this] {
+            if (!Replayable())
+                Run();
+            else if (runs_ == 0)
+                RunAndKeepLeaves();
+            else
+                Replay();
+            ++runs_;
+        });
     }
 
+    // Graph replay of repeated Contract() calls (default on); off: every call
+    // runs the tasks eagerly.
+    void SetGraphReplay(bool on)
+    {
+        replay_on_ = on;
+        ResetReplay();
+    }
+    // Whether the next Contract() launches a captured graph.
+    bool HasReplayGraph() const noexcept { return replay_.graph != nullptr; }
+
+    ~TaskBasedContractor() { ResetReplay(); }
+
   private:
+    // The replay runs on this package's Jet::Tensor; for other tensor types
+    // (CudaTensor) Contract() stays eager and S only names a valid type.
+    static constexpr bool kGpuTensor =
+        std::is_same_v<TensorType, Tensor<std::complex<float>>> ||
+        std::is_same_v<TensorType, Tensor<std::complex<double>>>;
+    using S = std::conditional_t<kGpuTensor, typename TensorType::scalar_type_t,
+                                 std::complex<float>>;
+
+    // What the captured graph reads and writes: leaf copies, one arena for
+    // the intermediates (first-fit over their lifetimes), the largest step's
+    // workspace, and per contraction task its operands' buffers and layout.
+    struct ReplayPlan {
+        struct Step {
+            size_t a, b, out;
+            typename Tensor<S>::ContractionLayout layout;
+        };
+        std::vector<Tensor<S>> leaves;             // by leaf slot
+        std::unordered_map<std::string, size_t> leaf_slot;
+        std::vector<Step> steps;
+        std::vector<size_t> offset, bytes;         // per buffer id
+        std::vector<int> leaf_of;                  // per buffer id: leaf slot or -1
+        std::vector<std::pair<size_t, size_t>> stores; // (buffer id, result index)
+        Gpu::DeviceBuffer arena, ws;
+        int precision = -1;
+        void *graph = nullptr;
+    };
+    ReplayPlan replay_;
+    bool replay_on_ = true;
+    size_t runs_ = 0;
+
+    bool Replayable() const noexcept { return kGpuTensor && replay_on_; }
+
+    void ResetReplay() noexcept
+    {
+        if (replay_.graph != nullptr)
+            jetgpu_graph_destroy(replay_.graph);
+        replay_ = ReplayPlan();
+        runs_ = 0;
+    }
+
+    // First run: the eager schedule, after copying every leaf the tasks read
+    // (the deletion tasks release the contractor's own leaves).
+    void RunAndKeepLeaves()
+    {
+        if constexpr (kGpuTensor) {
+            std::unordered_set<std::string> produced;
+            for (const Task &t : tasks_)
+                if (t.kind == Task::CONTRACT)
+                    produced.insert(t.name);
+            for (const Task &t : tasks_) {
+                if (t.kind != Task::CONTRACT)
+                    continue;
+                for (const std::string *in : {&t.input_1, &t.input_2})
+                    if (!produced.count(*in) && !replay_.leaf_slot.count(*in)) {
+                        replay_.leaf_slot.emplace(*in, replay_.leaves.size());
+                        replay_.leaves.push_back(*name_to_tensor_.at(*in));
+                    }
+            }
+            replay_.precision = Tensor<S>::template ContractPrecision<S>();
+        }
+        Run();
+    }
+
+    void Replay()
+    {
+        if constexpr (kGpuTensor) {
+            Gpu::Range range("Jet::TaskBasedContractor::Contract (graph)");
+            if (replay_.graph != nullptr &&
+                replay_.precision != Tensor<S>::template ContractPrecision<S>()) {
+                jetgpu_graph_destroy(replay_.graph);
+                replay_.graph = nullptr;
+                replay_.precision = Tensor<S>::template ContractPrecision<S>();
+            }
+            if (replay_.graph == nullptr)
+                Capture();
+            Gpu::Check(jetgpu_graph_launch(replay_.graph, Gpu::Stream()), "graph launch");
+            for (const auto &st : replay_.stores)
+                results_[st.second].GetMutableDeviceData(); // the host copy is stale
+            for (const Task &task : tasks_)
+                if (task.kind == Task::REDUCE)
+                    Reduce();
+            Gpu::Synchronize();
+        }
+    }
+
+    void Capture()
+    {
+        if constexpr (kGpuTensor) {
+            ReplayPlan &r = replay_;
+            r.steps.clear();
+            r.stores.clear();
+            std::unordered_map<std::string, size_t> id;
+            std::vector<Tensor<S>> shape_of; // per buffer id: labels and shape, no data
+            auto buffer = [&](const std::string &name) -> size_t {
+                const auto it = id.find(name);
+                if (it != id.end())
+                    return it->second;
+                const auto leaf = r.leaf_slot.at(name);
+                id.emplace(name, shape_of.size());
+                shape_of.push_back(Tensor<S>(r.leaves[leaf].GetIndices(), r.leaves[leaf].GetShape()));
+                r.leaf_of.push_back((int)leaf);
+                return shape_of.size() - 1;
+            };
+            const int dt = Gpu::DtypeCode<S>();
+            size_t ws = 0;
+            for (const Task &t : tasks_) {
+                if (t.kind == Task::CONTRACT) {
+                    const size_t a = buffer(t.input_1);
+                    const size_t b = buffer(t.input_2);
+                    auto layout = Tensor<S>::template LayoutOf<S>(shape_of[a], shape_of[b]);
+                    const auto &l = layout;
+                    ws = std::max(ws, jetgpu_contract_workspace_size(
+                                          (int)l.a_shape.size(), l.a_shape.data(), l.a_perm.data(),
+                                          (int)l.b_shape.size(), l.b_shape.data(), l.b_perm.data(),
+                                          l.m, l.n, l.k, dt, r.precision));
+                    id[t.name] = shape_of.size();
+                    shape_of.push_back(Tensor<S>(l.c_indices, l.c_shape));
+                    r.leaf_of.push_back(-1);
+                    r.steps.push_back({a, b, shape_of.size() - 1, std::move(layout)});
+                }
+                else if (t.kind == Task::STORE) {
+                    r.stores.emplace_back(id.at(t.name), t.result_id);
+                }
+            }
+            // Arena: first fit over each intermediate's lifetime (from its
+            // step to its last consumer; stored results are copied out by
+            // the task right after their step).
+            const size_t nb = shape_of.size();
+            std::vector<int> last(nb, -1);
+            for (size_t i = 0; i < r.steps.size(); ++i) {
+                last[r.steps[i].a] = (int)i;
+                last[r.steps[i].b] = (int)i;
+            }
+            r.offset.assign(nb, 0);
+            r.bytes.assign(nb, 0);
+            std::map<size_t, size_t> free_blocks;
+            size_t top = 0;
+            auto alloc = [&](size_t bytes) {
+                bytes = (bytes + 255) / 256 * 256;
+                for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it)
+                    if (it->second >= bytes) {
+                        const size_t off = it->first, rem = it->second - bytes;
+                        free_blocks.erase(it);
+                        if (rem)
+                            free_blocks[off + bytes] = rem;
+                        return off;
+                    }
+                top += bytes;
+                return top - bytes;
+            };
+            auto release = [&](size_t off, size_t bytes) {
+                bytes = (bytes + 255) / 256 * 256;
+                auto it = free_blocks.emplace(off, bytes).first;
+                auto nx = std::next(it);
+                if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+                    it->second += nx->second;
+                    free_blocks.erase(nx);
+                }
+                if (it != free_blocks.begin()) {
+                    auto pv = std::prev(it);
+                    if (pv->first + pv->second == it->first) {
+                        pv->second += it->second;
+                        free_blocks.erase(it);
+                    }
+                }
+            };
+            for (size_t i = 0; i < r.steps.size(); ++i) {
+                const auto &st = r.steps[i];
+                r.bytes[st.out] = std::max<size_t>(shape_of[st.out].GetSize(), 1) * sizeof(S);
+                r.offset[st.out] = alloc(r.bytes[st.out]);
+                for (size_t in : {st.a, st.b})
+                    if (r.leaf_of[in] < 0 && last[in] == (int)i)
+                        release(r.offset[in], r.bytes[in]);
+            }
+            r.arena = Gpu::DeviceBuffer(std::max<size_t>(top, 256));
+            r.ws = Gpu::DeviceBuffer(ws);
+            auto ptr = [&](size_t b) -> void * {
+                if (r.leaf_of[b] >= 0)
+                    return const_cast<S *>(r.leaves[r.leaf_of[b]].GetDeviceData());
+                return static_cast<char *>(r.arena.get()) + r.offset[b];
+            };
+            // Leaf and result buffers are resolved (and, if need be, uploaded)
+            // before the capture: nothing below may allocate or copy from host.
+            for (size_t b = 0; b < nb; ++b)
+                if (r.leaf_of[b] >= 0)
+                    ptr(b);
+            std::vector<void *> result_ptr(r.stores.size());
+            for (size_t i = 0; i < r.stores.size(); ++i)
+                result_ptr[i] = results_[r.stores[i].second].GetMutableDeviceData();
+            Gpu::Synchronize();
+            void *st = Gpu::Stream();
+            Gpu::Check(jetgpu_graph_begin(st), "capture begin");
+            size_t next_store = 0;
+            for (const auto &step : r.steps) {
+                const auto &l = step.layout;
+                Gpu::Check(jetgpu_contract(ptr(step.a), (int)l.a_shape.size(), l.a_shape.data(),
+                                           l.a_perm.data(), ptr(step.b), (int)l.b_shape.size(),
+                                           l.b_shape.data(), l.b_perm.data(), ptr(step.out), l.m,
+                                           l.n, l.k, dt, r.precision, JETGPU_ALGO_4M, 0, 0,
+                                           r.ws.get(), r.ws.size(), st),
+                           "ContractTensors (capture)");
+                while (next_store < r.stores.size() && r.stores[next_store].first == step.out) {
+                    Gpu::Check(jetgpu_memcpy(result_ptr[next_store], ptr(step.out),
+                                             r.bytes[step.out], 2, st),
+                               "result copy (capture)");
+                    ++next_store;
+                }
+            }
+            Gpu::Check(jetgpu_graph_end(st, &r.graph), "capture end");
+        }
+    }
     size_t num_threads_;
     std::vector<Task> tasks_;
     NameToTaskMap name_to_task_;

@@ -441,49 +441,72 @@ template <class T = std::complex<float>> class Tensor {
     }
     Tensor<T> Conj() const { return Conj<T>(*this); }
 
-    // Tensor::ContractTensors (reference Tensor.hpp:708-752): labels
-    // left = A\B (A order), right = B\A (B order), common = A∩B (A order);
-    // C carries left ++ right.
+    // The device call of one pairwise contraction, from the operands' labels
+    // and shapes: labels left = A\B (A order), right = B\A (B order),
+    // common = A∩B (A order); C carries left ++ right; a_perm / b_perm order
+    // A as (left ++ common) and B as (common ++ right).
+    struct ContractionLayout {
+        std::vector<std::string> c_indices;
+        std::vector<size_t> c_shape;
+        std::vector<uint64_t> a_shape, b_shape;
+        std::vector<int32_t> a_perm, b_perm;
+        uint64_t m = 1, n = 1, k = 1;
+    };
     template <class U = T>
-    static Tensor<U> ContractTensors(const Tensor<U> &A, const Tensor<U> &B)
+    static ContractionLayout LayoutOf(const Tensor<U> &A, const Tensor<U> &B)
     {
         using namespace Utilities;
+        ContractionLayout l;
         const auto left = VectorSubtraction(A.GetIndices(), B.GetIndices());
         const auto right = VectorSubtraction(B.GetIndices(), A.GetIndices());
         const auto common = VectorIntersection(A.GetIndices(), B.GetIndices());
         const auto &ad = A.GetIndexToDimension();
         const auto &bd = B.GetIndexToDimension();
-        uint64_t m = 1, n = 1, k = 1;
-        std::vector<size_t> c_shape;
         for (const auto &x : left) {
-            m *= ad.at(x);
-            c_shape.push_back(ad.at(x));
+            l.m *= ad.at(x);
+            l.c_shape.push_back(ad.at(x));
         }
         for (const auto &x : right) {
-            n *= bd.at(x);
-            c_shape.push_back(bd.at(x));
+            l.n *= bd.at(x);
+            l.c_shape.push_back(bd.at(x));
         }
         for (const auto &x : common)
-            k *= ad.at(x);
-        std::vector<int32_t> a_perm, b_perm;
+            l.k *= ad.at(x);
         for (const auto &x : VectorConcatenation(left, common))
-            a_perm.push_back(PositionOf(A.GetIndices(), x));
+            l.a_perm.push_back(PositionOf(A.GetIndices(), x));
         for (const auto &x : VectorConcatenation(common, right))
-            b_perm.push_back(PositionOf(B.GetIndices(), x));
-        Tensor<U> C(VectorConcatenation(left, right), c_shape);
+            l.b_perm.push_back(PositionOf(B.GetIndices(), x));
+        l.c_indices = VectorConcatenation(left, right);
+        l.a_shape.assign(A.GetShape().begin(), A.GetShape().end());
+        l.b_shape.assign(B.GetShape().begin(), B.GetShape().end());
+        return l;
+    }
+
+    // Precision a contraction of this element type runs in: the setting for
+    // complex64, FP64 for complex128.
+    template <class U = T> static int ContractPrecision()
+    {
+        return Gpu::DtypeCode<U>() == JETGPU_C128 ? JETGPU_PREC_FP32 : Gpu::GetPrecision();
+    }
+
+    // Tensor::ContractTensors (reference Tensor.hpp:708-752).
+    template <class U = T>
+    static Tensor<U> ContractTensors(const Tensor<U> &A, const Tensor<U> &B)
+    {
+        const ContractionLayout l = LayoutOf<U>(A, B);
+        Tensor<U> C(l.c_indices, l.c_shape);
         C.AllocateDevice();
-        std::vector<uint64_t> as(A.GetShape().begin(), A.GetShape().end());
-        std::vector<uint64_t> bs(B.GetShape().begin(), B.GetShape().end());
         const int dt = Gpu::DtypeCode<U>();
-        const int prec = dt == JETGPU_C128 ? JETGPU_PREC_FP32 : Gpu::GetPrecision();
-        const size_t ws = jetgpu_contract_workspace_size((int)as.size(), as.data(), a_perm.data(),
-                                                         (int)bs.size(), bs.data(), b_perm.data(),
-                                                         m, n, k, dt, prec);
+        const int prec = ContractPrecision<U>();
+        const size_t ws = jetgpu_contract_workspace_size(
+            (int)l.a_shape.size(), l.a_shape.data(), l.a_perm.data(), (int)l.b_shape.size(),
+            l.b_shape.data(), l.b_perm.data(), l.m, l.n, l.k, dt, prec);
         Gpu::DeviceBuffer work(ws);
-        Gpu::Check(jetgpu_contract(A.GetDeviceData(), (int)as.size(), as.data(), a_perm.data(),
-                                   B.GetDeviceData(), (int)bs.size(), bs.data(), b_perm.data(),
-                                   C.dev_.get(), m, n, k, dt, prec, JETGPU_ALGO_4M, 0, 0,
-                                   work.get(), work.size(), Gpu::Stream()),
+        Gpu::Check(jetgpu_contract(A.GetDeviceData(), (int)l.a_shape.size(), l.a_shape.data(),
+                                   l.a_perm.data(), B.GetDeviceData(), (int)l.b_shape.size(),
+                                   l.b_shape.data(), l.b_perm.data(), C.dev_.get(), l.m, l.n, l.k,
+                                   dt, prec, JETGPU_ALGO_4M, 0, 0, work.get(), work.size(),
+                                   Gpu::Stream()),
                    "ContractTensors");
         C.MarkDeviceWritten();
         return C;

@@ -210,3 +210,45 @@ def test_config0_amplitude(jet, precision):
         ref_case = [c for c in json.load(f)["network"] if c["rows"] == 4][0]
     ref_amp = complex(*ref_case["out"][0])
     assert abs(got - ref_amp) <= 1e-5 * abs(ref_amp)
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_repeated_contract_replays_a_graph(jet, precision):
+    """Repeated TaskBasedContractor.contract() calls of the same tasks: the
+    first runs eagerly, the second captures the contractions into one CUDA
+    graph and every later call replays it. Every call's results (two networks
+    sharing tasks, their FP64 reduction) equal those of a contractor that
+    runs eagerly, bit for bit."""
+    from jet_gb300 import circuits
+
+    net = circuits.random_circuit_network(3, 4, 6, seed=31)
+    path = circuits.greedy_path(net, seed=31)
+    sliced = circuits.choose_slices(net, path, 1)
+    old = jet.get_precision()
+    jet.set_precision(precision)
+    try:
+        def build(replay):
+            tbc = jet.TaskBasedContractor(dtype="complex64")
+            tbc.set_graph_replay(replay)
+            for v in range(2):
+                tn = jet.TensorNetwork(dtype="complex64")
+                for lab, sh, d in net.tensors:
+                    tn.add_tensor(jet.Tensor(indices=lab, shape=sh, data=list(d),
+                                             dtype="complex64"))
+                tn.slice_indices(sliced, v)
+                tbc.add_contraction_tasks(tn, jet.PathInfo(tn, path))
+            tbc.add_deletion_tasks()
+            tbc.add_reduction_task()
+            return tbc
+
+        eager = build(False)
+        eager.contract()
+        want = [complex(r.data[0]) for r in eager.results] + [eager.reduction_result.data[0]]
+        tbc = build(True)
+        for call in range(4):
+            tbc.contract()
+            got = [complex(r.data[0]) for r in tbc.results] + [tbc.reduction_result.data[0]]
+            assert got == want, call
+            assert tbc.has_replay_graph == (call >= 1)
+    finally:
+        jet.set_precision(old)
