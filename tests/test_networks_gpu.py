@@ -110,12 +110,12 @@ def test_m12_reference_slices(jet, amps, precision):
         vals.append(got)
     ref0 = _c(ent["slices"]["0"]["ref_c64"])
     assert _rel(vals[0], ref0) <= 1e-5, _rel(vals[0], ref0)
-    # The three slices in one batch, summed in FP64 on the device.
-    sc3 = jet.SlicedContractorC64(tnf.tensors, path, ent["sliced"], precision)
-    sc3.set_batch_size(3)
-    total = sc3.contract(0, 3)[0]
-    want = sum(_c(ent["slices"][str(v)]["oracle_c128"]) for v in (0, 1, 2))
-    scale = sum(abs(_c(ent["slices"][str(v)]["oracle_c128"])) for v in (0, 1, 2))
+    # Slices 0 and 1 in one batch, summed in FP64 on the device.
+    sc2 = jet.SlicedContractorC64(tnf.tensors, path, ent["sliced"], precision)
+    sc2.set_batch_size(2)
+    total = sc2.contract(0, 2)[0]
+    want = sum(_c(ent["slices"][str(v)]["oracle_c128"]) for v in (0, 1))
+    scale = sum(abs(_c(ent["slices"][str(v)]["oracle_c128"])) for v in (0, 1))
     assert abs(total - want) <= 1e-5 * scale
 
 
