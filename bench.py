@@ -249,66 +249,54 @@ def run_ours(args, rank, world, local_rank):
         base, _, algo = form.partition("_")
         three_m = algo == "3m"
         bf, hf = base == "bf16x3", base == "fp16x3"
+        # --tc-variant 1: the N = 256 main loop (six B planes with -im).
+        wide = (bf or hf) and not three_m and args.tc_variant == 1
         fmt = capi.FMT_BF16 if bf else capi.FMT_FP16 if hf else capi.FMT_TF32
         word = torch.int16 if (bf or hf) else torch.float32
         aplanes = 6 if three_m else 4
-        bplanes = 6 if three_m else 4 if (bf or hf) else capi.tc_b_planes()
+        bplanes = 6 if (three_m or wide) else 4 if (bf or hf) else capi.tc_b_planes()
+        extra_a = capi.SPLIT_SUM if three_m else 0
+        extra_b = capi.SPLIT_SUM if three_m else capi.SPLIT_NEG_IM if wide else 0
         pa = torch.empty(aplanes * m * kp, dtype=word, device=dev)
         pb = torch.empty(bplanes * n * kp, dtype=word, device=dev)
         e2 = torch.empty(2, dtype=torch.int32, device=dev)  # FP16: max exponents of A, B
 
-        def step3m(events=None):
+        def step16(events=None):
+            """16-bit forms: the general split and product stages."""
             if events:
                 events[0].record(stream)
             if hf:
                 capi.max_exponent(A, stream=stream, out=e2[0:1])
-            capi.split_planes(A, w["a_shape"], w["a_perm"], m, k, kp, pa, fmt,
-                              extra=capi.SPLIT_SUM, e_max=e2[0:1] if hf else None, stream=stream)
+            capi.split_planes(A, w["a_shape"], w["a_perm"], m, k, kp, pa, fmt, extra=extra_a,
+                              e_max=e2[0:1] if hf else None, stream=stream)
             if events:
                 events[1].record(stream)
             if hf:
                 capi.max_exponent(B, stream=stream, out=e2[1:2])
-            capi.split_planes(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, fmt,
-                              extra=capi.SPLIT_SUM, e_max=e2[1:2] if hf else None, stream=stream)
+            capi.split_planes(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, fmt, extra=extra_b,
+                              e_max=e2[1:2] if hf else None, stream=stream)
             if events:
                 events[2].record(stream)
-            capi.gemm_split(pa, pb, m, n, k, kp, C, fmt, algo=capi.ALGO_3M,
-                            e_max2=e2 if hf else None, stream=stream)
+            capi.gemm_split(pa, pb, m, n, k, kp, C, fmt,
+                            algo=capi.ALGO_3M if three_m else capi.ALGO_4M,
+                            e_max2=e2 if hf else None, stream=stream, variant=1 if wide else 0)
             if events:
                 events[3].record(stream)
 
         def step(events=None):
-            if three_m:
-                return step3m(events)
+            if bf or hf:
+                return step16(events)
+            # TF32: the TF32x3 stage entry points (B planes per jetgpu_tc_b_planes).
             if events:
                 events[0].record(stream)
-            if hf:
-                capi.max_exponent(A, stream=stream, out=e2[0:1])
-                capi.split_fp16(A, w["a_shape"], w["a_perm"], m, k, kp, pa, e2[0:1],
-                                stream=stream)
-            elif bf:
-                capi.split_bf16(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
-            else:
-                capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
+            capi.split_tf32(A, w["a_shape"], w["a_perm"], m, k, kp, pa, stream=stream)
             if events:
                 events[1].record(stream)
-            if hf:
-                capi.max_exponent(B, stream=stream, out=e2[1:2])
-                capi.split_fp16(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, e2[1:2],
-                                stream=stream)
-            elif bf:
-                capi.split_bf16(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, stream=stream)
-            else:
-                capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb,
-                                n_planes=bplanes, stream=stream)
+            capi.split_tf32(B, w["b_shape"], w["b_perm_nk"], n, k, kp, pb, n_planes=bplanes,
+                            stream=stream)
             if events:
                 events[2].record(stream)
-            if hf:
-                capi.gemm_fp16x3(pa, pb, m, n, k, kp, C, e2, stream=stream)
-            elif bf:
-                capi.gemm_bf16x3(pa, pb, m, n, k, kp, C, stream=stream)
-            else:
-                capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
+            capi.gemm_tf32x3(pa, pb, m, n, k, kp, C, stream=stream)
             if events:
                 events[3].record(stream)
 

@@ -345,11 +345,13 @@ size_t jetgpu_contract_noalloc_max_scratch(void);
  *
  * jetgpu_set_tc_variant selects the main-loop shape of the tensor-core
  * products for the calling process: 0 = default (M 128 x N 128 MMAs over 4 B
- * planes, 3 stages of 64-byte rows); 1 = TF32 with M 128 x N 256 MMAs over
- * 6 B planes (stacked [Br; Bi] and [-Bi; Br] operands, half the MMA count);
- * 2 = BF16 with 32-byte rows in 6 stages (twice the pipeline depth in the
- * same shared memory). jetgpu_tc_b_planes() reports the B planes the TF32
- * product reads.
+ * planes, 3 stages of 64-byte rows); 1 = M 128 x N 256 MMAs over 6 B planes
+ * (stacked [Br; Bi] and [-Bi; Br] operands, half the MMA count; TF32, BF16 and
+ * FP16 through jetgpu_contract*); 2 = BF16 with 32-byte rows in 6 stages
+ * (twice the pipeline depth in the same shared memory). jetgpu_tc_b_planes()
+ * reports the B planes the TF32 stage product (jetgpu_gemm_tf32x3) reads; the
+ * BF16 and FP16 stage products (jetgpu_gemm_bf16x3, jetgpu_gemm_fp16x3) always
+ * read four.
  */
 int jetgpu_split_tf32(const void *in, int rank, const uint64_t *shape,
                       const int32_t *perm, uint64_t rows, uint64_t cols,
@@ -467,24 +469,26 @@ int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void 
  * The two stages of any split form, with either complex product algorithm.
  *
  * jetgpu_split_planes: fmt 0 TF32 (float words, pitch % 4 == 0), 1 BF16,
- * 2 FP16 (uint16 words, pitch % 8 == 0); planes 0-3 as above; extra 2
- * (JETGPU_ALGO_3M's operands) also writes plane 4 = hi and plane 5 = lo of
- * re + im, and for FP16 scales by 2^(s - 1) instead of 2^s so the sums stay
- * below 2^15. extra 0 writes four planes. e_max_dev: FP16 only.
+ * 2 FP16 (uint16 words, pitch % 8 == 0); planes 0-3 as above; extra 1 also
+ * writes plane 4 = -im_hi and plane 5 = -im_lo (the B operand of the N = 256
+ * main loop); extra 2 (JETGPU_ALGO_3M's operands) writes plane 4 = hi and
+ * plane 5 = lo of re + im, and for FP16 scales by 2^(s - 1) instead of 2^s so
+ * the sums stay below 2^15. extra 0 writes four planes. e_max_dev: FP16 only.
  *
  * jetgpu_gemm_split: C = A * B^T from the planes of A (m x k) and B (n x k):
- * algo JETGPU_ALGO_4M reads four planes per operand, JETGPU_ALGO_3M six
- * (written with extra 2) and forms P1 = ArBr, P2 = AiBi,
- * P3 = (Ar + Ai)(Br + Bi), Cr = P1 - P2, Ci = P3 - P1 - P2. e_max_dev: two
- * device ints (A, B) for FP16. Replaces the cblas_cgemm call of
- * TensorHelpers.hpp:47-61.
+ * algo JETGPU_ALGO_4M reads four planes of A and, with variant 0, four of B
+ * (variant 1: the N = 256 main loop on six B planes written with extra 1);
+ * JETGPU_ALGO_3M reads six per operand (written with extra 2) and forms
+ * P1 = ArBr, P2 = AiBi, P3 = (Ar + Ai)(Br + Bi), Cr = P1 - P2,
+ * Ci = P3 - P1 - P2 (variant ignored). e_max_dev: two device ints (A, B) for
+ * FP16. Replaces the cblas_cgemm call of TensorHelpers.hpp:47-61.
  */
 int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
                         uint64_t rows, uint64_t cols, uint64_t pitch, uint64_t plane_stride,
                         int fmt, int extra, const int *e_max_dev, void *planes, void *stream);
 
 int jetgpu_gemm_split(const void *a_planes, const void *b_planes, void *C, uint64_t m,
-                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo,
+                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo, int variant,
                       const int *e_max_dev, float out_scale, void *stream);
 
 /*

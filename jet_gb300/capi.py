@@ -53,6 +53,7 @@ ALGO_3M = 1
 FMT_TF32 = 0
 FMT_BF16 = 1
 FMT_FP16 = 2
+SPLIT_NEG_IM = 1  # extra planes 4, 5: -im hi, lo (B of the N = 256 main loop)
 SPLIT_SUM = 2  # extra planes 4, 5: hi, lo of re + im (3M operands)
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -73,7 +74,7 @@ lib.jetgpu_split_planes.argtypes = [_vp, ctypes.c_int, _u64p, _i32p, ctypes.c_ui
                                     ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
 lib.jetgpu_gemm_split.argtypes = [_vp, _vp, _vp, ctypes.c_uint64, ctypes.c_uint64,
                                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
-                                  _vp, ctypes.c_float, _vp]
+                                  ctypes.c_int, _vp, ctypes.c_float, _vp]
 lib.jetgpu_permute.argtypes = [_vp, _vp, ctypes.c_int, _u64p, _i32p, ctypes.c_int, _vp]
 lib.jetgpu_permute_batched.argtypes = [_vp, _vp, ctypes.c_uint64, ctypes.c_int, _u64p, _i32p,
                                        ctypes.c_int, _vp]
@@ -434,11 +435,13 @@ def split_planes(x, shape, perm, rows, cols, pitch, planes, fmt, extra=0, e_max=
 
 
 def gemm_split(a_planes, b_planes, m, n, k, kpitch, out, fmt, algo=ALGO_4M, e_max2=None,
-               out_scale=1.0, stream=None):
+               out_scale=1.0, stream=None, variant=0):
     """Split-precision product of planes written by split_planes (ALGO_3M
-    reads six planes per operand)."""
+    reads six planes per operand; variant 1, the N = 256 main loop, six B
+    planes written with extra=SPLIT_NEG_IM)."""
     check(lib.jetgpu_gemm_split(_ptr(a_planes), _ptr(b_planes), _ptr(out), m, n, k, kpitch,
-                                int(fmt), int(algo), _ptr(e_max2), out_scale, _stream(stream)))
+                                int(fmt), int(algo), int(variant), _ptr(e_max2), out_scale,
+                                _stream(stream)))
     return out
 
 

@@ -126,10 +126,10 @@ __host__ __device__ inline float Pow2f(int e)
 }
 
 // Extra plane pair (planes 4 and 5) of a split: none; -im_hi, -im_lo (the
-// N = 256 TF32 main loop); hi, lo of re + im (the 3M product's sums).
+// N = 256 main loop's B operand); hi, lo of re + im (the 3M product's sums).
 constexpr int kSplitNone = 0, kSplitNegIm = 1, kSplitSum = 2;
 
-// PermuteSplitTf32Batched for any word format (kSplitNegIm with TF32 only).
+// PermuteSplitTf32Batched for any word format.
 // For FP16, `e_max_dev` points at the operand's max exponent on the device
 // and sets the scale (Fp16ScaleExp, one less with kSplitSum so the sums stay
 // in range); scale_exp is then ignored.

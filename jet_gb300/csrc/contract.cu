@@ -73,11 +73,17 @@ SplitLayout LayoutFor(int precision, uint64_t k, double work, int variant = -1,
     l.variant = variant >= 0 ? variant : TcVariant();
     l.algo = algo;
     l.a_planes = algo == JETGPU_ALGO_3M ? 6 : 4;
-    l.b_planes = (algo == JETGPU_ALGO_3M || (l.fmt == SplitFormat::kTf32 && l.variant == 1))
-                     ? 6
-                     : 4;
+    l.b_planes = (algo == JETGPU_ALGO_3M || l.variant == 1) ? 6 : 4;
     l.group_m = group_m;
     return l;
+}
+
+// The main-loop setting for the 16-bit stage entry points, whose B operand
+// has four planes: the N = 256 loop (variant 1) needs six, so it runs as 0.
+int FourPlaneVariant()
+{
+    const int v = TcVariant();
+    return v == 1 ? 0 : v;
 }
 
 bool IsIdentity(int rank, const int32_t *perm)
@@ -269,7 +275,8 @@ int jetgpu_gemm_fp16x3(const uint16_t *a_planes, const uint16_t *b_planes, void 
                        e_max_dev != nullptr,
                    "null pointer");
     return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
-                                  SplitFormat::kFp16, AsStream(stream), -1, e_max_dev);
+                                  SplitFormat::kFp16, AsStream(stream), FourPlaneVariant(),
+                                  e_max_dev);
 }
 
 int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const int32_t *perm,
@@ -278,7 +285,8 @@ int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const i
 {
     ClearError();
     JETGPU_REQUIRE(fmt >= 0 && fmt <= 2, "fmt must be 0 (TF32), 1 (BF16) or 2 (FP16)");
-    JETGPU_REQUIRE(extra == kSplitNone || extra == kSplitSum, "extra must be 0 or 2");
+    JETGPU_REQUIRE(extra == kSplitNone || extra == kSplitNegIm || extra == kSplitSum,
+                   "extra must be 0, 1 or 2");
     const SplitFormat f = static_cast<SplitFormat>(fmt);
     JETGPU_REQUIRE(pitch >= cols && pitch % SplitPitchAlign(f) == 0,
                    "pitch must be >= cols and span a multiple of 16 bytes");
@@ -292,15 +300,16 @@ int jetgpu_split_planes(const void *in, int rank, const uint64_t *shape, const i
 }
 
 int jetgpu_gemm_split(const void *a_planes, const void *b_planes, void *C, uint64_t m,
-                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo,
+                      uint64_t n, uint64_t k, uint64_t kpitch, int fmt, int algo, int variant,
                       const int *e_max_dev, float out_scale, void *stream)
 {
     ClearError();
     JETGPU_REQUIRE(fmt >= 0 && fmt <= 2, "fmt must be 0 (TF32), 1 (BF16) or 2 (FP16)");
+    JETGPU_REQUIRE(variant == 0 || variant == 1, "variant must be 0 or 1");
     JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
     return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
-                                  static_cast<SplitFormat>(fmt), AsStream(stream), 0, e_max_dev,
-                                  0, nullptr, nullptr, algo);
+                                  static_cast<SplitFormat>(fmt), AsStream(stream), variant,
+                                  e_max_dev, 0, nullptr, nullptr, algo);
 }
 
 int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void *C, uint64_t m,
@@ -309,7 +318,7 @@ int jetgpu_gemm_bf16x3(const uint16_t *a_planes, const uint16_t *b_planes, void 
     ClearError();
     JETGPU_REQUIRE(C != nullptr && a_planes != nullptr && b_planes != nullptr, "null pointer");
     return GemmSplitPlanarBatched(a_planes, 0, b_planes, 0, C, 1, m, n, k, kpitch, out_scale,
-                                  SplitFormat::kBf16, AsStream(stream));
+                                  SplitFormat::kBf16, AsStream(stream), FourPlaneVariant());
 }
 
 } // extern "C"
@@ -370,10 +379,9 @@ size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const 
                              batch * m, n, k, dtype, precision, algo);
     }
     if (p.tc) {
-        // Sized for six TF32 B planes whatever the main-loop variant.
+        // Sized for six B planes whatever the main-loop variant.
         const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k, -1, 0, algo);
-        const int bpl = (l.fmt == SplitFormat::kTf32 || algo == JETGPU_ALGO_3M) ? 6 : 4;
-        return l.a_bytes(p.ba * m) + AlignUp(bpl * p.bb * n * l.kp * l.word) + l.exp_bytes();
+        return l.a_bytes(p.ba * m) + AlignUp(6 * p.bb * n * l.kp * l.word) + l.exp_bytes();
     }
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;

@@ -68,6 +68,9 @@ constexpr int kTileRing = 4;                  // tile indices in flight between 
 //                 half-size stages.
 // A chunk is the K extent accumulated in TMEM before the FP32 fold, in
 // stages (a kernel argument; see the kernel comment).
+//  8, 9 BF16 / FP16 wide: variant 1's N = 256 main loop on 16-bit planes
+//                 (two stages of 4 A + 6 B boxes of 32 k; the B triples of
+//                 variant 1 with the negated imaginary planes).
 //  5, 6, 7 3M:    TF32 / BF16 / FP16 planes, 64-byte rows, 2 stages of six A
 //                 plane boxes (re, im, re + im; hi, lo) and six B boxes;
 //                 9 MMAs of N = 128 per k step, each product into its own
@@ -94,6 +97,14 @@ template <> struct TcCfg<3> {
 template <> struct TcCfg<4> {
     static constexpr bool Wide = false, ThreeM = false;
     static constexpr int Fmt = kFmtFp16, Stages = 3, Tiles = 8, RowBytes = 64;
+};
+template <> struct TcCfg<8> {
+    static constexpr bool Wide = true, ThreeM = false;
+    static constexpr int Fmt = kFmtBf16, Stages = 2, Tiles = 10, RowBytes = 64;
+};
+template <> struct TcCfg<9> {
+    static constexpr bool Wide = true, ThreeM = false;
+    static constexpr int Fmt = kFmtFp16, Stages = 2, Tiles = 10, RowBytes = 64;
 };
 template <> struct TcCfg<5> {
     static constexpr bool Wide = false, ThreeM = true;
@@ -995,8 +1006,8 @@ int LaunchTc(const CUtensorMap &ta, const CUtensorMap &tb, void *C, uint64_t bat
     return CheckLaunch("tc_gemm_split_kernel");
 }
 
-// Main-loop variant (jetgpu_set_tc_variant): 0 default, 1 TF32 N = 256,
-// 2 BF16 with 32-byte rows and 6 stages.
+// Main-loop variant (jetgpu_set_tc_variant): 0 default, 1 N = 256 (any
+// format; six B planes), 2 BF16 with 32-byte rows and 6 stages.
 std::atomic<int> g_tc_variant{0};
 
 } // namespace
@@ -1049,7 +1060,7 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return rc;
     if (variant < 0)
         variant = TcVariant();
-    const bool wide = !half && variant == 1 && !three_m;
+    const bool wide = variant == 1 && !three_m;
     const bool deep = bf16 && variant == 2 && !three_m;
     const int row_bytes = deep ? TcCfg<3>::RowBytes : TcCfg<0>::RowBytes;
     const int aplanes = three_m ? 6 : 4;
@@ -1074,6 +1085,12 @@ int GemmSplitPlanarBatched(const void *a_planes, int a_batched, const void *b_pl
         return LaunchTc<5>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
                            nullptr, group_m, out_emax, tile_counter);
     }
+    if (wide && fp16)
+        return LaunchTc<9>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           e_max_dev, group_m, out_emax, tile_counter);
+    if (wide && bf16)
+        return LaunchTc<8>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
+                           nullptr, group_m, out_emax, tile_counter);
     if (fp16)
         return LaunchTc<4>(ta, tb, C, batch, m, n, k, out_scale, a_batched, b_batched, stream,
                            e_max_dev, group_m, out_emax, tile_counter);
@@ -1116,7 +1133,7 @@ extern "C" int jetgpu_set_tc_variant(int variant)
 {
     jetgpu::ClearError();
     JETGPU_REQUIRE(variant >= 0 && variant <= 2,
-                   "variant must be 0 (default), 1 (TF32 N = 256) or 2 (BF16 6-stage)");
+                   "variant must be 0 (default), 1 (N = 256) or 2 (BF16 6-stage)");
     jetgpu::g_tc_variant.store(variant, std::memory_order_relaxed);
     return JETGPU_OK;
 }

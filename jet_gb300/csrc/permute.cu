@@ -224,7 +224,7 @@ struct SplitOut {
     uint64_t cols;         // logical columns of the permuted view
     uint64_t pitch;        // words per row in a plane
     float scale;           // exact power of two
-    int extra;             // planes 4, 5: kSplitNegIm -im_hi, -im_lo (TF32);
+    int extra;             // planes 4, 5: kSplitNegIm -im_hi, -im_lo;
                            // kSplitSum hi, lo of re + im (the 3M product's sums)
     int bf16;              // 16-bit BF16 words instead of TF32-in-FP32 words
     int fp16;              // 16-bit FP16 words of the operand scaled by its FP16 scale
@@ -266,6 +266,10 @@ __device__ __forceinline__ void WriteSplit(const SplitOut &so, uint64_t o,
         pl[off + so.plane_stride] = (uint16_t)(l & 0xffffu);
         pl[off + 2 * so.plane_stride] = (uint16_t)(h >> 16);
         pl[off + 3 * so.plane_stride] = (uint16_t)(l >> 16);
+        if (so.extra == kSplitNegIm) { // -x: the sign bit of each piece flipped
+            pl[off + 4 * so.plane_stride] = (uint16_t)((h >> 16) ^ 0x8000u);
+            pl[off + 5 * so.plane_stride] = (uint16_t)((l >> 16) ^ 0x8000u);
+        }
         if (so.extra == kSplitSum) {
             Split16x2(so, re + im, 0.f, h, l);
             pl[off + 4 * so.plane_stride] = (uint16_t)(h & 0xffffu);
@@ -701,6 +705,10 @@ struct SplitStore {
             *reinterpret_cast<uint32_t *>(pl + base + so.plane_stride) = rl;
             *reinterpret_cast<uint32_t *>(pl + base + 2 * so.plane_stride) = ih;
             *reinterpret_cast<uint32_t *>(pl + base + 3 * so.plane_stride) = il;
+            if (so.extra == kSplitNegIm) { // -x: the sign bit of each piece flipped
+                *reinterpret_cast<uint32_t *>(pl + base + 4 * so.plane_stride) = ih ^ 0x80008000u;
+                *reinterpret_cast<uint32_t *>(pl + base + 5 * so.plane_stride) = il ^ 0x80008000u;
+            }
             if (so.extra == kSplitSum) {
                 uint32_t sh, sl;
                 Split16x2(so, ar + ai, br + bi, sh, sl);
@@ -1000,8 +1008,6 @@ int PermuteSplitPlanes(const void *in, void *planes, uint64_t batch, int rank,
 {
     JETGPU_REQUIRE(extra == kSplitNone || extra == kSplitNegIm || extra == kSplitSum,
                    "unknown extra plane pair");
-    JETGPU_REQUIRE(!(extra == kSplitNegIm && fmt != SplitFormat::kTf32),
-                   "negated planes are TF32 only");
     JETGPU_REQUIRE(fmt != SplitFormat::kFp16 || e_max_dev != nullptr,
                    "FP16 planes need the operand's max exponent");
     Simplified s;

@@ -60,10 +60,11 @@ def _product_model(a, b):
         p(arh, arl, bih, bil) + p(aih, ail, brh, brl))
 
 
-@pytest.fixture(params=[0, 2], ids=["rows64", "rows32x6"])
+@pytest.fixture(params=[0, 1, 2], ids=["rows64", "n256", "rows32x6"])
 def bf16_variant(request, cuda):
-    """Runs a test under both BF16 main loops: 3 stages of 64-byte rows, and
-    6 stages of 32-byte rows."""
+    """Runs a test under the BF16 main loops: 3 stages of 64-byte rows, N = 256
+    MMAs over six B planes (contractions only; the stage entry points read
+    four B planes and keep the default loop), and 6 stages of 32-byte rows."""
     from jet_gb300 import capi
 
     capi.set_tc_variant(request.param)
@@ -164,7 +165,12 @@ def test_bf16x3_stages_equal_contract(cuda, bf16_variant):
     capi.split_bf16(db, [k, n], [1, 0], n, k, kp, pb)
     c = torch.empty(m * n, dtype=torch.complex64, device=cuda)
     capi.gemm_bf16x3(pa, pb, m, n, k, kp, c)
-    assert np.array_equal(c.cpu().numpy(), ref)
+    if bf16_variant == 1:
+        # N = 256 MMAs in the contraction, N = 128 in the stages: the same
+        # three-product sums in another instruction shape.
+        assert _rel(c.cpu().numpy(), ref) <= 1e-6
+    else:
+        assert np.array_equal(c.cpu().numpy(), ref)
 
 
 def test_bf16x3_reference_contractions(cuda, golden):

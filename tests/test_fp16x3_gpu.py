@@ -139,6 +139,31 @@ def test_fp16x3_random_gemm(cuda, m, n, k):
     assert capi.take_device_status() == 0
 
 
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (200, 136, 100), (1024, 512, 256),
+                                   (130, 300, 33), (384, 256, 4096)])
+def test_fp16x3_n256_main_loop(cuda, m, n, k):
+    """The N = 256 main loop (jetgpu_set_tc_variant(1): stacked [Br; Bi] and
+    [-Bi; Br] B operands on six FP16 planes) against complex128 and the exact
+    three-product model."""
+    from jet_gb300 import capi
+
+    rng = np.random.default_rng(m * 3 + n * 7 + k)
+    a = _data(rng, m, k)
+    b = _data(rng, k, n)
+    want = a.astype(np.complex128) @ b.astype(np.complex128)
+    model = _product_model(a, b)
+    capi.set_tc_variant(1)
+    try:
+        got = capi.contract(_dev(a.reshape(-1), cuda), [m, k], [0, 1],
+                            _dev(b.reshape(-1), cuda), [k, n], [0, 1], m, n, k,
+                            precision=capi.PREC_FP16X3).cpu().numpy().reshape(m, n)
+    finally:
+        capi.set_tc_variant(0)
+    assert _rel(got, want) <= 1e-5, _rel(got, want)
+    assert np.linalg.norm(got - model) <= 2e-6 * np.linalg.norm(want)
+    assert capi.take_device_status() == 0
+
+
 @pytest.mark.parametrize("sa,sb", [(2.0**-60, 2.0**40), (2.0**30, 2.0**-50), (2.0**-100, 1.0)])
 def test_fp16x3_operands_outside_fp16_range(cuda, sa, sb):
     from jet_gb300 import capi
