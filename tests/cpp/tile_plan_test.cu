@@ -10,6 +10,7 @@
 // equal plain division.
 #include "../../jet_gb300/csrc/permute.cu"
 
+#include <algorithm>
 #include <cstdio>
 #include <random>
 
@@ -207,6 +208,31 @@ int main()
             FAIL("fixed case %zu: expected no tile on the merged axes\n", c);
         if (Check(f.shape, f.perm, f.batch, f.eb) != 1)
             FAIL("fixed case %zu: no plan or failed\n", c);
+    }
+    // A plan on the original axes of a rank-58 tensor with a batch of 2 (the
+    // second try of PlanTile): the batch and every axis outside the tile
+    // enumerate the tiles, and must fit the plan's kMaxRank + 1 entries. Too
+    // large to replay; the plan's tiles must cover the tensor exactly.
+    {
+        std::vector<uint64_t> shape = {3, 3};
+        shape.insert(shape.end(), 56, 2);
+        const int rank = (int)shape.size();
+        std::vector<int32_t> perm(rank);
+        for (int i = 0; i < rank; ++i)
+            perm[i] = i;
+        std::reverse(perm.end() - 6, perm.end());
+        Simplified u;
+        Unmerged(rank, shape.data(), perm.data(), u);
+        static TileParams tp;
+        if ((int)u.dims.size() != rank || !BuildTile(u, 2, 8, tp))
+            FAIL("rank-%d plan on the original axes: none\n", rank);
+        if (tp.nr < 1 || tp.nr > kMaxRank + 1)
+            FAIL("rank-%d plan: %d enumerating axes\n", rank, tp.nr);
+        uint64_t covered = (uint64_t)tp.T;
+        for (int a = 0; a < tp.nr; ++a)
+            covered *= tp.r_dims[a];
+        if (covered != (9ull << 56) * 2 || covered / tp.T != tp.tiles)
+            FAIL("rank-%d plan covers %llu elements\n", rank, (unsigned long long)covered);
     }
     std::printf("ok %d of %d cases tiled, %d of %d large cases, %zu merged-axes cases\n", planned,
                 cases, big_planned, big_cases, fixed.size());
