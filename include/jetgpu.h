@@ -406,9 +406,10 @@ int jetgpu_set_auto_form(int precision);
  * variant and tile order (group_m, 0 = the jetgpu_set_tc_group_m setting),
  * and the measured ms per contraction of the JETGPU_AUTOTUNE_CANDIDATES
  * candidates: FP32, TF32X3 (variant 0), TF32X3 (variant 1), FP16X3, FP16X3
- * in row-major tile order (group_m 1); -1: not timed.
+ * in row-major tile order (group_m 1), FP16X3 with the N = 256 main loop
+ * (variant 1); -1: not timed.
  */
-#define JETGPU_AUTOTUNE_CANDIDATES 5
+#define JETGPU_AUTOTUNE_CANDIDATES 6
 int jetgpu_set_autotune_min_work(uint64_t mnk);
 size_t jetgpu_autotune_count(void);
 int jetgpu_autotune_entry(size_t index, uint64_t *batch_m_n_k, int *precision, int *variant,

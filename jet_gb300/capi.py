@@ -510,7 +510,8 @@ def max_exponent(x, stream=None, out=None):
     return e if out is not None else int(e.item())
 
 
-AUTOTUNE_CANDIDATES = ("fp32", "tf32x3", "tf32x3_wide", "fp16x3", "fp16x3_rowmajor")
+AUTOTUNE_CANDIDATES = ("fp32", "tf32x3", "tf32x3_wide", "fp16x3", "fp16x3_rowmajor",
+                       "fp16x3_wide")
 
 
 def set_autotune_min_work(mnk: int) -> None:
@@ -536,7 +537,8 @@ def autotune_table():
         if prec.value == PREC_FP32:
             choice = "fp32"
         elif prec.value == PREC_FP16X3:
-            choice = "fp16x3_rowmajor" if grp.value == 1 else "fp16x3"
+            choice = ("fp16x3_rowmajor" if grp.value == 1 else
+                      "fp16x3_wide" if var.value == 1 else "fp16x3")
         else:
             choice = "tf32x3_wide" if var.value == 1 else "tf32x3"
         out.append({"batch": bmnk[0], "m": bmnk[1], "n": bmnk[2], "k": bmnk[3],

@@ -42,9 +42,10 @@ constexpr Candidate kCandidate[kCandidates] = {{JETGPU_PREC_FP32, -1, 0},
                                                {JETGPU_PREC_TF32X3, 0, 0},
                                                {JETGPU_PREC_TF32X3, 1, 0},
                                                {JETGPU_PREC_FP16X3, 0, 0},
-                                               {JETGPU_PREC_FP16X3, 0, 1}};
+                                               {JETGPU_PREC_FP16X3, 0, 1},
+                                               {JETGPU_PREC_FP16X3, 1, 0}};
 // Trial order: fastest expected first, so the slow forms are cut short.
-constexpr int kTrialOrder[kCandidates] = {3, 4, 1, 2, 0};
+constexpr int kTrialOrder[kCandidates] = {3, 5, 4, 1, 2, 0};
 
 struct Entry {
     uint64_t batch, m, n, k;

@@ -205,12 +205,35 @@ __global__ void __launch_bounds__(256)
     const int64_t k_begin = s * kchunk;
     const int64_t k_end = min(K, k_begin + kchunk);
     KahanSum<T> sr, si;
-    if (m < M)
-        for (int64_t k = k_begin + part * 32 + lane; k < k_end; k += wpr * 32) {
+    if (m < M) {
+        // Four products per compensated add: four loads in flight per thread
+        // and a quarter of the compensation work (the sum of four products
+        // carries one rounding of the plain FMA chain).
+        const int64_t step = wpr * 32;
+        int64_t k = k_begin + part * 32 + lane;
+        for (; k + 3 * step < k_end; k += 4 * step) {
+            V a[4], xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = A[m * K + k + u * step];
+                xv[u] = x[k + u * step];
+            }
+            T re = a[0].x * xv[0].x - a[0].y * xv[0].y;
+            T im = a[0].x * xv[0].y + a[0].y * xv[0].x;
+#pragma unroll
+            for (int u = 1; u < 4; ++u) {
+                re = fma(a[u].x, xv[u].x, fma(-a[u].y, xv[u].y, re));
+                im = fma(a[u].x, xv[u].y, fma(a[u].y, xv[u].x, im));
+            }
+            sr.add(re);
+            si.add(im);
+        }
+        for (; k < k_end; k += step) {
             V a = A[m * K + k], b = x[k];
             sr.add(fma(a.x, b.x, -a.y * b.y));
             si.add(fma(a.x, b.y, a.y * b.x));
         }
+    }
     T re = sr.s, im = si.s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -259,12 +282,32 @@ __global__ void __launch_bounds__(256)
     B += b * sb;
     out += (s * gridDim.z + b) * N;
     KahanSum<T> sr, si;
-    if (n < N)
-        for (int64_t k = k_begin + tk; k < k_end; k += tk_count) {
+    if (n < N) {
+        // Four products per compensated add (see gemv_rows_kernel).
+        int64_t k = k_begin + tk;
+        for (; k + 3 * (int64_t)tk_count < k_end; k += 4 * (int64_t)tk_count) {
+            V a[4], v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = x[k + u * tk_count];
+                v[u] = B[(k + u * tk_count) * N + n];
+            }
+            T re = a[0].x * v[0].x - a[0].y * v[0].y;
+            T im = a[0].x * v[0].y + a[0].y * v[0].x;
+#pragma unroll
+            for (int u = 1; u < 4; ++u) {
+                re = fma(a[u].x, v[u].x, fma(-a[u].y, v[u].y, re));
+                im = fma(a[u].x, v[u].y, fma(a[u].y, v[u].x, im));
+            }
+            sr.add(re);
+            si.add(im);
+        }
+        for (; k < k_end; k += tk_count) {
             V a = x[k], v = B[k * N + n];
             sr.add(fma(a.x, v.x, -a.y * v.y));
             si.add(fma(a.x, v.y, a.y * v.x));
         }
+    }
     if (tk_count == 1) {
         if (n < N)
             out[n] = V{sr.s * scale, si.s * scale};

@@ -341,9 +341,8 @@ struct TileParams {
 // permute is bound by its launch, and the tile plan's 12 KB parameter block and
 // host-side tables would only add to that.
 constexpr uint64_t kTileMinElements = 1ull << 18;
-constexpr int kTileGroupMax = kThreads / 2; // tiles per pass (a base per thread)
-constexpr int kTileSlotBytes = 16384;    // shared memory for one pass's elements
-constexpr int kTileBuffers = 2;          // passes in flight per CTA (double buffering)
+constexpr int kTileGroupMax = kThreads; // tiles per pass (one base per thread)
+constexpr int kTileSlotBytes = 32768;    // shared memory for one pass's elements
 
 // Tile bases: tile t decoded over the enumerating axes (last fastest).
 __device__ __forceinline__ void TileBases(const TileParams &p, uint64_t t, uint64_t &bi,
@@ -396,18 +395,14 @@ template <typename E> __device__ __forceinline__ void CopyAsync(E *dst, const E 
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 
-// Each pass moves G consecutive tiles (G * T elements, up to 16 KB) through
-// shared memory: slot u holds element u mod T of the pass's tile u / T. The
-// passes of a CTA are software-pipelined over two buffers: the cp.async loads
-// of the next pass are in flight while the current pass is stored.
+// Each pass moves G consecutive tiles (G * T elements, up to 32 KB) through
+// shared memory: slot u holds element u mod T of the pass's tile u / T.
 template <typename E, typename Store>
 __global__ void __launch_bounds__(kThreads)
     tile_permute_kernel(const __grid_constant__ TileParams p, const E *__restrict__ in, Store store)
 {
-    constexpr int kSlots = kTileSlotBytes / sizeof(E);
-    __shared__ E tile[kTileBuffers][kSlots];
-    __shared__ uint64_t base_in[kTileBuffers][kTileGroupMax];
-    __shared__ uint64_t base_out[kTileBuffers][kTileGroupMax];
+    __shared__ E tile[kTileSlotBytes / sizeof(E)];
+    __shared__ uint64_t base_in[kTileGroupMax], base_out[kTileGroupMax];
     // The offset tables move to shared memory once, in 16-byte words: indexed
     // per thread, a kernel-parameter array serialises every warp's load, so
     // the tile loops read them from shared memory instead.
@@ -427,45 +422,28 @@ __global__ void __launch_bounds__(kThreads)
             reinterpret_cast<int4 *>(pos)[i] = src_pos[i];
     }
     const uint64_t passes = (p.tiles + p.G - 1) / p.G;
-    // Tile bases of pass ps into buffer b, then its loads (one commit group).
-    auto issue = [&](uint64_t ps, int b) {
+    for (uint64_t ps = blockIdx.x; ps < passes; ps += gridDim.x) {
         const uint64_t t0 = ps * p.G;
         const int g = (int)min((uint64_t)p.G, p.tiles - t0);
         if ((int)threadIdx.x < g)
-            TileBases(p, t0 + threadIdx.x, base_in[b][threadIdx.x], base_out[b][threadIdx.x]);
+            TileBases(p, t0 + threadIdx.x, base_in[threadIdx.x], base_out[threadIdx.x]);
         __syncthreads();
         const int n = g * p.T;
 #pragma unroll 4
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
             const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
             const int e = u - j * p.T;
-            CopyAsync(&tile[b][j * p.T + pos[e]], in + base_in[b][j] + (uint64_t)in_off[e]);
+            CopyAsync(&tile[j * p.T + pos[e]], in + base_in[j] + (uint64_t)in_off[e]);
         }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-    __syncthreads(); // the tables are in shared memory
-    if ((uint64_t)blockIdx.x < passes)
-        issue(blockIdx.x, 0);
-    int b = 0;
-    for (uint64_t ps = blockIdx.x; ps < passes; ps += gridDim.x, b ^= 1) {
-        const uint64_t next = ps + gridDim.x;
-        if (next < passes) {
-            issue(next, b ^ 1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory"); // this pass's loads
-        }
-        else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
         __syncthreads();
-        const int g = (int)min((uint64_t)p.G, p.tiles - ps * p.G);
-        const int n = g * p.T;
 #pragma unroll 4
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
             const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
             const int f = u - j * p.T;
-            store(base_out[b][j] + (uint64_t)out_off[f], tile[b][u]);
+            store(base_out[j] + (uint64_t)out_off[f], tile[u]);
         }
-        __syncthreads(); // buffer b is free for the pass after next
+        __syncthreads();
     }
 }
 
@@ -548,13 +526,22 @@ bool BuildTile(const Simplified &s, uint64_t batch, size_t elem_bytes, TileParam
             p.r_out[nr] = s.size;
             ++nr;
         }
+#ifndef JETGPU_TILE_OUTPUT_ORDER
+#define JETGPU_TILE_OUTPUT_ORDER 0
+#endif
+        std::vector<int> rest;
         for (int a = 0; a < r; ++a)
-            if (!in_u[a]) {
-                p.r_dims[nr] = s.dims[a];
-                p.r_in[nr] = in_stride[a];
-                p.r_out[nr] = out_stride[a];
-                ++nr;
-            }
+            if (!in_u[a])
+                rest.push_back(a);
+        if (JETGPU_TILE_OUTPUT_ORDER)
+            std::stable_sort(rest.begin(), rest.end(),
+                             [&](int x, int y) { return out_stride[x] > out_stride[y]; });
+        for (int a : rest) {
+            p.r_dims[nr] = s.dims[a];
+            p.r_in[nr] = in_stride[a];
+            p.r_out[nr] = out_stride[a];
+            ++nr;
+        }
         p.nr = nr;
         p.tiles = (s.size / T) * batch;
         p.narrow = p.tiles < (1ull << 32) ? 1 : 0;
