@@ -599,7 +599,7 @@ def time_sliced_form(jet, tn, path, sliced, prec, batch, chunks, start=None, aft
     return out, info
 
 
-def sliced_golden(name):
+def config_golden(name):
     """The record of a sliced circuit in the golden fixtures (made on the CPU
     by tests/golden/make_network_fixtures.py): circuit, path, sliced bonds
     and, where the oracle could run one, complex128 amplitudes of slices."""
@@ -616,7 +616,7 @@ def run_sliced_leg(name, batch, chunks, fp32_chunks=1):
     import jet_gb300 as jet
     from jet_gb300 import capi, circuits
 
-    ent = sliced_golden(name)
+    ent = config_golden(name)
     net = circuits.random_circuit_network(ent["rows"], ent["cols"], ent["cycles"],
                                           seed=ent["seed"], removed=tuple(ent["removed"]))
     path = [tuple(p) for p in ent["path"]]
@@ -959,6 +959,78 @@ def run_sliced(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_m12(args, rank, world, local_rank):
+    """The reference's own m12 benchmark network (53 qubits, depth 12;
+    examples/paper_benchmarks/data_files/m12.json, kept as a golden fixture)
+    with the reference's 9-index slicing (GPU/jet_gpu_m12/jet_sliced_subset.cpp:
+    53-54, 512 slices), loaded through the TensorNetworkSerializer
+    counterpart and contracted by the sliced contractor in AUTO and plain
+    FP32: slices/s, eff. TFLOP/s, the amplitude error of slices 0-2 against
+    the fixture's complex128 oracle values, and the CPU oracle (numpy
+    complex64, the reference's per-step arithmetic) timed on one slice."""
+    import torch
+
+    import jet_gb300 as jet
+    from jet_gb300 import capi
+
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    import make_network_fixtures as mk
+
+    torch.cuda.set_device(local_rank)
+    ent = config_golden("m12")
+    tensors, path = mk.load_network_npz(os.path.join(REPO, "tests", "golden", "m12_network.npz"))
+    tnf = jet.TensorNetworkSerializer(dtype="complex64")(mk.network_json_text(tensors, path))
+    sliced = ent["sliced"]
+    batch = args.sliced_batch or 8
+    chunks = args.sliced_chunks or 4
+    capi.set_auto_form(capi.PREC_FP16X3)
+    forms, errs = {}, {}
+    for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+        forms[name], info = time_sliced_form(jet, tnf.tensors, path, sliced, prec, batch, chunks)
+        one = jet.SlicedContractorC64(tnf.tensors, path, sliced, prec)
+        one.set_batch_size(1)
+        errs[name] = {}
+        for v, rec in ent["slices"].items():
+            got = one.contract(int(v), 1)[0]
+            want = complex(*rec["oracle_c128"])
+            errs[name]["slice_" + v] = abs(got - want) / abs(want)
+        del one
+        forms[name]["rel_err_vs_fp64"] = max(errs[name].values())
+        forms[name]["rel_err_per_slice"] = errs[name]
+    line = {"metric": METRIC, "value": forms["auto"]["slices_per_s"], "unit": "slices/s",
+            "n_gpus": world, "steps": 1, "warmup": 1,
+            "ms_per_step": forms["auto"]["s_per_slice"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "the reference's m12 network (golden fixture of its data file)",
+            "config": {"workload": "m12: %d tensors, stored path of %d steps, %d sliced indices "
+                                   "(%d slices), %d slices per batch"
+                                   % (len(tensors), len(path), len(sliced), info["num_slices"],
+                                      batch)},
+            "forms": forms,
+            "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
+            "slice_pathinfo_flops": info["slice_flops"],
+            "extrapolated_all_slices_s": {f: info["num_slices"] / forms[f]["slices_per_s"]
+                                          for f in forms},
+            "error_reference": "complex128 oracle amplitudes of slices 0, 1, 2 (golden)"}
+    if not args.no_cpu_baseline:
+        from oracle import jet_oracle as jo
+
+        tn = jo.OTensorNetwork()
+        for _, lab, sh, d in tensors:
+            tn.add_tensor(jo.OTensor.make(lab, sh, np.asarray(d, np.complex64), np.complex64))
+        tn.slice_indices(list(sliced), 0)
+        t0 = time.perf_counter()
+        tn.contract(path, release=True)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "slices/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "slice 0 of m12 in complex64 through the numpy oracle "
+                                          "(TensorNetwork::Contract restated, BLAS threads = "
+                                          "host cores), %.1f s" % dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_grad(args, rank, world, local_rank):
     """Config 3: d Re<psi|Z_i Z_j|psi> / d(720 angles) of a 6x6, 10-layer
     RX-RZ-CZ circuit through the hand-written adjoint (light-cone-pruned
@@ -1152,7 +1224,8 @@ def main():
                          "(SlicedContractor.profile_chunk) to this JSON file")
     ap.add_argument("--check-fp64", action="store_true",
                     help="sliced configs: also contract slice 0 in complex128")
-    ap.add_argument("--form", default="auto", choices=["auto", "tf32x3", "bf16x3", "fp16x3"],
+    ap.add_argument("--form", default="auto",
+                    choices=["auto", "tf32x3", "bf16x3", "fp16x3", "bf16x3_3m", "fp16x3_3m"],
                     help="split form of the config-1 step (auto: all timed, the headline is "
                          "the fastest whose error on the step is within 1e-5)")
     ap.add_argument("--sliced-forms", default="auto,tuned,auto_tf32,fp32",
@@ -1176,7 +1249,8 @@ def main():
                     help="tensor-core main loop: 0 = N 128 MMAs, 1 = N 256 MMAs")
     ap.add_argument("--config", default="1",
                     help="1 (default): the pairwise contraction; 0, 2, 4, 4q (qutrits): sliced "
-                         "circuit amplitudes through the sliced executor; 3: gradients")
+                         "circuit amplitudes through the sliced executor; 3: gradients; m12: the "
+                         "reference's m12 network with its own slicing")
     ap.add_argument("--permute-shape", default=None,
                     help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
                          "permutation)")
@@ -1197,6 +1271,9 @@ def main():
         return
     if args.config == "3":
         run_grad(args, rank, world, local_rank)
+        return
+    if args.config == "m12":
+        run_m12(args, rank, world, local_rank)
         return
     if args.config != "1":
         run_sliced(args, rank, world, local_rank)
