@@ -532,25 +532,12 @@ bool BuildTile(const Simplified &s, uint64_t batch, size_t elem_bytes, TileParam
         // while they are still in L2. In input order the runs of a sector
         // were written far apart in time; measured on random permutations,
         // 3^18 complex64 went from 3.1 to 4.8 TB/s.
-#ifndef JETGPU_TILE_ORDER
-#define JETGPU_TILE_ORDER 1
-#endif
         std::vector<int> rest;
         for (int a = 0; a < r; ++a)
             if (!in_u[a])
                 rest.push_back(a);
-        if (JETGPU_TILE_ORDER >= 1)
-            std::stable_sort(rest.begin(), rest.end(),
-                             [&](int x, int y) { return out_stride[x] > out_stride[y]; });
-        if (JETGPU_TILE_ORDER == 2 && !rest.empty()) {
-            // The axis of smallest input stride fastest, the rest in output order.
-            auto it = std::min_element(rest.begin(), rest.end(), [&](int x, int y) {
-                return in_stride[x] < in_stride[y];
-            });
-            const int a = *it;
-            rest.erase(it);
-            rest.push_back(a);
-        }
+        std::stable_sort(rest.begin(), rest.end(),
+                         [&](int x, int y) { return out_stride[x] > out_stride[y]; });
         for (int a : rest) {
             p.r_dims[nr] = s.dims[a];
             p.r_in[nr] = in_stride[a];
