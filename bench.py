@@ -1202,6 +1202,94 @@ def run_permute(args):
         "exact": exact, "clocks": clocks}))
 
 
+def run_gate(args):
+    """One gate applied to a state-like tensor through jetgpu_contract (the
+    skinny kernel): --gate-shape 'D^R:Q' is a tensor of R axes of dimension D
+    and a gate reading Q of them (seeded positions) and writing Q new ones,
+    contracted as Tensor::ContractTensors orders it (state's free axes, then
+    the gate's outputs). Timed with CUDA events over --steps launches after
+    --warmup; the transposing path (jetgpu_permute of the state, then
+    jetgpu_multiply) is timed beside it and must give the same bits.
+    Algorithmic traffic: the state read once and the output written once."""
+    import numpy as np
+    import torch
+
+    from jet_gb300 import capi
+
+    dev = torch.device("cuda:0")
+    dims, q = args.gate_shape.split(":")
+    shape = _parse_shape(dims)
+    q = int(q)
+    r, d = len(shape), shape[0]
+    rng = np.random.default_rng(SEED)
+    gate_axes = sorted(int(v) for v in rng.choice(r, size=q, replace=False))
+    free = [i for i in range(r) if i not in gate_axes]
+    a_perm = free + gate_axes
+    k = n = d ** q
+    m = int(np.prod([shape[i] for i in free]))
+    g_shape = [d] * (2 * q)
+    b_perm = list(range(q, 2 * q)) + list(range(q))  # gate labels (out..., in...)
+    tdt = torch.complex128 if args.permute_dtype == "c128" else torch.complex64
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    x = torch.randn(m * k, dtype=tdt, device=dev, generator=gen)
+    gt = torch.randn(k * n, dtype=tdt, device=dev, generator=gen)
+    y = torch.empty(m * n, dtype=tdt, device=dev)
+    xt = torch.empty_like(x)
+    y2 = torch.empty_like(y)
+    bt = capi.permute(gt, g_shape, b_perm)
+    assert capi.contract_workspace_size(shape, a_perm, g_shape, b_perm, m, n, k,
+                                        capi.dtype_code(tdt), capi.PREC_FP32) == 0
+
+    def skinny():
+        capi.contract(x, shape, a_perm, gt, g_shape, b_perm, m, n, k, out=y)
+
+    def transposing():
+        capi.permute(x, shape, a_perm, out=xt)
+        capi.multiply(xt, bt, m, n, k, out=y2)
+
+    st = torch.cuda.current_stream()
+    times = {}
+    for name, fn in (("skinny", skinny), ("transposing", transposing)):
+        for _ in range(args.warmup):
+            fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if name == "skinny":
+            with Clocks(0) as clk:
+                e0.record(st)
+                for _ in range(args.steps):
+                    fn()
+                e1.record(st)
+                torch.cuda.synchronize()
+            clocks = clk.summary()
+        else:
+            e0.record(st)
+            for _ in range(args.steps):
+                fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+        times[name] = e0.elapsed_time(e1) / args.steps
+    exact = bool(torch.equal(y, y2))
+    nbytes = (m * k + m * n) * x.element_size()
+    gbs = nbytes / times["skinny"] / 1e6
+    hbm, _, src = measured_peaks()
+    print(json.dumps({
+        "metric": "gate_bandwidth", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": times["skinny"],
+        "higher_is_better": True, "dtype": args.permute_dtype, "data": "synthetic (seeded)",
+        "config": {"workload": "gate on %s %s: %d-axis gate on axes %s (m %d, k %d, n %d)"
+                               % (dims, args.permute_dtype, q, gate_axes, m, k, n),
+                   "l2": "input and output each larger than L2" if nbytes // 2 > 129e6
+                   else "fits L2 (launch-bound case)"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": gbs / hbm, "peak_source": src, "traffic_algorithmic": nbytes},
+        "transposing_ms": times["transposing"],
+        "speedup_vs_transposing": times["transposing"] / times["skinny"],
+        "same_bits_as_transposing": exact, "clocks": clocks}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1254,8 +1342,17 @@ def main():
     ap.add_argument("--permute-shape", default=None,
                     help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
                          "permutation)")
-    ap.add_argument("--permute-dtype", default="c64", choices=["c64", "c128"])
+    ap.add_argument("--permute-dtype", default="c64", choices=["c64", "c128"],
+                    help="element type of --permute-shape and --gate-shape")
+    ap.add_argument("--gate-shape", default=None,
+                    help="time one gate applied to a state-like tensor instead: 'D^R:Q' (R axes "
+                         "of dimension D, a Q-axis gate on seeded positions)")
     args = ap.parse_args()
+    if args.gate_shape:
+        if args.warmup < 3:
+            args.warmup = 3
+        run_gate(args)
+        return
     if args.permute_shape:
         if args.warmup < 3:
             args.warmup = 3

@@ -71,6 +71,31 @@ inline unsigned GridFor(uint64_t work_items, int per_sm)
     return (unsigned)(g ? g : 1);
 }
 
+// Division by an invariant d (Granlund-Montgomery, the round-up method):
+// Magic32(d) gives (m, s) with n / d = (t + (n - t) / 2) >> s, t = hi32(n m),
+// exact for every 32-bit n; m = 0 marks d = 1.
+inline void Magic32(uint64_t d, uint32_t &m, uint32_t &sh)
+{
+    if (d <= 1) {
+        m = 0;
+        sh = 0;
+        return;
+    }
+    int l = 0;
+    while ((1ull << l) < d)
+        ++l;
+    m = (uint32_t)(((((1ull << l) - d) << 32) / d) + 1);
+    sh = (uint32_t)(l - 1);
+}
+
+__device__ __forceinline__ uint32_t DivMagic(uint32_t n, uint32_t m, uint32_t s)
+{
+    if (m == 0)
+        return n;
+    const uint32_t t = __umulhi(n, m);
+    return (t + ((n - t) >> 1)) >> s;
+}
+
 // Internal entry points shared between translation units.
 int PermuteImpl(const void *in, void *out, uint64_t batch, int rank,
                 const uint64_t *shape, const int32_t *perm, int dtype,
@@ -225,6 +250,20 @@ int ContractTuned(uint64_t batch, const void *A, int a_rank, const uint64_t *a_s
                   const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
                   uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_a, int scale_b,
                   void *workspace, cudaStream_t st, const ExpHints *hints = nullptr);
+
+// Skinny contractions (skinny.cu): one side of the product at most 16 wide,
+// k <= 64, read straight from the operands' layouts without transposes or
+// workspace. SkinnyApplies: whether the kernel takes this contraction (its
+// operands' axes fit its index tables); arguments as ContractForm's, after
+// its batch normalisation (batch 1: both flags 0).
+bool SkinnyApplies(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_perm,
+                   int a_batched, int b_rank, const uint64_t *b_shape, const int32_t *b_perm,
+                   int b_batched, uint64_t m, uint64_t n, uint64_t k);
+int SkinnyContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
+                   const int32_t *a_perm, int a_batched, const void *B, int b_rank,
+                   const uint64_t *b_shape, const int32_t *b_perm, int b_batched, void *C,
+                   uint64_t m, uint64_t n, uint64_t k, int dtype, int scale_exp,
+                   cudaStream_t st);
 
 int MultiplyPlain(const void *A, const void *B, void *C, uint64_t m,
                   uint64_t n, uint64_t k, int dtype, int scale_exp,

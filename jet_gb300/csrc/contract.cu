@@ -383,6 +383,9 @@ size_t FormWorkspace(uint64_t batch, int a_rank, const uint64_t *a_shape, const 
         const SplitLayout l = LayoutFor(precision, k, (double)batch * m * n * k, -1, 0, algo);
         return l.a_bytes(p.ba * m) + AlignUp(6 * p.bb * n * l.kp * l.word) + l.exp_bytes();
     }
+    if (k > 0 && SkinnyApplies(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape,
+                               b_perm, b_batched, m, n, k))
+        return 0;
     const size_t eb = ElemBytes(dtype);
     size_t ws = 0;
     if (!IsIdentity(a_rank, a_perm))
@@ -447,6 +450,10 @@ int ContractForm(uint64_t batch, const void *A, int a_rank, const uint64_t *a_sh
                             batch, A, a_rank, a_shape, a_perm, p.ba, p.ba > 1 ? a_batched : 0, B,
                             b_rank, b_shape, b_perm, p.bb, p.bb > 1 ? b_batched : 0, C, m, n, k,
                             dtype, scale_a, scale_b, ws, st, hints);
+    if (k > 0 && SkinnyApplies(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape,
+                               b_perm, b_batched, m, n, k))
+        return SkinnyContract(batch, A, a_rank, a_shape, a_perm, a_batched, B, b_rank, b_shape,
+                              b_perm, b_batched, C, m, n, k, dtype, scale_a + scale_b, st);
     int rc;
     const size_t eb = ElemBytes(dtype);
     const void *at = A;

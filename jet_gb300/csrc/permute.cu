@@ -115,16 +115,6 @@ struct GatherParams {
     uint32_t size_magic, size_shift;
 };
 
-// n / d for 32-bit n, with (m, s) from Magic32(d): t = hi32(n m),
-// q = (t + (n - t) / 2) >> s (the round-up method; exact for every n < 2^32).
-__device__ __forceinline__ uint32_t DivMagic(uint32_t n, uint32_t m, uint32_t s)
-{
-    if (m == 0)
-        return n;
-    const uint32_t t = __umulhi(n, m);
-    return (t + ((n - t) >> 1)) >> s;
-}
-
 // Input offset of output element idx: the mixed-radix walk over the output
 // dims, in 32-bit indices with multiply-shift division when the tensor has
 // fewer than 2^32 elements, else in 64 bits.
@@ -447,8 +437,6 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-void Magic32(uint64_t d, uint32_t &m, uint32_t &sh);
-
 // The tile plan of a simplified permutation (false: no tile of at most
 // kTileMax elements, or offsets past 32 bits; the gather kernel then runs).
 bool BuildTile(const Simplified &s, uint64_t batch, size_t elem_bytes, TileParams &p)
@@ -600,20 +588,6 @@ int LaunchTile(const TileParams &p, const void *in, Store store, cudaStream_t st
 
 // Multiplier and shift for dividing 32-bit values by d (d = 1: magic 0):
 // l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, s = l - 1.
-void Magic32(uint64_t d, uint32_t &m, uint32_t &sh)
-{
-    if (d <= 1) {
-        m = 0;
-        sh = 0;
-        return;
-    }
-    int l = 0;
-    while ((1ull << l) < d)
-        ++l;
-    m = (uint32_t)(((((1ull << l) - d) << 32) / d) + 1);
-    sh = (uint32_t)(l - 1);
-}
-
 void BuildGather(const Simplified &s, uint64_t batch, GatherParams &p)
 {
     int r = (int)s.dims.size();

@@ -154,6 +154,23 @@ def test_tuned_precision_accepted_and_workspace_covers_every_form():
     assert capi.lib.jetgpu_autotune_entry(0, None, None, None, None, None) == capi.ERR_INVALID
 
 
+def test_skinny_products_need_no_workspace():
+    """A gate on any axes of a large tensor (one side <= 16 wide, k <= 64) is
+    read in place by the skinny kernel: no transpose buffers. Wider products
+    keep the transposing path's workspace (host arithmetic only)."""
+    from jet_gb300 import capi
+
+    shape = [2] * 16
+    a_perm = [0, 1, 2, 4, 5, 6, 7, 8, 9, 10, 11, 13, 14, 15, 3, 12]  # gate on axes 3, 12
+    for n, prec in ((4, capi.PREC_FP32), (16, capi.PREC_FP32), (4, capi.PREC_AUTO)):
+        assert capi.contract_workspace_size(shape, a_perm, [4, n], [0, 1], 2 ** 14, n, 4,
+                                            capi.C64, prec) == 0
+        assert capi.contract_workspace_size([4, n], [1, 0], shape, a_perm[14:] + a_perm[:14],
+                                            n, 2 ** 14, 4, capi.C128, capi.PREC_FP32) == 0
+    assert capi.contract_workspace_size(shape, a_perm, [4, 32], [0, 1], 2 ** 14, 32, 4,
+                                        capi.C64, capi.PREC_FP32) > 0
+
+
 def test_group_offset_tables_match_numpy_views():
     """capi.view_offsets (the grouped launch's batch / row / column tables):
     element (b, i, j) of a view is the tensor's flat element at
