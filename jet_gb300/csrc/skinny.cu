@@ -46,7 +46,8 @@ struct SkinnyParams {
     uint64_t rows; // extent of the large operand's free index
     int s, k;      // small operand's free extent, contracted extent
     int narrow;    // rows < 2^32: row digits by 32-bit multiply-shift
-    int vec;       // complex64 rows of C stored 16 bytes at a time
+    int vec;       // complex64 rows of C stored 16 bytes at a time (s = S even)
+    uint32_t s_magic, s_shift; // division by s (DivMagic)
     SkAxes row;    // large operand: free axes
     uint32_t row_magic[kSkAxes], row_shift[kSkAxes];
     SkAxes big_c, big_b;               // large operand: contracted, batch axes
@@ -100,20 +101,43 @@ template <typename V> __device__ __forceinline__ void Mac(V &acc, const V &a, co
     acc.y = fma(a.y, b.x, acc.y);
 }
 
-// One CTA per (row range, batch item); each thread one row of the large
-// operand at a time. S: the small extent rounded up to a power of two (table
-// columns j >= s are zero and not stored). BigIsA: the large operand is A
-// (C's rows), else B (C's columns); the operands keep their roles in Mac.
+// Rows of the large operand one thread carries at once (more loads in
+// flight for narrow products; each table value read from shared memory
+// serves R rows). FP64 products are FMA-bound on this GPU: fewer.
+template <typename T, int S> struct SkRows {
+    static constexpr int R = sizeof(T) == 8 ? (S <= 4 ? 2 : 1) : (S <= 4 ? 4 : 2);
+    // CTAs per SM the register allocation must leave room for: three for
+    // the HBM-bound complex64 widths (measured: at two, S = 8 lost 25 %).
+    static constexpr int kMinBlocks = (sizeof(T) == 4 && S <= 8) ? 3 : 1;
+};
+
+// One CTA per (row range, batch item); each thread R rows of the large
+// operand at a time, `step` apart, so that every row's loads and stores are
+// coalesced across the warp. S: the small extent, or the next width the
+// kernel is built for (table columns j >= s are zero and not stored).
+// BigIsA: the large operand is A (C's rows), else B (C's columns); the
+// operands keep their roles in Mac.
 template <typename T, int S, bool BigIsA>
-__global__ void __launch_bounds__(kSkThreads)
+__global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
     skinny_kernel(const typename C2<T>::type *__restrict__ big,
                   const typename C2<T>::type *__restrict__ small,
                   typename C2<T>::type *__restrict__ C, const __grid_constant__ SkinnyParams p,
                   T scale)
 {
     using V = typename C2<T>::type;
+    constexpr int R = SkRows<T, S>::R;
+    constexpr int KC = 8 / R; // contracted values loaded per row at once
+    // Complex64 rows of 9 outputs (qutrit pairs) leave through shared memory:
+    // each warp's 32 rows of C are one contiguous run, written 16 bytes a
+    // lane, where direct 8-byte stores 72 bytes apart cost four times the
+    // store requests (measured: 3,233 -> 3,870 GB/s on 3^17). For 3, 4 and 8
+    // outputs the stage's registers and shared memory cost more occupancy
+    // than it saves (measured slower). Row stride in the stage odd (in 8-byte
+    // words): conflict-free writes.
+    constexpr bool kStage = std::is_same<T, float>::value && BigIsA && S == 9;
     __shared__ V tab[kSkMaxK][S];
     __shared__ uint64_t coff[kSkMaxK];
+    __shared__ V stage[kStage ? kSkThreads / 32 : 1][kStage ? 32 * (S + 1) : 1];
     const uint64_t b = blockIdx.y;
     big += AxesOffset(p.big_b, b);
     small += AxesOffset(p.small_b, b);
@@ -127,46 +151,113 @@ __global__ void __launch_bounds__(kSkThreads)
         coff[c] = AxesOffset(p.big_c, c);
     __syncthreads();
 
+    // The loop runs per warp (its first row wb), so that all 32 lanes stay in
+    // it together for the staged stores; lanes past the end only skip work.
+    const int lane = threadIdx.x & 31;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < p.rows; r += step) {
-        const V *x = big + RowOffset(p, r);
-        V acc[S];
+    for (uint64_t wb = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x - lane); wb < p.rows;
+         wb += step * R) {
+        const uint64_t r0 = wb + lane;
+        const V *x[R];
+        bool ok[R];
 #pragma unroll
-        for (int j = 0; j < S; ++j)
-            acc[j] = V{0, 0};
-        for (int c0 = 0; c0 < p.k; c0 += 8) {
-            V v[8];
+        for (int i = 0; i < R; ++i) {
+            const uint64_t r = r0 + i * step;
+            ok[i] = r < p.rows;
+            x[i] = big + (ok[i] ? RowOffset(p, r) : 0);
+        }
+        V acc[R][S];
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
-                v[u] = c0 + u < p.k ? __ldg(x + coff[c0 + u]) : V{0, 0};
+        for (int i = 0; i < R; ++i)
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int j = 0; j < S; ++j)
+                acc[i][j] = V{0, 0};
+        for (int c0 = 0; c0 < p.k; c0 += KC) {
+            V v[R][KC];
+#pragma unroll
+            for (int u = 0; u < KC; ++u) {
+                const bool in = c0 + u < p.k;
+                const uint64_t o = in ? coff[c0 + u] : 0;
+#pragma unroll
+                for (int i = 0; i < R; ++i)
+                    v[i][u] = (in && ok[i]) ? __ldg(x[i] + o) : V{0, 0};
+            }
+#pragma unroll
+            for (int u = 0; u < KC; ++u) {
                 if (c0 + u >= p.k)
                     break;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    if (BigIsA)
-                        Mac(acc[j], v[u], tab[c0 + u][j]);
-                    else
-                        Mac(acc[j], tab[c0 + u][j], v[u]);
+                    const V t = tab[c0 + u][j];
+#pragma unroll
+                    for (int i = 0; i < R; ++i) {
+                        if (BigIsA)
+                            Mac(acc[i][j], v[i][u], t);
+                        else
+                            Mac(acc[i][j], t, v[i][u]);
+                    }
                 }
             }
         }
-        V *out = C + r * p.out_row;
-        if constexpr (std::is_same<T, float>::value && BigIsA && S >= 2) {
-            if (p.vec) {
-                float4 *o4 = reinterpret_cast<float4 *>(out);
+        if constexpr (kStage) {
+            V *w = stage[threadIdx.x >> 5];
+            const int ws = p.s | 1;
 #pragma unroll
-                for (int j = 0; j < S; j += 2)
-                    o4[j / 2] = make_float4(acc[j].x * scale, acc[j].y * scale,
-                                            acc[j + 1].x * scale, acc[j + 1].y * scale);
-                continue;
+            for (int i = 0; i < R; ++i) {
+                const uint64_t rw = wb + i * step; // the warp's first row
+                if (rw >= p.rows)
+                    continue;
+                const int nv = (int)min((uint64_t)32, p.rows - rw);
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < S; ++j)
+                    if (j < p.s)
+                        w[lane * ws + j] = V{acc[i][j].x * scale, acc[i][j].y * scale};
+                __syncwarp();
+                V *dst = C + rw * p.out_row;
+                const uint32_t tot = (uint32_t)(nv * p.s);
+                if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+                    for (uint32_t q = lane; q < tot / 2; q += 32) {
+                        const uint32_t e = 2 * q;
+                        const uint32_t r = DivMagic(e, p.s_magic, p.s_shift);
+                        const uint32_t c = e - r * p.s;
+                        const V lo = w[r * ws + c];
+                        const V hi = c + 1 < (uint32_t)p.s ? w[r * ws + c + 1] : w[(r + 1) * ws];
+                        reinterpret_cast<float4 *>(dst)[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
+                    }
+                    if ((tot & 1) && lane == 0) {
+                        const uint32_t r = DivMagic(tot - 1, p.s_magic, p.s_shift);
+                        dst[tot - 1] = w[r * ws + (tot - 1 - r * p.s)];
+                    }
+                } else {
+                    for (uint32_t e = lane; e < tot; e += 32) {
+                        const uint32_t r = DivMagic(e, p.s_magic, p.s_shift);
+                        dst[e] = w[r * ws + (e - r * p.s)];
+                    }
+                }
             }
+            continue;
         }
 #pragma unroll
-        for (int j = 0; j < S; ++j)
-            if (j < p.s)
-                out[j * p.out_col] = V{acc[j].x * scale, acc[j].y * scale};
+        for (int i = 0; i < R; ++i) {
+            if (!ok[i])
+                continue;
+            V *out = C + (r0 + i * step) * p.out_row;
+            if constexpr (std::is_same<T, float>::value && BigIsA && S % 2 == 0) {
+                if (p.vec) {
+                    float4 *o4 = reinterpret_cast<float4 *>(out);
+#pragma unroll
+                    for (int j = 0; j < S; j += 2)
+                        o4[j / 2] = make_float4(acc[i][j].x * scale, acc[i][j].y * scale,
+                                                acc[i][j + 1].x * scale, acc[i][j + 1].y * scale);
+                    continue;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < S; ++j)
+                if (j < p.s)
+                    out[j * p.out_col] = V{acc[i][j].x * scale, acc[i][j].y * scale};
+        }
     }
 }
 
@@ -266,6 +357,7 @@ bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_
     if (p.narrow)
         for (int i = 0; i < p.row.n; ++i)
             Magic32(p.row.dim[i], p.row_magic[i], p.row_shift[i]);
+    Magic32((uint64_t)p.s, p.s_magic, p.s_shift);
     p.out_row = big_is_a ? n : 1;
     p.out_col = big_is_a ? 1 : n;
     p.out_batch = m * n;
@@ -293,7 +385,7 @@ int LaunchS(const void *big, const void *small, void *C, SkinnyParams &p, uint64
 {
     using V = typename C2<T>::type;
     auto kernel = skinny_kernel<T, S, BigIsA>;
-    p.vec = (std::is_same<T, float>::value && BigIsA && S >= 2 && p.s == S &&
+    p.vec = (std::is_same<T, float>::value && BigIsA && S % 2 == 0 && p.s == S &&
              (reinterpret_cast<uintptr_t>(C) & 15) == 0)
                 ? 1
                 : 0;
@@ -313,12 +405,20 @@ int LaunchT(const void *big, const void *small, void *C, SkinnyParams &p, uint64
             int scale_exp, cudaStream_t st)
 {
     const T scale = (T)ldexp(1.0, scale_exp);
-    if (p.s <= 1)
+    switch (p.s) {
+    case 1:
         return LaunchS<T, 1, BigIsA>(big, small, C, p, batch, scale, st);
-    if (p.s <= 2)
+    case 2:
         return LaunchS<T, 2, BigIsA>(big, small, C, p, batch, scale, st);
-    if (p.s <= 4)
+    case 3:
+        return LaunchS<T, 3, BigIsA>(big, small, C, p, batch, scale, st);
+    case 4:
         return LaunchS<T, 4, BigIsA>(big, small, C, p, batch, scale, st);
+    case 9:
+        return LaunchS<T, 9, BigIsA>(big, small, C, p, batch, scale, st);
+    default:
+        break;
+    }
     if (p.s <= 8)
         return LaunchS<T, 8, BigIsA>(big, small, C, p, batch, scale, st);
     return LaunchS<T, 16, BigIsA>(big, small, C, p, batch, scale, st);

@@ -145,6 +145,33 @@ def test_any_axis_order_and_unaligned_output(cuda):
         assert _rel(got, want) <= 1e-5, offset
 
 
+@pytest.mark.parametrize("s,k", [(5, 5), (6, 64), (7, 3), (10, 12), (12, 1), (15, 33)])
+@pytest.mark.parametrize("gate_first", [False, True])
+def test_widths_between_the_built_ones(cuda, s, k, gate_first):
+    """Small extents the kernel rounds up (5-7 to 8, 10-15 to 16), with
+    contracted extents that are not multiples of the load chunk, over a row
+    count that ends in a partial warp."""
+    from jet_gb300 import capi
+
+    big_shape = [13, k, 31, 8]
+    big = cases.tensor_data(600 + s, big_shape, np.complex64)
+    small = cases.tensor_data(700 + k, [s, k], np.complex64)
+    rows = 13 * 31 * 8
+    big_t = np.transpose(big.astype(np.complex128).reshape(big_shape), [0, 2, 3, 1]).reshape(rows, k)
+    small_m = small.astype(np.complex128).reshape(s, k)
+    if gate_first:
+        got = capi.contract(_dev(small, cuda), [s, k], [0, 1], _dev(big, cuda), big_shape,
+                            [1, 0, 2, 3], s, rows, k)
+        want = small_m @ big_t.T
+        m, n = s, rows
+    else:
+        got = capi.contract(_dev(big, cuda), big_shape, [0, 2, 3, 1], _dev(small, cuda), [s, k],
+                            [1, 0], rows, s, k)
+        want = big_t @ small_m.T
+        m, n = rows, s
+    assert _rel(got.cpu().numpy()[: m * n].reshape(m, n), want) <= 1e-5
+
+
 def test_more_axes_than_the_index_tables_fall_back(cuda):
     """Free axes that merge into more than the kernel's 12 index axes take
     the transposing path; the result is the same."""
