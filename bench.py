@@ -533,7 +533,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if not args.no_sliced and world == 1:
         line["sliced"] = {"config4": run_sliced_leg("config4", batch=16, chunks=2),
-                          "config2": run_sliced_leg("config2", batch=2, chunks=2)}
+                          "config2": run_sliced_leg("config2", batch=2, chunks=2),
+                          "m12": m12_leg(batch=8, chunks=4)[0]}
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_sample()
@@ -959,30 +960,25 @@ def run_sliced(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
-def run_m12(args, rank, world, local_rank):
+def m12_leg(batch=8, chunks=4):
     """The reference's own m12 benchmark network (53 qubits, depth 12;
     examples/paper_benchmarks/data_files/m12.json, kept as a golden fixture)
     with the reference's 9-index slicing (GPU/jet_gpu_m12/jet_sliced_subset.cpp:
     53-54, 512 slices), loaded through the TensorNetworkSerializer
     counterpart and contracted by the sliced contractor in AUTO and plain
-    FP32: slices/s, eff. TFLOP/s, the amplitude error of slices 0-2 against
-    the fixture's complex128 oracle values, and the CPU oracle (numpy
-    complex64, the reference's per-step arithmetic) timed on one slice."""
-    import torch
-
+    FP32: slices/s, eff. TFLOP/s and the amplitude error of slices 0-2
+    against the fixture's complex128 oracle values. Returns (record, the
+    fixture's tensors and path, the sliced labels)."""
     import jet_gb300 as jet
     from jet_gb300 import capi
 
     sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
     import make_network_fixtures as mk
 
-    torch.cuda.set_device(local_rank)
     ent = config_golden("m12")
     tensors, path = mk.load_network_npz(os.path.join(REPO, "tests", "golden", "m12_network.npz"))
     tnf = jet.TensorNetworkSerializer(dtype="complex64")(mk.network_json_text(tensors, path))
     sliced = ent["sliced"]
-    batch = args.sliced_batch or 8
-    chunks = args.sliced_chunks or 4
     capi.set_auto_form(capi.PREC_FP16X3)
     forms, errs = {}, {}
     for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
@@ -997,21 +993,34 @@ def run_m12(args, rank, world, local_rank):
         del one
         forms[name]["rel_err_vs_fp64"] = max(errs[name].values())
         forms[name]["rel_err_per_slice"] = errs[name]
+    out = {"workload": "m12: %d tensors, stored path of %d steps, %d sliced indices "
+                       "(%d slices), %d slices per batch"
+                       % (len(tensors), len(path), len(sliced), info["num_slices"], batch),
+           "unit": "slices/s", "forms": forms,
+           "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
+           "slice_pathinfo_flops": info["slice_flops"],
+           "extrapolated_all_slices_s": {f: info["num_slices"] / forms[f]["slices_per_s"]
+                                         for f in forms},
+           "error_reference": "complex128 oracle amplitudes of slices 0, 1, 2 (golden)"}
+    return out, tensors, path, sliced
+
+
+def run_m12(args, rank, world, local_rank):
+    """m12_leg as its own bench line, with the CPU oracle (numpy complex64,
+    the reference's per-step arithmetic) timed on one slice."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    batch = args.sliced_batch or 8
+    rec, tensors, path, sliced = m12_leg(batch, args.sliced_chunks or 4)
+    forms = rec["forms"]
     line = {"metric": METRIC, "value": forms["auto"]["slices_per_s"], "unit": "slices/s",
             "n_gpus": world, "steps": 1, "warmup": 1,
             "ms_per_step": forms["auto"]["s_per_slice"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64",
             "data": "the reference's m12 network (golden fixture of its data file)",
-            "config": {"workload": "m12: %d tensors, stored path of %d steps, %d sliced indices "
-                                   "(%d slices), %d slices per batch"
-                                   % (len(tensors), len(path), len(sliced), info["num_slices"],
-                                      batch)},
-            "forms": forms,
-            "tc_vs_plain_speedup": forms["auto"]["slices_per_s"] / forms["fp32"]["slices_per_s"],
-            "slice_pathinfo_flops": info["slice_flops"],
-            "extrapolated_all_slices_s": {f: info["num_slices"] / forms[f]["slices_per_s"]
-                                          for f in forms},
-            "error_reference": "complex128 oracle amplitudes of slices 0, 1, 2 (golden)"}
+            "config": {"workload": rec["workload"]}}
+    line.update({k: v for k, v in rec.items() if k not in ("workload", "unit")})
     if not args.no_cpu_baseline:
         from oracle import jet_oracle as jo
 
@@ -1027,6 +1036,100 @@ def run_m12(args, rank, world, local_rank):
                                 "sample": "slice 0 of m12 in complex64 through the numpy oracle "
                                           "(TensorNetwork::Contract restated, BLAS threads = "
                                           "host cores), %.1f s" % dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_m10(args, rank, world, local_rank):
+    """The reference's m10 benchmark network (53 qubits, depth 10;
+    examples/paper_benchmarks/data_files/m10.json, kept as a golden fixture)
+    contracted whole on its stored path, as GPU/jet_gpu_m10/jet_full.cpp does:
+    a TaskBasedContractor built over the path and run, per amplitude, in AUTO
+    and plain FP32; then one contractor contracted again and again (graph
+    replay). Errors against the fixture's compiled-reference complex<double>
+    amplitude; the CPU oracle (numpy complex64, the reference's per-step
+    arithmetic) timed on the same contraction."""
+    import torch
+
+    import jet_gb300 as jet
+    from jet_gb300 import capi
+
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    import make_network_fixtures as mk
+
+    torch.cuda.set_device(local_rank)
+    ent = config_golden("m10")
+    tensors, path = mk.load_network_npz(os.path.join(REPO, "tests", "golden", "m10_network.npz"))
+    tnf = jet.TensorNetworkSerializer(dtype="complex64")(mk.network_json_text(tensors, path))
+    want = complex(*ent["ref_c128"])
+    capi.set_auto_form(capi.PREC_FP16X3)
+    forms = {}
+    for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+        jet.set_precision(prec)
+
+        def run_tbc():
+            tbc = jet.TaskBasedContractor(dtype="complex64")
+            tbc.add_contraction_tasks(tnf.tensors, tnf.path)
+            tbc.add_deletion_tasks()
+            tbc.contract()
+            return complex(tbc.results[0].data[0])
+
+        for _ in range(args.warmup):
+            amp = run_tbc()
+        reps = []
+        while sum(reps) < 2.0 or len(reps) < 5:
+            t1 = time.perf_counter()
+            amp = run_tbc()
+            reps.append(time.perf_counter() - t1)
+        tbc = jet.TaskBasedContractor(dtype="complex64")
+        tbc.add_contraction_tasks(tnf.tensors, tnf.path)
+        tbc.add_deletion_tasks()
+        for _ in range(args.warmup):
+            tbc.contract()
+        rreps = []
+        while sum(rreps) < 2.0 or len(rreps) < 5:
+            t1 = time.perf_counter()
+            tbc.contract()
+            rreps.append(time.perf_counter() - t1)
+        ramp = complex(tbc.results[0].data[0])
+        del tbc
+        jet.set_precision(jet.PREC_FP32)
+        dt, dtr = statistics.median(reps), statistics.median(rreps)
+        flops = ent["pathinfo_flops"]
+        forms[name] = {"amplitudes_per_s": 1.0 / dt, "s_per_amplitude": dt,
+                       "eff_tflops": 4.0 * flops / dt / 1e12, "runs": len(reps),
+                       "rel_err_vs_fp64": abs(amp - want) / abs(want),
+                       "replayed": {"amplitudes_per_s": 1.0 / dtr, "s_per_amplitude": dtr,
+                                    "eff_tflops": 4.0 * flops / dtr / 1e12, "runs": len(rreps),
+                                    "same_bits": ramp == amp}}
+    line = {"metric": "amplitudes/s & eff. TFLOP/s of the m10 network, TC-split vs plain FP32",
+            "value": forms["auto"]["amplitudes_per_s"], "unit": "amplitudes/s",
+            "n_gpus": world, "steps": forms["auto"]["runs"],
+            "warmup": args.warmup, "ms_per_step": forms["auto"]["s_per_amplitude"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "the reference's m10 network (golden fixture of its data file)",
+            "config": {"workload": "m10: %d tensors, stored path of %d steps, whole network "
+                                   "(one amplitude) per TaskBasedContractor run"
+                                   % (len(tensors), len(path))},
+            "forms": forms,
+            "tc_vs_plain_speedup": forms["auto"]["amplitudes_per_s"]
+            / forms["fp32"]["amplitudes_per_s"],
+            "pathinfo_flops": ent["pathinfo_flops"],
+            "error_reference": "the compiled reference's complex<double> amplitude (golden)"}
+    if not args.no_cpu_baseline:
+        from oracle import jet_oracle as jo
+
+        tn = jo.OTensorNetwork()
+        for _, lab, sh, d in tensors:
+            tn.add_tensor(jo.OTensor.make(lab, sh, np.asarray(d, np.complex64), np.complex64))
+        t0 = time.perf_counter()
+        tn.contract(path, release=True)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "amplitudes/s",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "the whole m10 contraction in complex64 through the "
+                                          "numpy oracle (TensorNetwork::Contract restated, BLAS "
+                                          "threads = host cores), %.1f s" % dt}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -1338,7 +1441,8 @@ def main():
     ap.add_argument("--config", default="1",
                     help="1 (default): the pairwise contraction; 0, 2, 4, 4q (qutrits): sliced "
                          "circuit amplitudes through the sliced executor; 3: gradients; m12: the "
-                         "reference's m12 network with its own slicing")
+                         "reference's m12 network with its own slicing; m10: the reference's m10 "
+                         "network contracted whole")
     ap.add_argument("--permute-shape", default=None,
                     help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
                          "permutation)")
@@ -1371,6 +1475,9 @@ def main():
         return
     if args.config == "m12":
         run_m12(args, rank, world, local_rank)
+        return
+    if args.config == "m10":
+        run_m10(args, rank, world, local_rank)
         return
     if args.config != "1":
         run_sliced(args, rank, world, local_rank)

@@ -327,6 +327,136 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Products with a small output and a long k: M <= 16 and N <= 32, or M <= 32
+// and N <= 16, with k >= 2048 -- steps that close two large tensors down to a
+// few values, such as the 16 x 32 x 2^21 step of the reference's m10 network,
+// where gemm_kernel's 32 x 64 tile is three quarters empty and streams 8 k per
+// pass with few loads in flight (1.06 ms, 0.76 TB/s). Here one CTA per
+// (k range, batch item):
+//  * the A (MT x KC, stored k-major under an XOR swizzle) and B (KC x NT)
+//    tiles of the range come in by cp.async, double-buffered, elements past
+//    M, N or the range zero-filled; KC = 32 (complex64) or 16 (complex128),
+//    so each warp has four (two) k per tile between barriers;
+//  * the 8 warps split every tile, each lane accumulating an
+//    (MT / 4) x (NT / 8) block, so each warp covers the whole output;
+//  * the warps' sums are added in warp order in shared memory and the k
+//    ranges' in the workspace by reduce_partials: a fixed order.
+template <typename V> __device__ __forceinline__ void CpAsyncElem(V *smem, const V *src, bool valid)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+    const int n = valid ? (int)sizeof(V) : 0; // 0: zero-fill, nothing read
+    if constexpr (sizeof(V) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n)
+                     : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n)
+                     : "memory");
+}
+
+template <typename T, int MT, int NT>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
+    gemm_small_kernel(const typename C2<T>::type *__restrict__ A,
+                      const typename C2<T>::type *__restrict__ B,
+                      typename C2<T>::type *__restrict__ C, int64_t M, int64_t N, int64_t K,
+                      T scale, int64_t sa, int64_t sb, int64_t kchunk)
+{
+    using V = typename C2<T>::type;
+    constexpr int TR = MT / 4, TC = NT / 8;
+    constexpr int kSmallKC = sizeof(T) == 4 ? 32 : 16;
+    constexpr int NS = 2; // stages (three measured 5 % slower: occupancy, not latency, binds)
+    __shared__ __align__(16) V As[NS][kSmallKC * MT];
+    __shared__ __align__(16) V Bs[NS][kSmallKC][NT];
+    __shared__ V red[MT * NT];
+    const int64_t s = blockIdx.x, bz = blockIdx.z, batch = gridDim.z;
+    A += bz * sa;
+    B += bz * sb;
+    C += (s * batch + bz) * M * N;
+    const int64_t k_begin = s * kchunk;
+    const int64_t k_end = min(K, k_begin + kchunk);
+    const int64_t tiles = k_end > k_begin ? (k_end - k_begin + kSmallKC - 1) / kSmallKC : 0;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rg = lane >> 3, cg = lane & 7;
+
+    auto load = [&](int st, int64_t t) {
+        const int64_t k0 = k_begin + t * kSmallKC;
+        for (int e = tid; e < MT * kSmallKC; e += 256) {
+            const int i = e / kSmallKC, kk = e % kSmallKC;
+            const bool ok = i < M && k0 + kk < k_end;
+            CpAsyncElem(&As[st][kk * MT + (i ^ (kk & (MT - 1)))], ok ? A + i * K + k0 + kk : A,
+                        ok);
+        }
+        for (int e = tid; e < kSmallKC * NT; e += 256) {
+            const int kk = e / NT, j = e % NT;
+            const bool ok = j < N && k0 + kk < k_end;
+            CpAsyncElem(&Bs[st][kk][j], ok ? B + (k0 + kk) * N + j : B, ok);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    V acc[TR][TC];
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+        for (int c = 0; c < TC; ++c)
+            acc[r][c] = V{0, 0};
+    // Every iteration commits one group (empty past the last tile), so
+    // wait_group NS - 1 always means "tile t has landed".
+    for (int q = 0; q < NS - 1; ++q) {
+        if (q < tiles)
+            load(q, q);
+        else
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+    for (int64_t t = 0; t < tiles; ++t) {
+        const int st = (int)(t % NS);
+        if (t + NS - 1 < tiles)
+            load((int)((t + NS - 1) % NS), t + NS - 1);
+        else
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(NS - 1) : "memory");
+        __syncthreads();
+#pragma unroll
+        for (int kk = warp; kk < kSmallKC; kk += 8) {
+            V a[TR], b[TC];
+#pragma unroll
+            for (int r = 0; r < TR; ++r)
+                a[r] = As[st][kk * MT + ((rg * TR + r) ^ (kk & (MT - 1)))];
+#pragma unroll
+            for (int c = 0; c < TC; ++c)
+                b[c] = Bs[st][kk][cg * TC + c];
+#pragma unroll
+            for (int r = 0; r < TR; ++r)
+#pragma unroll
+                for (int c = 0; c < TC; ++c) {
+                    acc[r][c].x = fma(a[r].x, b[c].x, acc[r][c].x);
+                    acc[r][c].x = fma(-a[r].y, b[c].y, acc[r][c].x);
+                    acc[r][c].y = fma(a[r].x, b[c].y, acc[r][c].y);
+                    acc[r][c].y = fma(a[r].y, b[c].x, acc[r][c].y);
+                }
+        }
+        __syncthreads(); // the next load reuses this stage
+    }
+    for (int w = 0; w < 8; ++w) {
+        if (warp == w) {
+#pragma unroll
+            for (int r = 0; r < TR; ++r)
+#pragma unroll
+                for (int c = 0; c < TC; ++c) {
+                    V &o = red[(rg * TR + r) * NT + cg * TC + c];
+                    if (w == 0)
+                        o = acc[r][c];
+                    else
+                        o = V{o.x + acc[r][c].x, o.y + acc[r][c].y};
+                }
+        }
+        __syncthreads();
+    }
+    for (int64_t e = tid; e < M * N; e += 256) {
+        const V v = red[(e / N) * NT + e % N];
+        C[e] = V{v.x * scale, v.y * scale};
+    }
+}
+
 template <typename T>
 __global__ void reduce_partials(const typename C2<T>::type *__restrict__ part,
                                 typename C2<T>::type *__restrict__ out,
@@ -365,6 +495,32 @@ int64_t GemmSplits(int64_t ctas, int64_t batch, int64_t K, int64_t out_bytes)
     int64_t s = (target + ctas - 1) / ctas;
     s = min(s, K / 256);
     s = min(s, (int64_t)65535 / (batch > 0 ? batch : 1));
+    s = min(s, (int64_t)(32ll << 20) / (out_bytes > 0 ? out_bytes : 1));
+    return s < 2 ? 1 : s;
+}
+
+// The small-output kernel's tile (MT x NT; 0: the product is not one) and
+// its k ranges: one wave of CTAs (the kernel's launch bounds guarantee three
+// per SM for complex64, one for complex128; a second, partial wave cost a
+// third of the time), at least 1024 k each, at most 32 MiB of partial sums.
+inline void SmallTile(int64_t M, int64_t N, int64_t K, int &mt, int &nt)
+{
+    mt = nt = 0;
+    if (K < 2048 || M < 2 || N < 2)
+        return;
+    if (M <= 16 && N <= 32) {
+        mt = 16;
+        nt = 32;
+    } else if (M <= 32 && N <= 16) {
+        mt = 32;
+        nt = 16;
+    }
+}
+
+int64_t SmallSplits(int64_t batch, int64_t K, int64_t out_bytes, size_t elem_bytes)
+{
+    int64_t s = (int64_t)SmCount() * (elem_bytes == 8 ? 3 : 1) / (batch > 0 ? batch : 1);
+    s = min(s, K / 1024);
     s = min(s, (int64_t)(32ll << 20) / (out_bytes > 0 ? out_bytes : 1));
     return s < 2 ? 1 : s;
 }
@@ -427,6 +583,13 @@ size_t VectorWorkspace(int64_t batch, int64_t m, int64_t n, int64_t k)
     if (batch < 1)
         return 0;
     if (m > 1 && n > 1) {
+        int mt, nt;
+        SmallTile(m, n, k, mt, nt);
+        if (mt) { // small output, long k: partial sums of its k ranges
+            const int64_t S =
+                SmallSplits(batch, k, batch * m * n * (int64_t)sizeof(V), sizeof(V));
+            return S > 1 ? (size_t)(S * batch * m * n) * sizeof(V) : 0;
+        }
         // Matrix products: partial sums of the k splits (GemmSplits).
         int64_t tn, tm;
         GemmGrid<T>(m, n, tn, tm);
@@ -483,9 +646,33 @@ int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename
           void *ws, size_t ws_bytes, cudaStream_t stream)
 {
     using V = typename C2<T>::type;
+    const size_t need = VectorWorkspace<T>(batch, M, N, K);
+    int mt, nt;
+    SmallTile(M, N, K, mt, nt);
+    if (mt) {
+        JETGPU_REQUIRE(batch <= 65535, "batch too large for one launch");
+        const int64_t S = (need > 0 && ws != nullptr && ws_bytes >= need)
+                              ? SmallSplits(batch, K, batch * M * N * (int64_t)sizeof(V),
+                                            sizeof(V))
+                              : 1;
+        const int64_t kchunk = (K + S - 1) / S;
+        V *dst = S > 1 ? (V *)ws : C;
+        const dim3 grid((unsigned)S, 1u, (unsigned)batch);
+        if (mt == 16)
+            gemm_small_kernel<T, 16, 32><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa,
+                                                                   sb, kchunk);
+        else
+            gemm_small_kernel<T, 32, 16><<<grid, 256, 0, stream>>>(A, B, dst, M, N, K, scale, sa,
+                                                                   sb, kchunk);
+        int rc = CheckLaunch("gemm_small_kernel");
+        if (rc || S == 1)
+            return rc;
+        reduce_partials<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(
+            dst, C, batch * M * N, S);
+        return CheckLaunch("reduce_partials");
+    }
     int64_t tn, tm;
     GemmGrid<T>(M, N, tn, tm);
-    const size_t need = VectorWorkspace<T>(batch, M, N, K);
     const int64_t S =
         (need > 0 && ws != nullptr && ws_bytes >= need)
             ? GemmSplits(tn * tm * batch, batch, K, batch * M * N * (int64_t)sizeof(V))

@@ -76,6 +76,22 @@ __device__ __forceinline__ uint64_t AxesOffset(const SkAxes &a, uint64_t idx)
     return off;
 }
 
+// AxesOffset for an index below 2^32 (table entries, batch items): 32-bit
+// digit arithmetic.
+__device__ __forceinline__ uint64_t SmallOffset(const SkAxes &a, uint32_t idx)
+{
+    uint64_t off = 0;
+#pragma unroll
+    for (int i = 0; i < kSkAxes; ++i)
+        if (i < a.n) {
+            const uint32_t d = (uint32_t)a.dim[i];
+            const uint32_t q = idx / d;
+            off += (uint64_t)(idx - q * d) * a.stride[i];
+            idx = q;
+        }
+    return off;
+}
+
 __device__ __forceinline__ uint64_t RowOffset(const SkinnyParams &p, uint64_t r)
 {
     if (!p.narrow)
@@ -136,19 +152,28 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
     // words): conflict-free writes.
     constexpr bool kStage = std::is_same<T, float>::value && BigIsA && S == 9;
     __shared__ V tab[kSkMaxK][S];
-    __shared__ uint64_t coff[kSkMaxK];
+    __shared__ uint64_t coff[kSkMaxK];                 // large operand, per c
+    __shared__ uint64_t s_coff[kSkMaxK], s_foff[S];    // small operand, per c and j
     __shared__ V stage[kStage ? kSkThreads / 32 : 1][kStage ? 32 * (S + 1) : 1];
-    const uint64_t b = blockIdx.y;
-    big += AxesOffset(p.big_b, b);
-    small += AxesOffset(p.small_b, b);
-    C += b * p.out_batch;
+    const uint32_t b = blockIdx.y;
+    big += SmallOffset(p.big_b, b);
+    small += SmallOffset(p.small_b, b);
+    C += (uint64_t)b * p.out_batch;
+    // Offsets first (k + k + s digit walks), then the table from them: a
+    // short setup matters for the many small steps of a network.
+    for (int t = threadIdx.x; t < 2 * kSkMaxK + S; t += blockDim.x) {
+        if (t < p.k)
+            coff[t] = SmallOffset(p.big_c, t);
+        else if (t >= kSkMaxK && t - kSkMaxK < p.k)
+            s_coff[t - kSkMaxK] = SmallOffset(p.small_c, t - kSkMaxK);
+        else if (t >= 2 * kSkMaxK && t - 2 * kSkMaxK < p.s)
+            s_foff[t - 2 * kSkMaxK] = SmallOffset(p.small_f, t - 2 * kSkMaxK);
+    }
+    __syncthreads();
     for (int e = threadIdx.x; e < p.k * S; e += blockDim.x) {
         const int c = e / S, j = e % S;
-        tab[c][j] = j < p.s ? small[AxesOffset(p.small_c, c) + AxesOffset(p.small_f, j)]
-                            : V{0, 0};
+        tab[c][j] = j < p.s ? small[s_coff[c] + s_foff[j]] : V{0, 0};
     }
-    for (int c = threadIdx.x; c < p.k; c += blockDim.x)
-        coff[c] = AxesOffset(p.big_c, c);
     __syncthreads();
 
     // The loop runs per warp (its first row wb), so that all 32 lanes stay in

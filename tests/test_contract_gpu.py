@@ -177,6 +177,43 @@ def test_multiply_vector_and_edge_shapes(cuda, m, n, k, dtype):
         assert _rel(direct.reshape(m, n), want) <= (1e-5 if dtype == np.complex64 else 1e-12)
 
 
+@pytest.mark.parametrize("m,n,k", [(16, 32, 4096), (2, 2, 2048), (16, 32, 1 << 18),
+                                   (32, 16, 100003), (5, 7, 65536), (32, 16, 2049),
+                                   (12, 30, 50000), (3, 17, 9000)])
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_small_output_long_k(cuda, m, n, k, dtype):
+    """Products with a small output and a long k (gemm_small_kernel: M <= 16
+    and N <= 32 or M <= 32 and N <= 16, k >= 2048), k split into ranges
+    reduced in a fixed order: against complex128, and the same bits on a
+    second run; a permuted operand and a batch sharing A."""
+    import torch
+
+    from jet_gb300 import capi
+
+    a = cases.tensor_data(m * 11 + k, [m * k], dtype)
+    b = cases.tensor_data(n * 13 + k, [k * n], dtype)
+    want = a.astype(np.complex128).reshape(m, k) @ b.astype(np.complex128).reshape(k, n)
+    tol = 1e-5 if dtype == np.complex64 else 1e-12
+    da, db = _dev(a, cuda), _dev(b, cuda)
+    outs = []
+    for prec in (capi.PREC_FP32, capi.PREC_AUTO, capi.PREC_FP32):
+        out = capi.contract(da, [m, k], [0, 1], db, [k, n], [0, 1], m, n, k, precision=prec)
+        torch.cuda.synchronize()
+        outs.append(out[: m * n].clone())
+        assert _rel(out.cpu().numpy()[: m * n].reshape(m, n), want) <= tol, prec
+    assert torch.equal(outs[0], outs[2])
+    # A stored transposed (k x m, permutation [1, 0]); A shared by a batch of 3 Bs.
+    at = np.ascontiguousarray(a.reshape(m, k).T)
+    got = capi.contract(_dev(at, cuda), [k, m], [1, 0], db, [k, n], [0, 1], m, n, k)
+    assert _rel(got.cpu().numpy()[: m * n].reshape(m, n), want) <= tol
+    b3 = np.concatenate([b, 2 * b, -b])
+    got3 = capi.contract_batched(3, da, [m, k], [0, 1], 0, _dev(b3, cuda), [k, n], [0, 1], 1,
+                                 m, n, k).cpu().numpy()[: 3 * m * n].reshape(3, m, n)
+    for i, f in enumerate((1, 2, -1)):
+        assert _rel(got3[i], f * want) <= tol, i
+    assert capi.take_device_status() == 0
+
+
 def test_power_of_two_scales(cuda, tc_variant):
     from jet_gb300 import capi
 

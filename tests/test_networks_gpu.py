@@ -19,8 +19,9 @@
     parameterised circuit through the hand-written adjoint, against
     complex128 torch.einsum autograd on the CPU.
 
-Tolerances (complex64): 1e-5 relative for amplitudes against complex128 and
-against the reference's own complex<float> result; gradients within 1e-4
+Tolerances (complex64): 1e-5 relative for amplitudes against complex128, and
+against the reference's own complex<float> result 1e-5 plus that result's
+own distance from complex128 (two complex64 evaluations; m10: 7.5e-6); gradients within 1e-4
 absolute (the benchmark spec's bound for adjoint gradients); the loss, an
 expectation value in [-1, 1] that here cancels down to about 8e-4, within
 1e-6 absolute. complex128 runs: 1e-12 relative (amplitudes), 1e-10 absolute
@@ -88,8 +89,11 @@ def test_m10_full_amplitude_through_serializer(jet, amps, dtype, precision):
     finally:
         jet.set_precision(old)
     if dtype == "complex64":
-        assert _rel(got, _c(ent["ref_c64"])) <= 1e-5, _rel(got, _c(ent["ref_c64"]))
         assert _rel(got, _c(ent["ref_c128"])) <= 1e-5, _rel(got, _c(ent["ref_c128"]))
+        # Two complex64 evaluations: within 1e-5 plus the reference's own
+        # complex<float> distance from complex128 (7.5e-6 on m10).
+        ref_err = _rel(_c(ent["ref_c64"]), _c(ent["ref_c128"]))
+        assert _rel(got, _c(ent["ref_c64"])) <= 1e-5 + ref_err, _rel(got, _c(ent["ref_c64"]))
     else:
         assert _rel(got, _c(ent["ref_c128"])) <= 1e-12
         assert _rel(got, _c(ent["oracle_c128"])) <= 1e-12
@@ -109,7 +113,8 @@ def test_m12_reference_slices(jet, amps, precision):
         assert _rel(got, want) <= 1e-5, (v, _rel(got, want))
         vals.append(got)
     ref0 = _c(ent["slices"]["0"]["ref_c64"])
-    assert _rel(vals[0], ref0) <= 1e-5, _rel(vals[0], ref0)
+    ref_err = _rel(ref0, _c(ent["slices"]["0"]["oracle_c128"]))
+    assert _rel(vals[0], ref0) <= 1e-5 + ref_err, _rel(vals[0], ref0)
     # Slices 0 and 1 in one batch, summed in FP64 on the device.
     sc2 = jet.SlicedContractorC64(tnf.tensors, path, ent["sliced"], precision)
     sc2.set_batch_size(2)
