@@ -1044,9 +1044,9 @@ def run_m10(args, rank, world, local_rank):
     """The reference's m10 benchmark network (53 qubits, depth 10;
     examples/paper_benchmarks/data_files/m10.json, kept as a golden fixture)
     contracted whole on its stored path, as GPU/jet_gpu_m10/jet_full.cpp does:
-    a TaskBasedContractor built over the path and run, per amplitude, in AUTO
-    and plain FP32; then one contractor contracted again and again (graph
-    replay). Errors against the fixture's compiled-reference complex<double>
+    a TaskBasedContractor built over the path, then its contract() timed, per
+    amplitude, in AUTO and plain FP32; then one contractor contracted again
+    and again (graph replay). Errors against the fixture's compiled-reference complex<double>
     amplitude; the CPU oracle (numpy complex64, the reference's per-step
     arithmetic) timed on the same contraction."""
     import torch
@@ -1068,19 +1068,25 @@ def run_m10(args, rank, world, local_rank):
         jet.set_precision(prec)
 
         def run_tbc():
+            """(contract() seconds, build seconds, amplitude): a fresh
+            contractor's first, eager contract() is timed, as the reference's
+            jet_full.cpp times tbc.Contract().wait() after building it."""
+            t0 = time.perf_counter()
             tbc = jet.TaskBasedContractor(dtype="complex64")
             tbc.add_contraction_tasks(tnf.tensors, tnf.path)
             tbc.add_deletion_tasks()
+            t1 = time.perf_counter()
             tbc.contract()
-            return complex(tbc.results[0].data[0])
+            t2 = time.perf_counter()
+            return t2 - t1, t1 - t0, complex(tbc.results[0].data[0])
 
         for _ in range(args.warmup):
-            amp = run_tbc()
-        reps = []
+            run_tbc()
+        reps, builds = [], []
         while sum(reps) < 2.0 or len(reps) < 5:
-            t1 = time.perf_counter()
-            amp = run_tbc()
-            reps.append(time.perf_counter() - t1)
+            dt, db, amp = run_tbc()
+            reps.append(dt)
+            builds.append(db)
         tbc = jet.TaskBasedContractor(dtype="complex64")
         tbc.add_contraction_tasks(tnf.tensors, tnf.path)
         tbc.add_deletion_tasks()
@@ -1098,6 +1104,9 @@ def run_m10(args, rank, world, local_rank):
         flops = ent["pathinfo_flops"]
         forms[name] = {"amplitudes_per_s": 1.0 / dt, "s_per_amplitude": dt,
                        "eff_tflops": 4.0 * flops / dt / 1e12, "runs": len(reps),
+                       "build_s": statistics.median(builds),
+                       "timed": "contract() of a freshly built TaskBasedContractor (eager), "
+                                "as jet_full.cpp times it; building it (build_s) untimed",
                        "rel_err_vs_fp64": abs(amp - want) / abs(want),
                        "replayed": {"amplitudes_per_s": 1.0 / dtr, "s_per_amplitude": dtr,
                                     "eff_tflops": 4.0 * flops / dtr / 1e12, "runs": len(rreps),

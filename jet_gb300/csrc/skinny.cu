@@ -24,7 +24,6 @@
 
 #include <cstring>
 #include <type_traits>
-#include <vector>
 
 namespace jetgpu {
 namespace {
@@ -50,9 +49,12 @@ struct SkinnyParams {
     uint32_t s_magic, s_shift; // division by s (DivMagic)
     SkAxes row;    // large operand: free axes
     uint32_t row_magic[kSkAxes], row_shift[kSkAxes];
-    SkAxes big_c, big_b;               // large operand: contracted, batch axes
-    SkAxes small_c, small_f, small_b;  // small operand: contracted, free, batch
+    SkAxes big_b, small_b;                // batch axes of the two operands
     uint64_t out_row, out_col, out_batch; // C's element strides
+    // Offsets tabulated on the host: the large operand's per contracted
+    // index c, the small operand's per c and per free index j.
+    uint64_t coff[kSkMaxK];
+    uint32_t s_coff[kSkMaxK], s_foff[kSkMaxS];
 };
 
 template <typename T> struct C2;
@@ -152,27 +154,14 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
     // words): conflict-free writes.
     constexpr bool kStage = std::is_same<T, float>::value && BigIsA && S == 9;
     __shared__ V tab[kSkMaxK][S];
-    __shared__ uint64_t coff[kSkMaxK];                 // large operand, per c
-    __shared__ uint64_t s_coff[kSkMaxK], s_foff[S];    // small operand, per c and j
     __shared__ V stage[kStage ? kSkThreads / 32 : 1][kStage ? 32 * (S + 1) : 1];
     const uint32_t b = blockIdx.y;
     big += SmallOffset(p.big_b, b);
     small += SmallOffset(p.small_b, b);
     C += (uint64_t)b * p.out_batch;
-    // Offsets first (k + k + s digit walks), then the table from them: a
-    // short setup matters for the many small steps of a network.
-    for (int t = threadIdx.x; t < 2 * kSkMaxK + S; t += blockDim.x) {
-        if (t < p.k)
-            coff[t] = SmallOffset(p.big_c, t);
-        else if (t >= kSkMaxK && t - kSkMaxK < p.k)
-            s_coff[t - kSkMaxK] = SmallOffset(p.small_c, t - kSkMaxK);
-        else if (t >= 2 * kSkMaxK && t - 2 * kSkMaxK < p.s)
-            s_foff[t - 2 * kSkMaxK] = SmallOffset(p.small_f, t - 2 * kSkMaxK);
-    }
-    __syncthreads();
     for (int e = threadIdx.x; e < p.k * S; e += blockDim.x) {
         const int c = e / S, j = e % S;
-        tab[c][j] = j < p.s ? small[s_coff[c] + s_foff[j]] : V{0, 0};
+        tab[c][j] = j < p.s ? small[p.s_coff[c] + p.s_foff[j]] : V{0, 0};
     }
     __syncthreads();
 
@@ -202,7 +191,7 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
 #pragma unroll
             for (int u = 0; u < KC; ++u) {
                 const bool in = c0 + u < p.k;
-                const uint64_t o = in ? coff[c0 + u] : 0;
+                const uint64_t o = in ? p.coff[c0 + u] : 0;
 #pragma unroll
                 for (int i = 0; i < R; ++i)
                     v[i][u] = (in && ok[i]) ? __ldg(x[i] + o) : V{0, 0};
@@ -261,68 +250,124 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
                     }
                 }
             }
-            continue;
-        }
+        } else {
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-            if (!ok[i])
-                continue;
-            V *out = C + (r0 + i * step) * p.out_row;
-            if constexpr (std::is_same<T, float>::value && BigIsA && S % 2 == 0) {
-                if (p.vec) {
-                    float4 *o4 = reinterpret_cast<float4 *>(out);
-#pragma unroll
-                    for (int j = 0; j < S; j += 2)
-                        o4[j / 2] = make_float4(acc[i][j].x * scale, acc[i][j].y * scale,
-                                                acc[i][j + 1].x * scale, acc[i][j + 1].y * scale);
+            for (int i = 0; i < R; ++i) {
+                if (!ok[i])
                     continue;
-                }
-            }
+                V *out = C + (r0 + i * step) * p.out_row;
+                if constexpr (std::is_same<T, float>::value && BigIsA && S % 2 == 0) {
+                    if (p.vec) {
+                        float4 *o4 = reinterpret_cast<float4 *>(out);
 #pragma unroll
-            for (int j = 0; j < S; ++j)
-                if (j < p.s)
-                    out[j * p.out_col] = V{acc[i][j].x * scale, acc[i][j].y * scale};
+                        for (int j = 0; j < S; j += 2)
+                            o4[j / 2] =
+                                make_float4(acc[i][j].x * scale, acc[i][j].y * scale,
+                                            acc[i][j + 1].x * scale, acc[i][j + 1].y * scale);
+                        continue;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < S; ++j)
+                    if (j < p.s)
+                        out[j * p.out_col] = V{acc[i][j].x * scale, acc[i][j].y * scale};
+            }
         }
     }
+}
+
+// Small outputs (rows x s at most kSkTiny, a step of a few gates): one
+// thread per output element reads its row's k values and the small operand's
+// k values straight from global memory, all loads issued before any
+// arithmetic, no shared memory and no barrier: one memory round trip, where
+// skinny_kernel's table and rows take two. Same FMA sequence.
+constexpr int kSkTiny = 4096;
+
+template <typename T, bool BigIsA>
+__global__ void __launch_bounds__(kSkThreads)
+    skinny_tiny_kernel(const typename C2<T>::type *__restrict__ big,
+                       const typename C2<T>::type *__restrict__ small,
+                       typename C2<T>::type *__restrict__ C,
+                       const __grid_constant__ SkinnyParams p, T scale)
+{
+    using V = typename C2<T>::type;
+    const uint32_t b = blockIdx.y;
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (uint32_t)p.rows * (uint32_t)p.s)
+        return;
+    const uint32_t r = DivMagic(e, p.s_magic, p.s_shift);
+    const uint32_t j = e - r * (uint32_t)p.s;
+    const V *x = big + SmallOffset(p.big_b, b) + RowOffset(p, r);
+    const V *y = small + SmallOffset(p.small_b, b) + p.s_foff[j];
+    V acc{0, 0};
+    for (int c0 = 0; c0 < p.k; c0 += 8) {
+        V xv[8], yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const bool in = c0 + u < p.k;
+            xv[u] = in ? __ldg(x + p.coff[c0 + u]) : V{0, 0};
+            yv[u] = in ? __ldg(y + p.s_coff[c0 + u]) : V{0, 0};
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (c0 + u >= p.k)
+                break;
+            if (BigIsA)
+                Mac(acc, xv[u], yv[u]);
+            else
+                Mac(acc, yv[u], xv[u]);
+        }
+    }
+    C[(uint64_t)b * p.out_batch + r * p.out_row + j * p.out_col] =
+        V{acc.x * scale, acc.y * scale};
 }
 
 struct Ax {
     uint64_t d, s; // dimension, element stride
 };
 
+// Axes of one index group, outermost first (at most the 64 axes of a tensor;
+// on the stack: planning runs several times per contraction).
+struct AxList {
+    int n = 0;
+    Ax a[65];
+    void push(Ax x) { a[n++] = x; }
+};
+
 // Packs axes given outermost first, dropping unit axes and merging neighbours
 // that are contiguous (outer stride = inner stride x inner dim).
-bool Pack(const std::vector<Ax> &outer_first, SkAxes &out)
+bool Pack(const AxList &outer_first, SkAxes &out)
 {
-    std::vector<Ax> m;
-    for (const Ax &a : outer_first) {
+    AxList m;
+    for (int i = 0; i < outer_first.n; ++i) {
+        const Ax &a = outer_first.a[i];
         if (a.d == 1)
             continue;
-        if (!m.empty() && m.back().s == a.s * a.d) {
-            m.back().d *= a.d;
-            m.back().s = a.s;
+        if (m.n > 0 && m.a[m.n - 1].s == a.s * a.d) {
+            m.a[m.n - 1].d *= a.d;
+            m.a[m.n - 1].s = a.s;
         } else {
-            m.push_back(a);
+            m.push(a);
         }
     }
-    if ((int)m.size() > kSkAxes)
+    if (m.n > kSkAxes)
         return false;
-    out.n = (int)m.size();
+    out.n = m.n;
     for (int i = 0; i < out.n; ++i) {
-        out.dim[i] = m[out.n - 1 - i].d;
-        out.stride[i] = m[out.n - 1 - i].s;
+        out.dim[i] = m.a[out.n - 1 - i].d;
+        out.stride[i] = m.a[out.n - 1 - i].s;
     }
     return true;
 }
 
 // Appends the axes perm[j], perm[j + 1], ... whose dimensions multiply to
 // `extent` (false if no run of them does).
-bool Take(int rank, const uint64_t *shape, const int32_t *perm, const std::vector<uint64_t> &st,
-          int &j, uint64_t extent, std::vector<Ax> &out)
+bool Take(int rank, const uint64_t *shape, const int32_t *perm, const uint64_t *st, int &j,
+          uint64_t extent, AxList &out)
 {
     uint64_t p = 1;
     while (p < extent && j < rank) {
-        out.push_back({shape[perm[j]], st[perm[j]]});
+        out.push({shape[perm[j]], st[perm[j]]});
         p *= shape[perm[j]];
         ++j;
     }
@@ -330,7 +375,7 @@ bool Take(int rank, const uint64_t *shape, const int32_t *perm, const std::vecto
 }
 
 struct OperandAxes {
-    std::vector<Ax> batch, first, second;
+    AxList batch, first, second;
 };
 
 // An operand's permutation as (batch axes) (first group) (second group) with
@@ -339,7 +384,11 @@ struct OperandAxes {
 bool SplitOperand(int rank, const uint64_t *shape, const int32_t *perm, int mode,
                   uint64_t batch, uint64_t e1, uint64_t e2, OperandAxes &o)
 {
-    std::vector<uint64_t> st(rank, 1);
+    if (rank < 0 || rank > 64)
+        return false;
+    uint64_t st[64];
+    if (rank > 0)
+        st[rank - 1] = 1;
     for (int i = rank - 2; i >= 0; --i)
         st[i] = st[i + 1] * shape[i + 1];
     const uint64_t size = rank ? st[0] * shape[0] : 1;
@@ -347,7 +396,7 @@ bool SplitOperand(int rank, const uint64_t *shape, const int32_t *perm, int mode
     if (mode == 2 && !Take(rank, shape, perm, st, j, batch, o.batch))
         return false;
     if (mode == 1)
-        o.batch.push_back({batch, size});
+        o.batch.push({batch, size});
     return Take(rank, shape, perm, st, j, e1, o.first) &&
            Take(rank, shape, perm, st, j, e2, o.second);
 }
@@ -370,14 +419,36 @@ bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_
     p.rows = big_is_a ? m : n;
     p.s = (int)s;
     p.k = (int)k;
-    const bool ok = big_is_a ? (Pack(a.first, p.row) && Pack(a.second, p.big_c) &&
-                                Pack(a.batch, p.big_b) && Pack(b.first, p.small_c) &&
-                                Pack(b.second, p.small_f) && Pack(b.batch, p.small_b))
-                             : (Pack(b.second, p.row) && Pack(b.first, p.big_c) &&
-                                Pack(b.batch, p.big_b) && Pack(a.second, p.small_c) &&
-                                Pack(a.first, p.small_f) && Pack(a.batch, p.small_b));
+    const bool ok = big_is_a ? (Pack(a.first, p.row) && Pack(a.batch, p.big_b) &&
+                                Pack(b.batch, p.small_b))
+                             : (Pack(b.second, p.row) && Pack(b.batch, p.big_b) &&
+                                Pack(a.batch, p.small_b));
     if (!ok)
         return false;
+    // The contracted and small free offsets, digit by digit (innermost axis
+    // fastest), k + k + s entries.
+    auto tabulate = [](const AxList &axes, uint64_t count, auto *out) {
+        for (uint64_t idx = 0; idx < count; ++idx) {
+            uint64_t x = idx, off = 0;
+            for (int i = axes.n - 1; i >= 0; --i) {
+                off += (x % axes.a[i].d) * axes.a[i].s;
+                x /= axes.a[i].d;
+            }
+            out[idx] = static_cast<std::remove_pointer_t<decltype(out)>>(off);
+        }
+    };
+    tabulate(big_is_a ? a.second : b.first, k, p.coff);
+    const AxList &sc = big_is_a ? b.first : a.second;
+    const AxList &sf = big_is_a ? b.second : a.first;
+    uint64_t small_size = 1; // elements of one small operand
+    for (int i = 0; i < sc.n; ++i)
+        small_size += (sc.a[i].d - 1) * sc.a[i].s;
+    for (int i = 0; i < sf.n; ++i)
+        small_size += (sf.a[i].d - 1) * sf.a[i].s;
+    if (small_size > 0xffffffffull)
+        return false;
+    tabulate(sc, k, p.s_coff);
+    tabulate(sf, s, p.s_foff);
     p.narrow = p.rows < (1ull << 32) ? 1 : 0;
     if (p.narrow)
         for (int i = 0; i < p.row.n; ++i)
@@ -430,6 +501,14 @@ int LaunchT(const void *big, const void *small, void *C, SkinnyParams &p, uint64
             int scale_exp, cudaStream_t st)
 {
     const T scale = (T)ldexp(1.0, scale_exp);
+    if (p.rows * (uint64_t)p.s <= (uint64_t)kSkTiny) {
+        using V = typename C2<T>::type;
+        const unsigned gx = (unsigned)((p.rows * p.s + kSkThreads - 1) / kSkThreads);
+        skinny_tiny_kernel<T, BigIsA><<<dim3(gx, (unsigned)batch), kSkThreads, 0, st>>>(
+            static_cast<const V *>(big), static_cast<const V *>(small), static_cast<V *>(C), p,
+            scale);
+        return CheckLaunch("skinny_tiny_kernel");
+    }
     switch (p.s) {
     case 1:
         return LaunchS<T, 1, BigIsA>(big, small, C, p, batch, scale, st);

@@ -179,7 +179,11 @@ template <class TensorType> class TaskBasedContractor {
             size_t a, b, out;
             typename Tensor<S>::ContractionLayout layout;
         };
-        std::vector<Tensor<S>> leaves;             // by leaf slot
+        // By leaf slot: the leaves the tasks read, taken over from the first
+        // run as its deletion tasks release them (owned), else still held by
+        // the contractor (leaves points there).
+        std::vector<std::unique_ptr<Tensor<S>>> owned;
+        std::vector<const Tensor<S> *> leaves;
         std::unordered_map<std::string, size_t> leaf_slot;
         std::vector<Step> steps;
         std::vector<size_t> offset, bytes;         // per buffer id
@@ -191,6 +195,7 @@ template <class TensorType> class TaskBasedContractor {
     };
     ReplayPlan replay_;
     bool replay_on_ = true;
+    bool keep_leaves_ = false; // Run() hands released leaves to replay_
     size_t runs_ = 0;
 
     bool Replayable() const noexcept { return kGpuTensor && replay_on_; }
@@ -203,8 +208,9 @@ template <class TensorType> class TaskBasedContractor {
         runs_ = 0;
     }
 
-    // First run: the eager schedule, after copying every leaf the tasks read
-    // (the deletion tasks release the contractor's own leaves).
+    // First run: the eager schedule, keeping every leaf the tasks read for
+    // the replays (the deletion tasks would release the contractor's own
+    // leaves; they are handed over instead, without a copy).
     void RunAndKeepLeaves()
     {
         if constexpr (kGpuTensor) {
@@ -212,18 +218,34 @@ template <class TensorType> class TaskBasedContractor {
             for (const Task &t : tasks_)
                 if (t.kind == Task::CONTRACT)
                     produced.insert(t.name);
+            std::vector<const std::string *> names;
             for (const Task &t : tasks_) {
                 if (t.kind != Task::CONTRACT)
                     continue;
                 for (const std::string *in : {&t.input_1, &t.input_2})
                     if (!produced.count(*in) && !replay_.leaf_slot.count(*in)) {
-                        replay_.leaf_slot.emplace(*in, replay_.leaves.size());
-                        replay_.leaves.push_back(*name_to_tensor_.at(*in));
+                        replay_.leaf_slot.emplace(*in, names.size());
+                        names.push_back(in);
                     }
             }
+            replay_.owned.resize(names.size());
+            replay_.leaves.assign(names.size(), nullptr);
             replay_.precision = Tensor<S>::template ContractPrecision<S>();
+            keep_leaves_ = true;
+            try {
+                Run();
+            } catch (...) {
+                keep_leaves_ = false;
+                throw;
+            }
+            keep_leaves_ = false;
+            for (size_t i = 0; i < names.size(); ++i)
+                replay_.leaves[i] = replay_.owned[i] ? replay_.owned[i].get()
+                                                     : name_to_tensor_.at(*names[i]).get();
         }
-        Run();
+        else {
+            Run();
+        }
     }
 
     void Replay()
@@ -262,7 +284,8 @@ template <class TensorType> class TaskBasedContractor {
                     return it->second;
                 const auto leaf = r.leaf_slot.at(name);
                 id.emplace(name, shape_of.size());
-                shape_of.push_back(Tensor<S>(r.leaves[leaf].GetIndices(), r.leaves[leaf].GetShape()));
+                shape_of.push_back(
+                    Tensor<S>(r.leaves[leaf]->GetIndices(), r.leaves[leaf]->GetShape()));
                 r.leaf_of.push_back((int)leaf);
                 return shape_of.size() - 1;
             };
@@ -341,7 +364,7 @@ template <class TensorType> class TaskBasedContractor {
             r.ws = Gpu::DeviceBuffer(ws);
             auto ptr = [&](size_t b) -> void * {
                 if (r.leaf_of[b] >= 0)
-                    return const_cast<S *>(r.leaves[r.leaf_of[b]].GetDeviceData());
+                    return const_cast<S *>(r.leaves[r.leaf_of[b]]->GetDeviceData());
                 return static_cast<char *>(r.arena.get()) + r.offset[b];
             };
             // Leaf and result buffers are resolved (and, if need be, uploaded)
@@ -419,8 +442,16 @@ template <class TensorType> class TaskBasedContractor {
                     std::make_unique<TensorType>(TensorType::ContractTensors(a, b));
                 const auto it = delete_after.find(t);
                 if (it != delete_after.end())
-                    for (const auto &name : it->second)
+                    for (const auto &name : it->second) {
+                        if constexpr (kGpuTensor) {
+                            const auto slot = replay_.leaf_slot.find(name);
+                            if (keep_leaves_ && slot != replay_.leaf_slot.end()) {
+                                replay_.owned[slot->second] = std::move(name_to_tensor_[name]);
+                                continue;
+                            }
+                        }
                         name_to_tensor_[name] = nullptr;
+                    }
             }
             else if (task.kind == Task::STORE) {
                 results_[task.result_id] = *name_to_tensor_.at(task.name);

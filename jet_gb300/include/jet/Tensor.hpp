@@ -452,33 +452,53 @@ template <class T = std::complex<float>> class Tensor {
         std::vector<int32_t> a_perm, b_perm;
         uint64_t m = 1, n = 1, k = 1;
     };
+    // One pass over the label pairs (ranks are at most 64): the same sets as
+    // VectorSubtraction / VectorIntersection (Utilities.hpp) build through
+    // hash sets, without their allocations -- this runs once per path step.
     template <class U = T>
     static ContractionLayout LayoutOf(const Tensor<U> &A, const Tensor<U> &B)
     {
-        using namespace Utilities;
         ContractionLayout l;
-        const auto left = VectorSubtraction(A.GetIndices(), B.GetIndices());
-        const auto right = VectorSubtraction(B.GetIndices(), A.GetIndices());
-        const auto common = VectorIntersection(A.GetIndices(), B.GetIndices());
-        const auto &ad = A.GetIndexToDimension();
-        const auto &bd = B.GetIndexToDimension();
-        for (const auto &x : left) {
-            l.m *= ad.at(x);
-            l.c_shape.push_back(ad.at(x));
-        }
-        for (const auto &x : right) {
-            l.n *= bd.at(x);
-            l.c_shape.push_back(bd.at(x));
-        }
-        for (const auto &x : common)
-            l.k *= ad.at(x);
-        for (const auto &x : VectorConcatenation(left, common))
-            l.a_perm.push_back(PositionOf(A.GetIndices(), x));
-        for (const auto &x : VectorConcatenation(common, right))
-            l.b_perm.push_back(PositionOf(B.GetIndices(), x));
-        l.c_indices = VectorConcatenation(left, right);
-        l.a_shape.assign(A.GetShape().begin(), A.GetShape().end());
-        l.b_shape.assign(B.GetShape().begin(), B.GetShape().end());
+        const auto &ai = A.GetIndices();
+        const auto &bi = B.GetIndices();
+        const auto &as = A.GetShape();
+        const auto &bs = B.GetShape();
+        const size_t ra = ai.size(), rb = bi.size();
+        std::vector<int32_t> b_pos(ra, -1); // first position in B of A's label i
+        std::vector<char> b_in_a(rb, 0);
+        for (size_t i = 0; i < ra; ++i)
+            for (size_t j = 0; j < rb; ++j)
+                if (ai[i] == bi[j]) {
+                    if (b_pos[i] < 0)
+                        b_pos[i] = static_cast<int32_t>(j);
+                    b_in_a[j] = 1;
+                }
+        l.c_indices.reserve(ra + rb);
+        l.c_shape.reserve(ra + rb);
+        l.a_perm.reserve(ra);
+        l.b_perm.reserve(rb);
+        for (size_t i = 0; i < ra; ++i)
+            if (b_pos[i] < 0) { // left = A \ B
+                l.m *= as[i];
+                l.c_shape.push_back(as[i]);
+                l.c_indices.push_back(ai[i]);
+                l.a_perm.push_back(static_cast<int32_t>(i));
+            }
+        for (size_t i = 0; i < ra; ++i)
+            if (b_pos[i] >= 0) { // common = A ∩ B, in A's order
+                l.k *= as[i];
+                l.a_perm.push_back(static_cast<int32_t>(i));
+                l.b_perm.push_back(b_pos[i]);
+            }
+        for (size_t j = 0; j < rb; ++j)
+            if (!b_in_a[j]) { // right = B \ A
+                l.n *= bs[j];
+                l.c_shape.push_back(bs[j]);
+                l.c_indices.push_back(bi[j]);
+                l.b_perm.push_back(static_cast<int32_t>(j));
+            }
+        l.a_shape.assign(as.begin(), as.end());
+        l.b_shape.assign(bs.begin(), bs.end());
         return l;
     }
 

@@ -89,6 +89,41 @@ def test_gate_on_state_matches_oracle(cuda, dtype, dim, rank, q_in, q_out, gate_
 
 
 @pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+@pytest.mark.parametrize("dim,rank,q_in,q_out", [(2, 8, 2, 2), (2, 10, 1, 1), (3, 5, 2, 2),
+                                                 (2, 9, 6, 1), (2, 4, 1, 0), (3, 6, 1, 1),
+                                                 (2, 12, 3, 3)])
+@pytest.mark.parametrize("gate_first", [False, True])
+def test_tiny_outputs_match_oracle_and_transposing_bits(cuda, dtype, dim, rank, q_in, q_out,
+                                                        gate_first):
+    """Outputs of at most 4096 elements (skinny_tiny_kernel: one thread per
+    output, no shared memory): the oracle, and where m, n > 1 the same bits
+    as permute + multiply."""
+    import torch
+
+    from jet_gb300 import capi
+
+    seed = 1000 + 100 * dim + 10 * rank + 3 * q_in + q_out
+    s_lab, s_shape, st, g_lab, g_shape, g = _gate_case(seed, rank, dim, q_in, q_out, dtype)
+    if gate_first:
+        a_lab, a_shape, a, b_lab, b_shape, b = g_lab, g_shape, g, s_lab, s_shape, st
+    else:
+        a_lab, a_shape, a, b_lab, b_shape, b = s_lab, s_shape, st, g_lab, g_shape, g
+    a_perm, b_perm, m, n, k, lab = _plan(a_lab, a_shape, b_lab, b_shape)
+    assert m * n <= 4096
+    want = jo.contract_tensors(jo.OTensor.make(a_lab, a_shape, a, np.complex128),
+                               jo.OTensor.make(b_lab, b_shape, b, np.complex128))
+    da, db = _dev(a, cuda), _dev(b, cuda)
+    got = capi.contract(da, a_shape, a_perm, db, b_shape, b_perm, m, n, k)
+    tol = 1e-5 if dtype == np.complex64 else 1e-12
+    assert _rel(got.cpu().numpy()[: m * n], want.data.reshape(-1)) <= tol
+    if m > 1 and n > 1:
+        ref = capi.multiply(capi.permute(da, a_shape, a_perm), capi.permute(db, b_shape, b_perm),
+                            m, n, k)
+        torch.cuda.synchronize()
+        assert torch.equal(got[: m * n], ref[: m * n])
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
 @pytest.mark.parametrize("q_in,q_out,gate_first", [(2, 2, False), (3, 3, True), (1, 1, False),
                                                    (4, 2, True), (6, 4, False)])
 def test_same_bits_as_the_transposing_path(cuda, dtype, q_in, q_out, gate_first):
