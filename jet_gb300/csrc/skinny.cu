@@ -401,9 +401,12 @@ bool SplitOperand(int rank, const uint64_t *shape, const int32_t *perm, int mode
            Take(rank, shape, perm, st, j, e2, o.second);
 }
 
+// The kernel parameters of a skinny contraction (false: not one). `tables`:
+// also tabulate the offsets (needed for a launch, not to decide).
 bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_perm,
           int a_batched, int b_rank, const uint64_t *b_shape, const int32_t *b_perm,
-          int b_batched, uint64_t m, uint64_t n, uint64_t k, SkinnyParams &p, bool &big_is_a)
+          int b_batched, uint64_t m, uint64_t n, uint64_t k, SkinnyParams &p, bool &big_is_a,
+          bool tables = true)
 {
     if (k == 0 || k > kSkMaxK || m == 0 || n == 0 || batch == 0 || batch > 65535)
         return false;
@@ -437,7 +440,6 @@ bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_
             out[idx] = static_cast<std::remove_pointer_t<decltype(out)>>(off);
         }
     };
-    tabulate(big_is_a ? a.second : b.first, k, p.coff);
     const AxList &sc = big_is_a ? b.first : a.second;
     const AxList &sf = big_is_a ? b.second : a.first;
     uint64_t small_size = 1; // elements of one small operand
@@ -447,6 +449,9 @@ bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_
         small_size += (sf.a[i].d - 1) * sf.a[i].s;
     if (small_size > 0xffffffffull)
         return false;
+    if (!tables)
+        return true;
+    tabulate(big_is_a ? a.second : b.first, k, p.coff);
     tabulate(sc, k, p.s_coff);
     tabulate(sf, s, p.s_foff);
     p.narrow = p.rows < (1ull << 32) ? 1 : 0;
@@ -537,7 +542,7 @@ bool SkinnyApplies(uint64_t batch, int a_rank, const uint64_t *a_shape, const in
     SkinnyParams p;
     bool big_is_a;
     return Plan(batch, a_rank, a_shape, a_perm, a_batched, b_rank, b_shape, b_perm, b_batched,
-                m, n, k, p, big_is_a);
+                m, n, k, p, big_is_a, false);
 }
 
 int SkinnyContract(uint64_t batch, const void *A, int a_rank, const uint64_t *a_shape,
