@@ -418,20 +418,42 @@ __global__ void __launch_bounds__(kThreads)
         if ((int)threadIdx.x < g)
             TileBases(p, t0 + threadIdx.x, base_in[threadIdx.x], base_out[threadIdx.x]);
         __syncthreads();
+        // Tiles of at least two thread sweeps go one tile at a time (no
+        // division per element; measured 4-5 % faster on 3^16, 3^18, 5^11);
+        // smaller tiles (81, 243 elements) share the sweeps across tiles.
+        const bool per_tile = p.T >= 2 * kThreads;
         const int n = g * p.T;
+        if (per_tile) {
+            for (int j = 0; j < g; ++j) {
+                const E *src = in + base_in[j];
+                E *dst = tile + j * p.T;
+                for (int e = threadIdx.x; e < p.T; e += blockDim.x)
+                    CopyAsync(&dst[pos[e]], src + in_off[e]);
+            }
+        } else {
 #pragma unroll 4
-        for (int u = threadIdx.x; u < n; u += blockDim.x) {
-            const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
-            const int e = u - j * p.T;
-            CopyAsync(&tile[j * p.T + pos[e]], in + base_in[j] + (uint64_t)in_off[e]);
+            for (int u = threadIdx.x; u < n; u += blockDim.x) {
+                const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
+                const int e = u - j * p.T;
+                CopyAsync(&tile[j * p.T + pos[e]], in + base_in[j] + (uint64_t)in_off[e]);
+            }
         }
         asm volatile("cp.async.wait_all;\n" ::: "memory");
         __syncthreads();
+        if (per_tile) {
+            for (int j = 0; j < g; ++j) {
+                const uint64_t bo = base_out[j];
+                const E *src = tile + j * p.T;
+                for (int f = threadIdx.x; f < p.T; f += blockDim.x)
+                    store(bo + (uint64_t)out_off[f], src[f]);
+            }
+        } else {
 #pragma unroll 4
-        for (int u = threadIdx.x; u < n; u += blockDim.x) {
-            const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
-            const int f = u - j * p.T;
-            store(base_out[j] + (uint64_t)out_off[f], tile[u]);
+            for (int u = threadIdx.x; u < n; u += blockDim.x) {
+                const int j = (int)DivMagic((uint32_t)u, p.t_magic, p.t_shift);
+                const int f = u - j * p.T;
+                store(base_out[j] + (uint64_t)out_off[f], tile[u]);
+            }
         }
         __syncthreads();
     }
