@@ -189,6 +189,8 @@ int jetgpu_multiply(const void *A, const void *B, void *C, uint64_t m,
  * the product (C = (2^scale_a A)(2^scale_b B)); 0 for none.
  * workspace: caller-owned device scratch of at least
  * jetgpu_contract_workspace_size(...) bytes (may be NULL when that is 0).
+ * Products with one side at most 16 wide and k <= 64 (a gate on a large
+ * tensor) read A and B in place through the permutations and need none.
  */
 size_t jetgpu_contract_workspace_size(int a_rank, const uint64_t *a_shape,
                                       const int32_t *a_perm, int b_rank,
