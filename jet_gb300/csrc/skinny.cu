@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
     // than it saves (measured slower). Row stride in the stage odd (in 8-byte
     // words): conflict-free writes.
     constexpr bool kStage = std::is_same<T, float>::value && BigIsA && S == 9;
-    __shared__ V tab[kSkMaxK][S];
+    __shared__ __align__(16) V tab[kSkMaxK][S];
     __shared__ V stage[kStage ? kSkThreads / 32 : 1][kStage ? 32 * (S + 1) : 1];
     const uint32_t b = blockIdx.y;
     big += SmallOffset(p.big_b, b);
