@@ -1264,8 +1264,9 @@ def _parse_shape(text):
 
 
 def run_permute(args):
-    """One permute (jetgpu_permute) of a seeded random permutation, timed with
-    CUDA events on the launching stream over --steps launches after --warmup;
+    """One permute (jetgpu_permute) of a seeded random permutation (or
+    --permute-perm), timed with CUDA events on the launching stream over
+    --steps launches after --warmup;
     the output is compared bit for bit with torch's permute of the same
     tensor. Algorithmic traffic: one read and one write of every element."""
     import numpy as np
@@ -1275,7 +1276,8 @@ def run_permute(args):
 
     dev = torch.device("cuda:0")
     shape = _parse_shape(args.permute_shape)
-    perm = [int(v) for v in np.random.default_rng(SEED).permutation(len(shape))]
+    perm = ([int(v) for v in args.permute_perm.split(",")] if args.permute_perm else
+            [int(v) for v in np.random.default_rng(SEED).permutation(len(shape))])
     tdt = torch.complex128 if args.permute_dtype == "c128" else torch.complex64
     n = int(np.prod(shape))
     g = torch.Generator(device=dev)
@@ -1455,6 +1457,9 @@ def main():
     ap.add_argument("--permute-shape", default=None,
                     help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
                          "permutation)")
+    ap.add_argument("--permute-perm", default=None,
+                    help="with --permute-shape: this permutation ('2,0,1') instead of a seeded "
+                         "random one")
     ap.add_argument("--permute-dtype", default="c64", choices=["c64", "c128"],
                     help="element type of --permute-shape and --gate-shape")
     ap.add_argument("--gate-shape", default=None,
