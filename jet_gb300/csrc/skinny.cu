@@ -291,6 +291,12 @@ __global__ void __launch_bounds__(kSkThreads)
                        const __grid_constant__ SkinnyParams p, T scale)
 {
     using V = typename C2<T>::type;
+    // Launched with programmatic stream serialisation: the launch may begin
+    // while the previous kernel of the stream finishes; every memory access
+    // here follows this wait for it (a no-op when launched plainly).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // The next tiny step may start launching now (it waits for this one).
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint32_t b = blockIdx.y;
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (uint32_t)p.rows * (uint32_t)p.s)
@@ -509,9 +515,22 @@ int LaunchT(const void *big, const void *small, void *C, SkinnyParams &p, uint64
     if (p.rows * (uint64_t)p.s <= (uint64_t)kSkTiny) {
         using V = typename C2<T>::type;
         const unsigned gx = (unsigned)((p.rows * p.s + kSkThreads - 1) / kSkThreads);
-        skinny_tiny_kernel<T, BigIsA><<<dim3(gx, (unsigned)batch), kSkThreads, 0, st>>>(
-            static_cast<const V *>(big), static_cast<const V *>(small), static_cast<V *>(C), p,
-            scale);
+        // A chain of tiny steps is bound by launch latency: let each launch
+        // overlap the end of the kernel before it (the kernel waits for it
+        // before touching memory).
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(gx, (unsigned)batch);
+        cfg.blockDim = dim3(kSkThreads);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        JETGPU_CUDA_TRY(cudaLaunchKernelEx(&cfg, skinny_tiny_kernel<T, BigIsA>,
+                                           static_cast<const V *>(big),
+                                           static_cast<const V *>(small), static_cast<V *>(C), p,
+                                           scale));
         return CheckLaunch("skinny_tiny_kernel");
     }
     switch (p.s) {
