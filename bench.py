@@ -611,7 +611,7 @@ def config_golden(name):
 def run_sliced_leg(name, batch, chunks, fp32_chunks=1):
     """A sliced circuit of the golden fixtures beside the config-1 line, in
     the tensor-core AUTO form and in plain FP32: slices/s of each and their
-    ratio (the benchmark spec's target is >= 3x), and each form's error on single
+    ratio (the target is at least 3x), and each form's error on single
     slices against the complex128 oracle amplitudes of the fixture where it
     has them (config 4), else AUTO's difference from FP32 (config 2)."""
     import jet_gb300 as jet

@@ -22,7 +22,7 @@
 Tolerances (complex64): 1e-5 relative for amplitudes against complex128, and
 against the reference's own complex<float> result 1e-5 plus that result's
 own distance from complex128 (two complex64 evaluations; m10: 7.5e-6); gradients within 1e-4
-absolute (the benchmark spec's bound for adjoint gradients); the loss, an
+absolute (the bound set for adjoint gradients); the loss, an
 expectation value in [-1, 1] that here cancels down to about 8e-4, within
 1e-6 absolute. complex128 runs: 1e-12 relative (amplitudes), 1e-10 absolute
 (gradients), 1e-12 absolute (loss).
