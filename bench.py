@@ -1040,6 +1040,79 @@ def run_m12(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_m12_tbc(args, rank, world, local_rank):
+    """The reference's m12 flow (GPU/jet_gpu_m12/jet_sliced_subset.cpp:
+    50-101) through the TaskBasedContractor API: the m12 network sliced over
+    its 9 indices, the first S slices (the reference's default: 3; here
+    --sliced-batch) each added to one contractor, which shares their
+    slice-independent tasks, then deletion and reduction tasks, and the
+    contractor's first contract() timed (eager), then its graph replay. The
+    reduction is checked against the sum of the fixture's complex128 oracle
+    amplitudes of those slices."""
+    import torch
+
+    import jet_gb300 as jet
+    from jet_gb300 import capi
+
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    import make_network_fixtures as mk
+
+    torch.cuda.set_device(local_rank)
+    ent = config_golden("m12")
+    tensors, path = mk.load_network_npz(os.path.join(REPO, "tests", "golden", "m12_network.npz"))
+    text = mk.network_json_text(tensors, path)
+    n_slices = args.sliced_batch or 3
+    capi.set_auto_form(capi.PREC_FP16X3)
+    forms = {}
+    for name, prec in (("auto", jet.PREC_AUTO), ("fp32", jet.PREC_FP32)):
+        jet.set_precision(prec)
+        runs, replays, shared = [], [], 0
+        for rep in range(args.warmup + 3):
+            tbc = jet.TaskBasedContractor(dtype="complex64")
+            for v in range(n_slices):
+                tnf = jet.TensorNetworkSerializer(dtype="complex64")(text)
+                tnf.tensors.slice_indices(ent["sliced"], v)
+                shared = max(shared, tbc.add_contraction_tasks(
+                    tnf.tensors, jet.PathInfo(tnf.tensors, tnf.path.path)))
+            tbc.add_deletion_tasks()
+            tbc.add_reduction_task()
+            t0 = time.perf_counter()
+            tbc.contract()
+            t1 = time.perf_counter()
+            got = complex(tbc.reduction_result.data[0])
+            t2 = time.perf_counter()
+            tbc.contract()
+            t3 = time.perf_counter()
+            if rep >= args.warmup:
+                runs.append(t1 - t0)
+                replays.append(t3 - t2)
+            del tbc
+        jet.set_precision(jet.PREC_FP32)
+        want = [complex(*ent["slices"][str(v)]["oracle_c128"])
+                for v in range(n_slices) if str(v) in ent["slices"]]
+        err = (abs(got - sum(want)) / sum(abs(w) for w in want)
+               if len(want) == n_slices else None)
+        dt, dtr = statistics.median(runs), statistics.median(replays)
+        forms[name] = {"slices_per_s": n_slices / dt, "s_per_contract": dt,
+                       "replayed": {"slices_per_s": n_slices / dtr, "s_per_contract": dtr},
+                       "shared_tasks": shared, "runs": len(runs),
+                       "rel_err_vs_fp64": err}
+    line = {"metric": METRIC, "value": forms["auto"]["slices_per_s"], "unit": "slices/s",
+            "n_gpus": world, "steps": forms["auto"]["runs"], "warmup": args.warmup,
+            "ms_per_step": forms["auto"]["s_per_contract"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "the reference's m12 network (golden fixture of its data file)",
+            "config": {"workload": "m12 as jet_sliced_subset.cpp drives it: %d slices of the "
+                                   "9-index slicing in one TaskBasedContractor (shared tasks, "
+                                   "deletion and reduction tasks), contract() timed"
+                                   % n_slices},
+            "forms": forms,
+            "error_reference": "sum of the complex128 oracle amplitudes of the slices (golden), "
+                               "normalised by the sum of their magnitudes"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_m10(args, rank, world, local_rank):
     """The reference's m10 benchmark network (53 qubits, depth 10;
     examples/paper_benchmarks/data_files/m10.json, kept as a golden fixture)
@@ -1452,8 +1525,9 @@ def main():
     ap.add_argument("--config", default="1",
                     help="1 (default): the pairwise contraction; 0, 2, 4, 4q (qutrits): sliced "
                          "circuit amplitudes through the sliced executor; 3: gradients; m12: the "
-                         "reference's m12 network with its own slicing; m10: the reference's m10 "
-                         "network contracted whole")
+                         "reference's m12 network with its own slicing; m12-tbc: m12 through the "
+                         "TaskBasedContractor as the reference's driver does; m10: the reference's "
+                         "m10 network contracted whole")
     ap.add_argument("--permute-shape", default=None,
                     help="time one permute instead: dims as '3^16' or '9,5,7,3' (seeded random "
                          "permutation)")
@@ -1492,6 +1566,9 @@ def main():
         return
     if args.config == "m10":
         run_m10(args, rank, world, local_rank)
+        return
+    if args.config == "m12-tbc":
+        run_m12_tbc(args, rank, world, local_rank)
         return
     if args.config != "1":
         run_sliced(args, rank, world, local_rank)

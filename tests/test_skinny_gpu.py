@@ -292,3 +292,35 @@ def test_batched_matches_single(cuda, dtype, modes, gate_first):
 
 
 pytestmark = pytest.mark.gpu
+
+
+def test_more_than_2_to_32_rows(cuda):
+    """Row indices past 32 bits (the 64-bit row decode): a 2^32 + 96 row
+    tensor times a 1 x 1 matrix (k = 1, s = 1), 34 GB each way; sampled rows
+    against complex128 products."""
+    import torch
+
+    from jet_gb300 import capi
+
+    free, total = torch.cuda.mem_get_info()
+    m = (1 << 32) + 96
+    if free < 3 * m * 8:
+        pytest.skip("needs about 103 GB of free device memory")
+    a = torch.empty(m, dtype=torch.complex64, device=cuda)
+    chunk = 1 << 28
+    for lo in range(0, m, chunk):
+        idx = torch.arange(lo, min(lo + chunk, m), device=cuda, dtype=torch.int64)
+        a[lo:lo + idx.numel()].real.copy_(((idx % 1009) - 504).float() * 2.0 ** -10)
+        a[lo:lo + idx.numel()].imag.copy_(((idx % 997) - 498).float() * 2.0 ** -11)
+    del idx
+    b = torch.tensor([0.75 - 0.5j], dtype=torch.complex64, device=cuda)
+    assert capi.contract_workspace_size([m, 1], [0, 1], [1, 1], [0, 1], m, 1, 1,
+                                        capi.C64, capi.PREC_FP32) == 0
+    out = capi.contract(a, [m, 1], [0, 1], b, [1, 1], [0, 1], m, 1, 1)
+    torch.cuda.synchronize()
+    rows = torch.tensor([0, 1, 4095, (1 << 31) + 7, (1 << 32) - 1, 1 << 32, m - 1],
+                        device=cuda)
+    got = out[rows].cpu().numpy()
+    want = a[rows].cpu().numpy().astype(np.complex128) * complex(0.75, -0.5)
+    assert np.allclose(got, want, rtol=1e-6, atol=0), (got, want)
+    assert capi.take_device_status() == 0
