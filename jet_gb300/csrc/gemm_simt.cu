@@ -457,6 +457,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
     }
 }
 
+// Sums of the k ranges' partial results, accumulated in FP64: the partials
+// of a long product can be much larger than their sum (an amplitude is a sum
+// of terms of both signs), so FP32 adds here would cost accuracy the k ranges
+// kept.
 template <typename T>
 __global__ void reduce_partials(const typename C2<T>::type *__restrict__ part,
                                 typename C2<T>::type *__restrict__ out,
@@ -465,14 +469,60 @@ __global__ void reduce_partials(const typename C2<T>::type *__restrict__ part,
     using V = typename C2<T>::type;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
          i += (int64_t)gridDim.x * blockDim.x) {
-        T re = 0, im = 0;
+        double re = 0, im = 0;
         for (int64_t s = 0; s < S; ++s) {
             V v = part[s * len + i];
             re += v.x;
             im += v.y;
         }
-        out[i] = V{re, im};
+        out[i] = V{(T)re, (T)im};
     }
+}
+
+// reduce_partials for few outputs over many partial sums (S >= 64): one warp
+// per output, lane l adding partials l, l + 32, ... in order (FP64), then a
+// fixed shuffle tree -- a fixed order, where one thread per output walked the
+// S partials one dependent load at a time (93 us for 512 outputs of 456 k
+// ranges).
+template <typename T>
+__global__ void reduce_partials_warp(const typename C2<T>::type *__restrict__ part,
+                                     typename C2<T>::type *__restrict__ out, int64_t len,
+                                     int64_t S)
+{
+    using V = typename C2<T>::type;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < len;
+         i += warps) {
+        double re = 0, im = 0;
+#pragma unroll 4
+        for (int64_t s = lane; s < S; s += 32) {
+            const V v = part[s * len + i];
+            re += v.x;
+            im += v.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            re += __shfl_xor_sync(0xffffffffu, re, o);
+            im += __shfl_xor_sync(0xffffffffu, im, o);
+        }
+        if (lane == 0)
+            out[i] = V{(T)re, (T)im};
+    }
+}
+
+// Sums S partial results of `len` elements each into out (a fixed order).
+template <typename T>
+int ReducePartials(const typename C2<T>::type *part, typename C2<T>::type *out, int64_t len,
+                   int64_t S, cudaStream_t stream)
+{
+    if (S >= 64 && len <= 65536) {
+        reduce_partials_warp<T><<<GridFor((len * 32 + 255) / 256, 8), 256, 0, stream>>>(
+            part, out, len, S);
+        return CheckLaunch("reduce_partials_warp");
+    }
+    reduce_partials<T><<<GridFor((len + 255) / 256, 4), 256, 0, stream>>>(part, out, len, S);
+    return CheckLaunch("reduce_partials");
 }
 
 template <typename T>
@@ -632,9 +682,7 @@ int MultiplyVectorT(const typename C2<T>::type *A, const typename C2<T>::type *B
     int rc = CheckLaunch(N == 1 && M > 1 ? "gemv_rows_kernel" : "gemv_cols_kernel");
     if (rc || S == 1)
         return rc;
-    reduce_partials<T><<<GridFor((batch * len + 255) / 256, 4), 256, 0, stream>>>(
-        dst, C, batch * len, S);
-    return CheckLaunch("reduce_partials");
+    return ReducePartials<T>(dst, C, batch * len, S, stream);
 }
 
 // Matrix product of `batch` pairs (strides sa, sb; 0 = shared), split over k
@@ -667,9 +715,7 @@ int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename
         int rc = CheckLaunch("gemm_small_kernel");
         if (rc || S == 1)
             return rc;
-        reduce_partials<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(
-            dst, C, batch * M * N, S);
-        return CheckLaunch("reduce_partials");
+        return ReducePartials<T>(dst, C, batch * M * N, S, stream);
     }
     int64_t tn, tm;
     GemmGrid<T>(M, N, tn, tm);
@@ -691,9 +737,7 @@ int GemmT(const typename C2<T>::type *A, const typename C2<T>::type *B, typename
     int rc = CheckLaunch("gemm_kernel");
     if (rc || S == 1)
         return rc;
-    reduce_partials<T><<<GridFor((batch * M * N + 255) / 256, 4), 256, 0, stream>>>(
-        dst, C, batch * M * N, S);
-    return CheckLaunch("reduce_partials");
+    return ReducePartials<T>(dst, C, batch * M * N, S, stream);
 }
 
 template <typename T>
