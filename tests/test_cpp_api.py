@@ -17,6 +17,11 @@ tile_plan_test.cu (host only, runs on the CPU): the tiled permute's plan for
 non-power-of-2 dims replayed pass by pass against the plain permutation,
 with every slot and offset checked against its buffer.
 
+skinny_plan_test.cu (host only, runs on the CPU): the skinny contraction's
+launch parameters (row digits, tabulated offsets, batch offsets, C strides)
+replayed against the permuted operands' offsets for random shapes, axis
+orders and batch modes.
+
 pool_limit_test.cpp (GPU): device memory exhaustion injected through a capped
 library pool raises Jet::Exception from Tensor::ContractTensors,
 TaskBasedContractor and SlicedContractor, and each recovers once the cap is
@@ -58,6 +63,24 @@ def test_tile_permute_plan(tmp_path):
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr[-4000:]
     res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
+    assert res.stdout.startswith("ok ")
+
+
+def test_skinny_plan(tmp_path):
+    nvcc = shutil.which("nvcc") or os.path.join(
+        os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    pkg = os.path.join(REPO, "jet_gb300")
+    exe = str(tmp_path / "skinny_plan_test")
+    cmd = [nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I" + os.path.join(REPO, "include"), "-I" + os.path.join(pkg, "csrc"),
+           os.path.join(REPO, "tests", "cpp", "skinny_plan_test.cu"), "-L" + pkg, "-ljetgpu",
+           "-Xlinker", "-rpath", "-Xlinker", pkg, "-o", exe]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-4000:]
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
     assert res.stdout.startswith("ok ")
 
