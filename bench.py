@@ -1046,7 +1046,8 @@ def run_m12_tbc(args, rank, world, local_rank):
     its 9 indices, the first S slices (the reference's default: 3; here
     --sliced-batch) each added to one contractor, which shares their
     slice-independent tasks, then deletion and reduction tasks, and the
-    contractor's first contract() timed (eager), then its graph replay. The
+    contractor's first contract() timed (eager), then a replay of the graph
+    its second call captured. The
     reduction is checked against the sum of the fixture's complex128 oracle
     amplitudes of those slices."""
     import torch
@@ -1080,6 +1081,7 @@ def run_m12_tbc(args, rank, world, local_rank):
             tbc.contract()
             t1 = time.perf_counter()
             got = complex(tbc.reduction_result.data[0])
+            tbc.contract()  # the second call captures the graph
             t2 = time.perf_counter()
             tbc.contract()
             t3 = time.perf_counter()
