@@ -124,9 +124,12 @@ template <typename V> __device__ __forceinline__ void Mac(V &acc, const V &a, co
 // serves R rows). FP64 products are FMA-bound on this GPU: fewer.
 template <typename T, int S> struct SkRows {
     static constexpr int R = sizeof(T) == 8 ? (S <= 4 ? 2 : 1) : (S <= 4 ? 4 : 2);
-    // CTAs per SM the register allocation must leave room for: three for
-    // the HBM-bound complex64 widths (measured: at two, S = 8 lost 25 %).
-    static constexpr int kMinBlocks = (sizeof(T) == 4 && S <= 8) ? 3 : 1;
+    // CTAs per SM the register allocation must leave room for, for the
+    // HBM-bound complex64 widths: four up to S = 4 (2-qubit gates on 2^27
+    // elements 5.7 -> 6.1 TB/s), three for S = 8 (at four it spills and loses
+    // 7 %; at two it lost 25 %).
+    static constexpr int kMinBlocks =
+        sizeof(T) != 4 ? 1 : S <= 4 ? 4 : S <= 8 ? 3 : 1;
 };
 
 // One CTA per (row range, batch item); each thread R rows of the large
