@@ -211,6 +211,7 @@ template <class T> void BindContractor(py::module_ &m)
         .def("add_reduction_task", &tbc_t::AddReductionTask)
         .def("add_deletion_tasks", &tbc_t::AddDeletionTasks)
         .def("set_graph_replay", &tbc_t::SetGraphReplay, py::arg("on"))
+        .def("set_grouping", &tbc_t::SetGrouping, py::arg("on"))
         .def_property_readonly("has_replay_graph", &tbc_t::HasReplayGraph)
         .def("contract",
              [](tbc_t &t) {

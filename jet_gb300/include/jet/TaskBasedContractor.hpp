@@ -23,6 +23,8 @@
 // call and every later one launch the graph, with no per-task host work.
 #pragma once
 
+#include <algorithm>
+#include <array>
 #include <future>
 #include <map>
 #include <memory>
@@ -157,6 +159,13 @@ template <class TensorType> class TaskBasedContractor {
         replay_on_ = on;
         ResetReplay();
     }
+    // Grouped launches of independent tiny steps in the replayed graph
+    // (default on; off: one launch per step, as the eager run).
+    void SetGrouping(bool on)
+    {
+        grouping_ = on;
+        ResetReplay();
+    }
     // Whether the next Contract() launches a captured graph.
     bool HasReplayGraph() const noexcept { return replay_.graph != nullptr; }
 
@@ -190,11 +199,52 @@ template <class TensorType> class TaskBasedContractor {
         std::vector<int> leaf_of;                  // per buffer id: leaf slot or -1
         std::vector<std::pair<size_t, size_t>> stores; // (buffer id, result index)
         Gpu::DeviceBuffer arena, ws;
+        Gpu::DeviceBuffer groups; // task tables of the grouped tiny steps
         int precision = -1;
         void *graph = nullptr;
     };
     ReplayPlan replay_;
     bool replay_on_ = true;
+    bool grouping_ = true;
+    // Steps whose batch m n k is below this replay in grouped launches.
+    static constexpr double kGroupMaxWork = 131072.0;
+
+    // Number of leading axes of `perm` whose dimensions multiply to `extent`.
+    static size_t SplitCount(const std::vector<uint64_t> &shape, const std::vector<int32_t> &perm,
+                             uint64_t extent)
+    {
+        size_t j = 0;
+        uint64_t p = 1;
+        while (j < perm.size() && p < extent)
+            p *= shape[perm[j++]];
+        return j;
+    }
+
+    // Appends the element offsets of every index over axes perm[from..to)
+    // (row-major, the last fastest) of a row-major tensor; returns where
+    // they start.
+    static size_t AppendOffsets(std::vector<int64_t> &out, const std::vector<uint64_t> &shape,
+                                const std::vector<int32_t> &perm, size_t from, size_t to)
+    {
+        std::vector<int64_t> st(shape.size(), 1);
+        for (int i = (int)shape.size() - 2; i >= 0; --i)
+            st[i] = st[i + 1] * (int64_t)shape[i + 1];
+        uint64_t count = 1;
+        for (size_t j = from; j < to; ++j)
+            count *= shape[perm[j]];
+        const size_t at = out.size();
+        for (uint64_t idx = 0; idx < count; ++idx) {
+            uint64_t x = idx;
+            int64_t off = 0;
+            for (size_t j = to; j-- > from;) {
+                const int a = perm[j];
+                off += (int64_t)(x % shape[a]) * st[a];
+                x /= shape[a];
+            }
+            out.push_back(off);
+        }
+        return at;
+    }
     bool keep_leaves_ = false; // Run() hands released leaves to replay_
     size_t runs_ = 0;
 
@@ -352,13 +402,56 @@ template <class TensorType> class TaskBasedContractor {
                     }
                 }
             };
-            for (size_t i = 0; i < r.steps.size(); ++i) {
-                const auto &st = r.steps[i];
-                r.bytes[st.out] = std::max<size_t>(shape_of[st.out].GetSize(), 1) * sizeof(S);
-                r.offset[st.out] = alloc(r.bytes[st.out]);
-                for (size_t in : {st.a, st.b})
-                    if (r.leaf_of[in] < 0 && last[in] == (int)i)
-                        release(r.offset[in], r.bytes[in]);
+            // Items: one step, or a run of independent tiny steps replayed as
+            // one grouped launch (the launches, not the arithmetic, bound
+            // them). Tiny here: batch m n k below kGroupMaxWork and k <= 64,
+            // where the per-step path also adds the k products in order with
+            // FP32 (FP64) FMAs, so the grouped replay gives its bits.
+            std::vector<std::vector<size_t>> items;
+            {
+                const bool plain = r.precision == JETGPU_PREC_FP32 ||
+                                   r.precision == JETGPU_PREC_AUTO;
+                std::vector<size_t> group, group_outs;
+                auto flush = [&] {
+                    if (!group.empty())
+                        items.push_back(group);
+                    group.clear();
+                    group_outs.clear();
+                };
+                for (size_t i = 0; i < r.steps.size(); ++i) {
+                    const auto &st = r.steps[i];
+                    const auto &l = st.layout;
+                    const bool tiny = grouping_ && plain && l.k <= 64 &&
+                                      (double)l.m * (double)l.n * (double)l.k < kGroupMaxWork;
+                    if (!tiny) {
+                        flush();
+                        items.push_back({i});
+                        continue;
+                    }
+                    const bool reads_group =
+                        std::find(group_outs.begin(), group_outs.end(), st.a) != group_outs.end() ||
+                        std::find(group_outs.begin(), group_outs.end(), st.b) != group_outs.end();
+                    if (reads_group || group.size() >= 256)
+                        flush();
+                    group.push_back(i);
+                    group_outs.push_back(st.out);
+                }
+                flush();
+            }
+            // A group's outputs are all live while it runs: allocate them
+            // before releasing the inputs it consumes for the last time.
+            for (const auto &item : items) {
+                for (size_t i : item) {
+                    const auto &st = r.steps[i];
+                    r.bytes[st.out] = std::max<size_t>(shape_of[st.out].GetSize(), 1) * sizeof(S);
+                    r.offset[st.out] = alloc(r.bytes[st.out]);
+                }
+                for (size_t i : item) {
+                    const auto &st = r.steps[i];
+                    for (size_t in : {st.a, st.b})
+                        if (r.leaf_of[in] < 0 && last[in] == (int)i)
+                            release(r.offset[in], r.bytes[in]);
+                }
             }
             r.arena = Gpu::DeviceBuffer(std::max<size_t>(top, 256));
             r.ws = Gpu::DeviceBuffer(ws);
@@ -375,24 +468,98 @@ template <class TensorType> class TaskBasedContractor {
             std::vector<void *> result_ptr(r.stores.size());
             for (size_t i = 0; i < r.stores.size(); ++i)
                 result_ptr[i] = results_[r.stores[i].second].GetMutableDeviceData();
+            // Task tables of the grouped items: per task the element offsets
+            // of A's rows and columns and of B's, in the product's view
+            // (left ++ common of A, common ++ right of B), and one batch offset.
+            std::vector<int64_t> tables{0}; // entry 0: the batch offset
+            std::vector<std::array<size_t, 4>> table_at(r.steps.size());
+            size_t n_tasks = 0;
+            for (const auto &item : items) {
+                if (item.size() < 2)
+                    continue;
+                for (size_t i : item) {
+                    const auto &l = r.steps[i].layout;
+                    const size_t na = SplitCount(l.a_shape, l.a_perm, l.m);
+                    const size_t nb_ = SplitCount(l.b_shape, l.b_perm, l.k);
+                    table_at[i] = {AppendOffsets(tables, l.a_shape, l.a_perm, 0, na),
+                                   AppendOffsets(tables, l.a_shape, l.a_perm, na,
+                                                 l.a_perm.size()),
+                                   AppendOffsets(tables, l.b_shape, l.b_perm, 0, nb_),
+                                   AppendOffsets(tables, l.b_shape, l.b_perm, nb_,
+                                                 l.b_perm.size())};
+                    ++n_tasks;
+                }
+            }
+            const size_t tables_bytes = (tables.size() * sizeof(int64_t) + 255) / 256 * 256;
+            r.groups = Gpu::DeviceBuffer(n_tasks ? tables_bytes + n_tasks * sizeof(jetgpu_group_task)
+                                                 : 0);
+            std::vector<jetgpu_group_task> tasks;
+            std::vector<std::pair<size_t, uint64_t>> group_at(items.size()); // (first task, tiles)
+            if (n_tasks) {
+                const auto *tdev = static_cast<const int64_t *>(r.groups.get());
+                for (size_t it = 0; it < items.size(); ++it) {
+                    if (items[it].size() < 2)
+                        continue;
+                    group_at[it] = {tasks.size(), 0};
+                    for (size_t i : items[it]) {
+                        const auto &step = r.steps[i];
+                        const auto &l = step.layout;
+                        jetgpu_group_task q;
+                        q.A = ptr(step.a);
+                        q.B = ptr(step.b);
+                        q.C = ptr(step.out);
+                        q.batch = 1;
+                        q.m = l.m;
+                        q.n = l.n;
+                        q.k = l.k;
+                        q.a_bat = tdev;
+                        q.a_row = tdev + table_at[i][0];
+                        q.a_col = tdev + table_at[i][1];
+                        q.b_bat = tdev;
+                        q.b_row = tdev + table_at[i][2];
+                        q.b_col = tdev + table_at[i][3];
+                        tasks.push_back(q);
+                        group_at[it].second += jetgpu_group_tiles(1, l.m, l.n);
+                    }
+                }
+                Gpu::Check(jetgpu_memcpy(r.groups.get(), tables.data(),
+                                         tables.size() * sizeof(int64_t), 0, Gpu::Stream()),
+                           "group tables");
+                Gpu::Check(jetgpu_memcpy(static_cast<char *>(r.groups.get()) + tables_bytes,
+                                         tasks.data(), tasks.size() * sizeof(jetgpu_group_task),
+                                         0, Gpu::Stream()),
+                           "group tasks");
+            }
             Gpu::Synchronize();
+            const auto *task_dev = reinterpret_cast<const jetgpu_group_task *>(
+                static_cast<const char *>(r.groups.get()) + tables_bytes);
             void *st = Gpu::Stream();
             Gpu::Check(jetgpu_graph_begin(st), "capture begin");
-            size_t next_store = 0;
-            for (const auto &step : r.steps) {
-                const auto &l = step.layout;
-                Gpu::Check(jetgpu_contract(ptr(step.a), (int)l.a_shape.size(), l.a_shape.data(),
-                                           l.a_perm.data(), ptr(step.b), (int)l.b_shape.size(),
-                                           l.b_shape.data(), l.b_perm.data(), ptr(step.out), l.m,
-                                           l.n, l.k, dt, r.precision, JETGPU_ALGO_4M, 0, 0,
-                                           r.ws.get(), r.ws.size(), st),
-                           "ContractTensors (capture)");
-                while (next_store < r.stores.size() && r.stores[next_store].first == step.out) {
-                    Gpu::Check(jetgpu_memcpy(result_ptr[next_store], ptr(step.out),
-                                             r.bytes[step.out], 2, st),
-                               "result copy (capture)");
-                    ++next_store;
+            for (size_t it = 0; it < items.size(); ++it) {
+                const auto &item = items[it];
+                if (item.size() >= 2) {
+                    Gpu::Check(jetgpu_contract_group(task_dev + group_at[it].first,
+                                                     (int)item.size(), group_at[it].second, dt,
+                                                     st),
+                               "grouped tiny steps (capture)");
                 }
+                else {
+                    const auto &step = r.steps[item[0]];
+                    const auto &l = step.layout;
+                    Gpu::Check(jetgpu_contract(ptr(step.a), (int)l.a_shape.size(),
+                                               l.a_shape.data(), l.a_perm.data(), ptr(step.b),
+                                               (int)l.b_shape.size(), l.b_shape.data(),
+                                               l.b_perm.data(), ptr(step.out), l.m, l.n, l.k, dt,
+                                               r.precision, JETGPU_ALGO_4M, 0, 0, r.ws.get(),
+                                               r.ws.size(), st),
+                               "ContractTensors (capture)");
+                }
+                for (size_t i : item)
+                    for (size_t q = 0; q < r.stores.size(); ++q)
+                        if (r.stores[q].first == r.steps[i].out)
+                            Gpu::Check(jetgpu_memcpy(result_ptr[q], ptr(r.steps[i].out),
+                                                     r.bytes[r.steps[i].out], 2, st),
+                                       "result copy (capture)");
             }
             Gpu::Check(jetgpu_graph_end(st, &r.graph), "capture end");
         }

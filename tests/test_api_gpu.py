@@ -218,7 +218,8 @@ def test_repeated_contract_replays_a_graph(jet, precision):
     first runs eagerly, the second captures the contractions into one CUDA
     graph and every later call replays it. Every call's results (two networks
     sharing tasks, their FP64 reduction) equal those of a contractor that
-    runs eagerly, bit for bit."""
+    runs eagerly, bit for bit, with the replay's independent tiny steps in
+    grouped launches (the default) and without."""
     from jet_gb300 import circuits
 
     net = circuits.random_circuit_network(3, 4, 6, seed=31)
@@ -227,9 +228,10 @@ def test_repeated_contract_replays_a_graph(jet, precision):
     old = jet.get_precision()
     jet.set_precision(precision)
     try:
-        def build(replay):
+        def build(replay, grouping=True):
             tbc = jet.TaskBasedContractor(dtype="complex64")
             tbc.set_graph_replay(replay)
+            tbc.set_grouping(grouping)
             for v in range(2):
                 tn = jet.TensorNetwork(dtype="complex64")
                 for lab, sh, d in net.tensors:
@@ -244,11 +246,12 @@ def test_repeated_contract_replays_a_graph(jet, precision):
         eager = build(False)
         eager.contract()
         want = [complex(r.data[0]) for r in eager.results] + [eager.reduction_result.data[0]]
-        tbc = build(True)
-        for call in range(4):
-            tbc.contract()
-            got = [complex(r.data[0]) for r in tbc.results] + [tbc.reduction_result.data[0]]
-            assert got == want, call
-            assert tbc.has_replay_graph == (call >= 1)
+        for grouping in (True, False):
+            tbc = build(True, grouping)
+            for call in range(4):
+                tbc.contract()
+                got = [complex(r.data[0]) for r in tbc.results] + [tbc.reduction_result.data[0]]
+                assert got == want, (grouping, call)
+                assert tbc.has_replay_graph == (call >= 1)
     finally:
         jet.set_precision(old)
