@@ -42,6 +42,113 @@
 
 namespace Jet {
 
+// The replay plan's scheduling, kept apart from the contractor so that it
+// can be checked without a GPU (tests/cpp/replay_plan_test.cpp).
+namespace replay_detail {
+
+// One contraction step: operand and output buffer ids, product shape.
+struct StepShape {
+    size_t a, b, out;
+    uint64_t m, n, k;
+};
+
+// Launch items in step order: one step, or (when `enabled`) a run of tiny
+// steps -- m n k below `max_work` and k <= 64 -- that read none of the run's
+// own outputs, at most 256 per run (a grouped launch's task limit).
+inline std::vector<std::vector<size_t>> GroupTinySteps(const std::vector<StepShape> &steps,
+                                                       bool enabled, double max_work)
+{
+    std::vector<std::vector<size_t>> items;
+    std::vector<size_t> group, group_outs;
+    auto flush = [&] {
+        if (!group.empty())
+            items.push_back(group);
+        group.clear();
+        group_outs.clear();
+    };
+    for (size_t i = 0; i < steps.size(); ++i) {
+        const StepShape &st = steps[i];
+        const bool tiny = enabled && st.k <= 64 &&
+                          (double)st.m * (double)st.n * (double)st.k < max_work;
+        if (!tiny) {
+            flush();
+            items.push_back({i});
+            continue;
+        }
+        const bool reads_group =
+            std::find(group_outs.begin(), group_outs.end(), st.a) != group_outs.end() ||
+            std::find(group_outs.begin(), group_outs.end(), st.b) != group_outs.end();
+        if (reads_group || group.size() >= 256)
+            flush();
+        group.push_back(i);
+        group_outs.push_back(st.out);
+    }
+    flush();
+    return items;
+}
+
+// First-fit arena offsets (256-byte aligned) of every step output, over its
+// lifetime: from its item to the item of its last consumer (never, for an
+// output no step reads). An item's outputs are all allocated before any input
+// it consumes for the last time is released: a grouped launch runs its steps
+// together. Leaves (leaf_of >= 0) live outside the arena. Returns the arena's
+// size; offset[b] is set for every step output b.
+inline size_t PlanArena(const std::vector<StepShape> &steps,
+                        const std::vector<std::vector<size_t>> &items,
+                        const std::vector<int> &leaf_of, const std::vector<size_t> &bytes,
+                        std::vector<size_t> &offset)
+{
+    const size_t nb = leaf_of.size();
+    std::vector<int> last(nb, -1);
+    for (size_t i = 0; i < steps.size(); ++i) {
+        last[steps[i].a] = (int)i;
+        last[steps[i].b] = (int)i;
+    }
+    offset.assign(nb, 0);
+    std::map<size_t, size_t> free_blocks;
+    size_t top = 0;
+    auto alloc = [&](size_t n) {
+        n = (n + 255) / 256 * 256;
+        for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it)
+            if (it->second >= n) {
+                const size_t off = it->first, rem = it->second - n;
+                free_blocks.erase(it);
+                if (rem)
+                    free_blocks[off + n] = rem;
+                return off;
+            }
+        top += n;
+        return top - n;
+    };
+    auto release = [&](size_t off, size_t n) {
+        n = (n + 255) / 256 * 256;
+        auto it = free_blocks.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_blocks.erase(nx);
+        }
+        if (it != free_blocks.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_blocks.erase(it);
+            }
+        }
+    };
+    for (const auto &item : items) {
+        for (size_t i : item)
+            offset[steps[i].out] = alloc(bytes[steps[i].out]);
+        for (size_t i : item)
+            for (size_t in : {steps[i].a, steps[i].b})
+                if (leaf_of[in] < 0 && last[in] == (int)i)
+                    release(offset[in], bytes[in]);
+    }
+    return top;
+}
+
+} // namespace replay_detail
+
 template <class TensorType> class TaskBasedContractor {
   public:
     struct Task {
@@ -360,99 +467,24 @@ template <class TensorType> class TaskBasedContractor {
                     r.stores.emplace_back(id.at(t.name), t.result_id);
                 }
             }
-            // Arena: first fit over each intermediate's lifetime (from its
-            // step to its last consumer; stored results are copied out by
-            // the task right after their step).
+            // Launch items (single steps, or runs of independent tiny steps
+            // replayed as one grouped launch) and the arena offsets of the
+            // intermediates over their lifetimes (replay_detail below).
             const size_t nb = shape_of.size();
-            std::vector<int> last(nb, -1);
+            std::vector<replay_detail::StepShape> shapes(r.steps.size());
             for (size_t i = 0; i < r.steps.size(); ++i) {
-                last[r.steps[i].a] = (int)i;
-                last[r.steps[i].b] = (int)i;
+                const auto &st = r.steps[i];
+                shapes[i] = {st.a, st.b, st.out, st.layout.m, st.layout.n, st.layout.k};
             }
-            r.offset.assign(nb, 0);
+            const bool plain =
+                r.precision == JETGPU_PREC_FP32 || r.precision == JETGPU_PREC_AUTO;
+            const std::vector<std::vector<size_t>> items =
+                replay_detail::GroupTinySteps(shapes, grouping_ && plain, kGroupMaxWork);
             r.bytes.assign(nb, 0);
-            std::map<size_t, size_t> free_blocks;
-            size_t top = 0;
-            auto alloc = [&](size_t bytes) {
-                bytes = (bytes + 255) / 256 * 256;
-                for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it)
-                    if (it->second >= bytes) {
-                        const size_t off = it->first, rem = it->second - bytes;
-                        free_blocks.erase(it);
-                        if (rem)
-                            free_blocks[off + bytes] = rem;
-                        return off;
-                    }
-                top += bytes;
-                return top - bytes;
-            };
-            auto release = [&](size_t off, size_t bytes) {
-                bytes = (bytes + 255) / 256 * 256;
-                auto it = free_blocks.emplace(off, bytes).first;
-                auto nx = std::next(it);
-                if (nx != free_blocks.end() && it->first + it->second == nx->first) {
-                    it->second += nx->second;
-                    free_blocks.erase(nx);
-                }
-                if (it != free_blocks.begin()) {
-                    auto pv = std::prev(it);
-                    if (pv->first + pv->second == it->first) {
-                        pv->second += it->second;
-                        free_blocks.erase(it);
-                    }
-                }
-            };
-            // Items: one step, or a run of independent tiny steps replayed as
-            // one grouped launch (the launches, not the arithmetic, bound
-            // them). Tiny here: batch m n k below kGroupMaxWork and k <= 64,
-            // where the per-step path also adds the k products in order with
-            // FP32 (FP64) FMAs, so the grouped replay gives its bits.
-            std::vector<std::vector<size_t>> items;
-            {
-                const bool plain = r.precision == JETGPU_PREC_FP32 ||
-                                   r.precision == JETGPU_PREC_AUTO;
-                std::vector<size_t> group, group_outs;
-                auto flush = [&] {
-                    if (!group.empty())
-                        items.push_back(group);
-                    group.clear();
-                    group_outs.clear();
-                };
-                for (size_t i = 0; i < r.steps.size(); ++i) {
-                    const auto &st = r.steps[i];
-                    const auto &l = st.layout;
-                    const bool tiny = grouping_ && plain && l.k <= 64 &&
-                                      (double)l.m * (double)l.n * (double)l.k < kGroupMaxWork;
-                    if (!tiny) {
-                        flush();
-                        items.push_back({i});
-                        continue;
-                    }
-                    const bool reads_group =
-                        std::find(group_outs.begin(), group_outs.end(), st.a) != group_outs.end() ||
-                        std::find(group_outs.begin(), group_outs.end(), st.b) != group_outs.end();
-                    if (reads_group || group.size() >= 256)
-                        flush();
-                    group.push_back(i);
-                    group_outs.push_back(st.out);
-                }
-                flush();
-            }
-            // A group's outputs are all live while it runs: allocate them
-            // before releasing the inputs it consumes for the last time.
-            for (const auto &item : items) {
-                for (size_t i : item) {
-                    const auto &st = r.steps[i];
-                    r.bytes[st.out] = std::max<size_t>(shape_of[st.out].GetSize(), 1) * sizeof(S);
-                    r.offset[st.out] = alloc(r.bytes[st.out]);
-                }
-                for (size_t i : item) {
-                    const auto &st = r.steps[i];
-                    for (size_t in : {st.a, st.b})
-                        if (r.leaf_of[in] < 0 && last[in] == (int)i)
-                            release(r.offset[in], r.bytes[in]);
-                }
-            }
+            for (const auto &st : r.steps)
+                r.bytes[st.out] = std::max<size_t>(shape_of[st.out].GetSize(), 1) * sizeof(S);
+            const size_t top =
+                replay_detail::PlanArena(shapes, items, r.leaf_of, r.bytes, r.offset);
             r.arena = Gpu::DeviceBuffer(std::max<size_t>(top, 256));
             r.ws = Gpu::DeviceBuffer(ws);
             auto ptr = [&](size_t b) -> void * {

@@ -17,6 +17,11 @@ tile_plan_test.cu (host only, runs on the CPU): the tiled permute's plan for
 non-power-of-2 dims replayed pass by pass against the plain permutation,
 with every slot and offset checked against its buffer.
 
+replay_plan_test.cpp (host only, runs on the CPU): the TaskBasedContractor
+replay's grouping of tiny steps and its arena plan on random contraction
+DAGs: runs hold only independent tiny steps, and no two buffers live at the
+same time overlap.
+
 skinny_plan_test.cu (host only, runs on the CPU): the skinny contraction's
 launch parameters (row digits, tabulated offsets, batch offsets, C strides)
 replayed against the permuted operands' offsets for random shapes, axis
@@ -81,6 +86,14 @@ def test_skinny_plan(tmp_path):
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr[-4000:]
     res = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
+    assert res.stdout.startswith("ok ")
+
+
+def test_replay_plan(tmp_path):
+    exe = str(tmp_path / "replay_plan_test")
+    _compile(exe, "replay_plan_test.cpp")
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
     assert res.stdout.startswith("ok ")
 
