@@ -24,6 +24,7 @@
 
 #include <cstring>
 #include <type_traits>
+#include <utility>
 
 namespace jetgpu {
 namespace {
@@ -158,6 +159,11 @@ __global__ void __launch_bounds__(kSkThreads, SkRows<T, S>::kMinBlocks)
     constexpr bool kStage = std::is_same<T, float>::value && BigIsA && S == 9;
     __shared__ __align__(16) V tab[kSkMaxK][S];
     __shared__ V stage[kStage ? kSkThreads / 32 : 1][kStage ? 32 * (S + 1) : 1];
+    // Launched with programmatic stream serialisation (LaunchPdl): every
+    // memory access follows this wait for the previous kernel of the stream,
+    // and the next kernel may start launching once every CTA is past it.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint32_t b = blockIdx.y;
     big += SmallOffset(p.big_b, b);
     small += SmallOffset(p.small_b, b);
@@ -474,6 +480,24 @@ bool Plan(uint64_t batch, int a_rank, const uint64_t *a_shape, const int32_t *a_
     return true;
 }
 
+// Launches `kernel` with programmatic stream serialisation: the launch may
+// begin while the previous kernel of the stream finishes, which a chain of
+// small steps is bound by (the kernels wait for it before touching memory).
+template <typename... P, typename... A>
+cudaError_t LaunchPdl(void (*kernel)(P...), dim3 grid, cudaStream_t st, A &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kSkThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
 // CTAs of skinny_kernel<T, S, BigIsA> that fit on an SM at once (cached).
 template <typename T, int S, bool BigIsA> int Resident()
 {
@@ -504,9 +528,9 @@ int LaunchS(const void *big, const void *small, void *C, SkinnyParams &p, uint64
     const uint64_t per_item = slots / batch > 0 ? slots / batch : 1;
     if (gx > per_item)
         gx = per_item;
-    kernel<<<dim3((unsigned)gx, (unsigned)batch), kSkThreads, 0, st>>>(
-        static_cast<const V *>(big), static_cast<const V *>(small), static_cast<V *>(C), p,
-        scale);
+    JETGPU_CUDA_TRY(LaunchPdl(kernel, dim3((unsigned)gx, (unsigned)batch), st,
+                              static_cast<const V *>(big), static_cast<const V *>(small),
+                              static_cast<V *>(C), p, scale));
     return CheckLaunch("skinny_kernel");
 }
 
@@ -518,22 +542,9 @@ int LaunchT(const void *big, const void *small, void *C, SkinnyParams &p, uint64
     if (p.rows * (uint64_t)p.s <= (uint64_t)kSkTiny) {
         using V = typename C2<T>::type;
         const unsigned gx = (unsigned)((p.rows * p.s + kSkThreads - 1) / kSkThreads);
-        // A chain of tiny steps is bound by launch latency: let each launch
-        // overlap the end of the kernel before it (the kernel waits for it
-        // before touching memory).
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(gx, (unsigned)batch);
-        cfg.blockDim = dim3(kSkThreads);
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        JETGPU_CUDA_TRY(cudaLaunchKernelEx(&cfg, skinny_tiny_kernel<T, BigIsA>,
-                                           static_cast<const V *>(big),
-                                           static_cast<const V *>(small), static_cast<V *>(C), p,
-                                           scale));
+        JETGPU_CUDA_TRY(LaunchPdl(skinny_tiny_kernel<T, BigIsA>, dim3(gx, (unsigned)batch), st,
+                                  static_cast<const V *>(big), static_cast<const V *>(small),
+                                  static_cast<V *>(C), p, scale));
         return CheckLaunch("skinny_tiny_kernel");
     }
     switch (p.s) {

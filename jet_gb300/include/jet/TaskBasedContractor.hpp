@@ -191,6 +191,27 @@ template <class TensorType> class TaskBasedContractor {
         const size_t result_id = results_.size();
         results_.resize(result_id + 1);
         size_t shared = 0;
+        // The contractor's own copy of each leaf, taken once per name. On the
+        // GPU it is made device resident here, as the reference's CudaTensor
+        // leaves are when the tasks are added, so that Contract() runs only
+        // the contraction; the uploads end before this call returns. A copy
+        // that cannot be uploaded now (device memory exhausted) stays on the
+        // host and is uploaded at its first use, whose failure Contract()
+        // reports.
+        bool uploaded = false;
+        auto take_leaf = [&](const std::string &name, size_t id) {
+            if (name_to_tensor_.count(name))
+                return;
+            auto copy = std::make_unique<TensorType>(nodes[id].tensor);
+            if constexpr (kGpuTensor) {
+                try {
+                    copy->GetDeviceData();
+                    uploaded = true;
+                } catch (const Exception &) {
+                }
+            }
+            name_to_tensor_.emplace(name, std::move(copy));
+        };
         for (size_t i = 0; i < path.size(); ++i) {
             const auto [id_1, id_2] = path[i];
             const std::string name_1 = TaskName(steps[id_1]);
@@ -202,11 +223,9 @@ template <class TensorType> class TaskBasedContractor {
             name_to_parents_[name_1].insert(name_3);
             name_to_parents_[name_2].insert(name_3);
             if (id_1 < num_leaves)
-                name_to_tensor_.try_emplace(name_1,
-                                            std::make_unique<TensorType>(nodes[id_1].tensor));
+                take_leaf(name_1, id_1);
             if (id_2 < num_leaves)
-                name_to_tensor_.try_emplace(name_2,
-                                            std::make_unique<TensorType>(nodes[id_2].tensor));
+                take_leaf(name_2, id_2);
             name_to_tensor_.try_emplace(name_3, nullptr);
             if (name_to_task_.count(name_3)) {
                 ++shared;
@@ -218,6 +237,14 @@ template <class TensorType> class TaskBasedContractor {
             tasks_.push_back(Task{Task::CONTRACT, name_3, name_1, name_2, 0});
             if (last)
                 tasks_.push_back(Task{Task::STORE, name_3, "", "", result_id});
+        }
+        if constexpr (kGpuTensor) {
+            if (uploaded) {
+                try {
+                    Gpu::Synchronize();
+                } catch (const Exception &) { // reported by the next device call
+                }
+            }
         }
         return shared;
     }

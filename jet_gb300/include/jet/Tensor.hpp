@@ -208,26 +208,42 @@ template <class T = std::complex<float>> class Tensor {
         return *this;
     }
 
+    // The label -> dimension map is built from the labels and shape when it
+    // is first read (GetIndexToDimension, RenameIndex, ==), by the same rule
+    // as the reference's constructor: a contraction step creates a tensor
+    // whose map nothing reads, and building it was a third of the step's
+    // host time.
     void InitIndicesAndShape(const std::vector<std::string> &indices,
                              const std::vector<size_t> &shape) noexcept
     {
         indices_ = indices;
         shape_ = shape;
         index_to_dimension_.clear();
-        for (size_t i = 0; i < shape_.size(); ++i)
-            index_to_dimension_[indices[i]] = shape[i];
+        dims_built_ = false;
     }
 
-    void SetShape(const std::vector<size_t> &shape) noexcept { shape_ = shape; }
+    // As the reference's SetShape, the map keeps the dimensions it had.
+    void SetShape(const std::vector<size_t> &shape) noexcept
+    {
+        GetIndexToDimension();
+        shape_ = shape;
+    }
     const std::vector<size_t> &GetShape() const noexcept { return shape_; }
     const std::vector<std::string> &GetIndices() const noexcept { return indices_; }
     const std::unordered_map<std::string, size_t> &GetIndexToDimension() const
     {
+        std::lock_guard<std::mutex> lock(sync_);
+        if (!dims_built_) {
+            for (size_t i = 0; i < shape_.size(); ++i)
+                index_to_dimension_[indices_[i]] = shape_[i];
+            dims_built_ = true;
+        }
         return index_to_dimension_;
     }
 
     void RenameIndex(size_t pos, std::string new_label) noexcept
     {
+        GetIndexToDimension();
         const auto old = indices_[pos];
         const size_t dim = index_to_dimension_[old];
         index_to_dimension_.erase(old);
@@ -241,7 +257,7 @@ template <class T = std::complex<float>> class Tensor {
     bool operator==(const Tensor &other) const
     {
         return shape_ == other.shape_ && indices_ == other.indices_ &&
-               index_to_dimension_ == other.index_to_dimension_ &&
+               GetIndexToDimension() == other.GetIndexToDimension() &&
                HostView() == other.HostView();
     }
     bool operator!=(const Tensor &other) const { return !(*this == other); }
@@ -554,7 +570,8 @@ template <class T = std::complex<float>> class Tensor {
   private:
     std::vector<std::string> indices_;
     std::vector<size_t> shape_;
-    std::unordered_map<std::string, size_t> index_to_dimension_;
+    mutable std::unordered_map<std::string, size_t> index_to_dimension_;
+    mutable bool dims_built_ = false;
     size_t size_ = 1;
     // Host mirror and device copy; an invalid pair means "all zeros".
     mutable std::vector<T> host_;
@@ -655,6 +672,9 @@ template <class T = std::complex<float>> class Tensor {
         indices_ = std::move(other.indices_);
         shape_ = std::move(other.shape_);
         index_to_dimension_ = std::move(other.index_to_dimension_);
+        dims_built_ = other.dims_built_;
+        other.index_to_dimension_.clear();
+        other.dims_built_ = false;
         size_ = other.size_;
         host_ = std::move(other.host_);
         host_valid_ = other.host_valid_;

@@ -27,6 +27,9 @@ launch parameters (row digits, tabulated offsets, batch offsets, C strides)
 replayed against the permuted operands' offsets for random shapes, axis
 orders and batch modes.
 
+tensor_labels_test.cpp (host only, runs on the CPU): Jet::Tensor's label ->
+dimension map, built when first read, against the reference's eager rules
+through construction, renames, SetShape, copies, moves and equality.
 pool_limit_test.cpp (GPU): device memory exhaustion injected through a capped
 library pool raises Jet::Exception from Tensor::ContractTensors,
 TaskBasedContractor and SlicedContractor, and each recovers once the cap is
@@ -96,6 +99,14 @@ def test_replay_plan(tmp_path):
     res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
     assert res.stdout.startswith("ok ")
+
+
+def test_tensor_label_map(tmp_path):
+    exe = str(tmp_path / "tensor_labels_test")
+    _compile(exe, "tensor_labels_test.cpp")
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
+    assert res.stdout.startswith("ok")
 
 
 def test_cuda_tensor_header_compiles(tmp_path):
