@@ -109,14 +109,21 @@ def build_leaves(leaves: Sequence[Leaf], thetas, phis, dtype=None, device=None,
                  const_cache=None):
     """torch leaves as differentiable functions of the angle tensors.
 
-    const_cache (a dict, optional) keeps the angle-independent leaves on the
-    device between calls, so a call makes no host-to-device copy (required
-    inside a CUDA graph capture)."""
+    The gates of one kind (RX, RZ) are built together: one gather of their
+    angles, one cos and one sin, one complex tensor of all their matrices and
+    one of its conjugates; each leaf is a row of those (torch.unbind, whose
+    backward is one stack). Built one by one, the gates of the 6 x 6, 10-layer
+    network took about 9,000 torch operations forward and as many backward.
+
+    const_cache (a dict, optional) keeps the angle-independent leaves and the
+    gathers' index tensors on the device between calls, so a call makes no
+    host-to-device copy (required inside a CUDA graph capture)."""
     import torch
 
     dtype = dtype or torch.complex64
     real = torch.float32 if dtype == torch.complex64 else torch.float64
-    out = []
+    out = [None] * len(leaves)
+    rows = {"rx": {}, "rz": {}}  # (layer, qubit) -> row of that kind's gates
     for i, lf in enumerate(leaves):
         if lf.kind == "const":
             key = (i, str(dtype), str(device))
@@ -125,22 +132,44 @@ def build_leaves(leaves: Sequence[Leaf], thetas, phis, dtype=None, device=None,
                 t = torch.as_tensor(lf.data, dtype=dtype, device=device).reshape(lf.shape)
                 if const_cache is not None:
                     const_cache[key] = t
+            out[i] = t
         else:
-            ang = (thetas if lf.kind == "rx" else phis)[lf.layer, lf.qubit].to(real)
-            c, s = torch.cos(ang / 2), torch.sin(ang / 2)
-            z = torch.zeros_like(c)
-            if lf.kind == "rx":
-                re = torch.stack([c, z, z, c])
-                im = torch.stack([z, -s, -s, z])
-            else:
-                re = torch.stack([c, z, z, c])
-                im = torch.stack([-s, z, z, s])
-            t = torch.complex(re, im).to(dtype).reshape(2, 2)
-            if device is not None:
-                t = t.to(device)
+            rows[lf.kind].setdefault((lf.layer, lf.qubit), len(rows[lf.kind]))
+    for kind, at in rows.items():
+        if not at:
+            continue
+        src = thetas if kind == "rx" else phis
+        key = ("index", kind, tuple(at), str(src.device))
+        idx = None if const_cache is None else const_cache.get(key)
+        if idx is None:
+            lq = torch.as_tensor(list(at.keys()), dtype=torch.long, device=src.device)
+            idx = (lq[:, 0].contiguous(), lq[:, 1].contiguous())
+            if const_cache is not None:
+                const_cache[key] = idx
+        ang = src[idx].to(real)
+        c, s = torch.cos(ang / 2), torch.sin(ang / 2)
+        z = torch.zeros_like(c)
+        re = torch.stack([c, z, z, c], dim=1)
+        if kind == "rx":  # [[c, -i s], [-i s, c]]
+            ns = -s
+            im = torch.stack([z, ns, ns, z], dim=1)
+        else:  # diag(e^{-i phi/2}, e^{i phi/2})
+            im = torch.stack([-s, z, z, s], dim=1)
+        g = torch.complex(re, im).to(dtype).reshape(-1, 2, 2)
+        if device is not None:
+            g = g.to(device)
+        kets = torch.unbind(g)
+        bras = None
+        for i, lf in enumerate(leaves):
+            if lf.kind != kind:
+                continue
+            r = at[(lf.layer, lf.qubit)]
             if lf.conj:
-                t = torch.conj(t).resolve_conj()
-        out.append(t)
+                if bras is None:
+                    bras = torch.unbind(torch.conj(g).resolve_conj())
+                out[i] = bras[r]
+            else:
+                out[i] = kets[r]
     return out
 
 
