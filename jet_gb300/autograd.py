@@ -14,9 +14,18 @@ contractions, replayed along the path in reverse:
     grad_B[common, right] = sum_left conj(A[left, common]) grad_C[left, right]
 
 (PyTorch's convention for complex gradients: grad = dL/d(conj z)), each
-followed by a transpose back to the operand's own label order. The forward
-keeps only the leaves: backward recomputes the intermediates (checkpointing),
-so memory stays at one forward's worth plus the gradients. Every contraction,
+followed by a transpose back to the operand's own label order. The reverse
+sweep carries the conjugated gradients H = conj(grad) instead:
+
+    H_A[left, common] = sum_right H_C[left, right] B[common, right]
+    H_B[common, right] = sum_left A[left, common] H_C[left, right]
+
+are plain contractions of the forward values (term by term the conjugates
+of the products above), and only the leaves' gradients are conjugated at the
+end, instead of every operand of every step. Operands whose subtree
+holds no leaf that needs a gradient get none. The forward keeps only the
+leaves: backward recomputes the intermediates (checkpointing), so memory
+stays at one forward's worth plus the gradients. Every contraction,
 conjugation and transpose runs in libjetgpu.so (jetgpu_contract,
 jetgpu_conj, jetgpu_permute).
 
@@ -96,8 +105,8 @@ class ContractionPlan:
         return self.shapes[-1]
 
 
-def _contract(a, a_labels, a_shape, b, b_labels, b_shape, precision):
-    """ContractTensors on device tensors; returns (C, C labels)."""
+def _contract(a, a_labels, a_shape, b, b_labels, b_shape, precision, out=None):
+    """ContractTensors on device tensors; returns (C, C labels, C shape)."""
     sb, sa = set(b_labels), set(a_labels)
     left = [x for x in a_labels if x not in sb]
     right = [x for x in b_labels if x not in sa]
@@ -113,14 +122,32 @@ def _contract(a, a_labels, a_shape, b, b_labels, b_shape, precision):
         k *= dims[x]
     out = capi.contract(a, list(a_shape), [a_labels.index(x) for x in left + common], b,
                         list(b_shape), [b_labels.index(x) for x in common + right], m, n, k,
-                        precision=precision)
+                        precision=precision, out=out)
     return out[: m * n], left + right, [dims[x] for x in left + right]
 
 
-def _to_order(x, labels, shape, target):
+def _out_labels(a_labels, b_labels):
+    sa, sb = set(a_labels), set(b_labels)
+    return [x for x in a_labels if x not in sb] + [x for x in b_labels if x not in sa]
+
+
+def _to_order(x, labels, shape, target, out=None):
     if labels == target:
         return x
-    return capi.permute(x, list(shape), [labels.index(t) for t in target])
+    return capi.permute(x, list(shape), [labels.index(t) for t in target], out=out)
+
+
+def _operand_h(x, x_labels, x_shape, y, y_labels, y_shape, target, precision, slot):
+    """The contraction of x and y in `target`'s label order, written into
+    `slot` (a leaf's place in one flat buffer) when given. Of contract(x, y)
+    and contract(y, x), one whose labels come out in that order needs no
+    transpose."""
+    for p, lp, sp, q, lq, sq in ((x, x_labels, x_shape, y, y_labels, y_shape),
+                                 (y, y_labels, y_shape, x, x_labels, x_shape)):
+        if _out_labels(lp, lq) == target:
+            return _contract(p, lp, sp, q, lq, sq, precision, out=slot)[0]
+    h, lh, sh = _contract(x, x_labels, x_shape, y, y_labels, y_shape, precision)
+    return _to_order(h, lh, sh, target, out=slot)
 
 
 def _forward(plan: ContractionPlan, leaves, precision: int, keep: bool):
@@ -138,28 +165,70 @@ def _forward(plan: ContractionPlan, leaves, precision: int, keep: bool):
     return vals
 
 
-def _backward(plan: ContractionPlan, vals, grad_out, precision: int):
-    grads = [None] * len(vals)
-    grads[-1] = grad_out
+def _needs(plan: ContractionPlan, leaf_needs) -> List[bool]:
+    """Per node of the path: whether a leaf of its subtree needs a gradient."""
+    need = [bool(x) for x in leaf_needs]
+    for st in plan.steps:
+        need.append(need[st.a] or need[st.b])
+    return need
+
+
+def _backward_conj(plan: ContractionPlan, vals, h_out, precision: int, need, slots=None):
+    """The reverse sweep over conjugated gradients: H of every leaf (None
+    where no gradient is needed), from H of the result. `slots` (optional):
+    per leaf, the place to write its H (one contribution per leaf: the path
+    consumes each node once)."""
+    slots = slots or {}
+    hs = [None] * len(vals)
+    hs[-1] = h_out
     for idx in range(len(plan.steps) - 1, -1, -1):
         st = plan.steps[idx]
         c_id = plan.num_leaves + idx
-        gc = grads[c_id]
-        if gc is None:
+        hc = hs[c_id]
+        if hc is None:
             continue
         la, lb, lc = plan.labels[st.a], plan.labels[st.b], plan.labels[c_id]
         sa, sb, sc = plan.shapes[st.a], plan.shapes[st.b], plan.shapes[c_id]
-        # grad_A = contract(grad_C, conj(B)) -> transpose to A's labels.
-        ga, lga, sga = _contract(gc, lc, sc, capi.conj(vals[st.b]), lb, sb, precision)
-        ga = _to_order(ga, lga, sga, la)
-        # grad_B = contract(conj(A), grad_C) -> transpose to B's labels.
-        gb, lgb, sgb = _contract(capi.conj(vals[st.a]), la, sa, gc, lc, sc, precision)
-        gb = _to_order(gb, lgb, sgb, lb)
-        grads[st.a] = ga if grads[st.a] is None else capi.add(grads[st.a], ga)
-        grads[st.b] = gb if grads[st.b] is None else capi.add(grads[st.b], gb)
-        grads[c_id] = None
+        # H_A = contract(H_C, B) and H_B = contract(A, H_C), each in its
+        # operand's label order.
+        for i, x, lx, sx, y, ly, sy, target in (
+                (st.a, hc, lc, sc, vals[st.b], lb, sb, la),
+                (st.b, vals[st.a], la, sa, hc, lc, sc, lb)):
+            if not need[i]:
+                continue
+            first = hs[i] is None
+            h = _operand_h(x, lx, sx, y, ly, sy, target, precision,
+                           slots.get(i) if first else None)
+            if first:
+                hs[i] = h
+            elif i in slots:
+                slots[i].copy_(capi.add(hs[i], h))
+            else:
+                hs[i] = capi.add(hs[i], h)
+        hs[c_id] = None
         vals[c_id] = None
-    return grads[: plan.num_leaves]
+    return hs[: plan.num_leaves]
+
+
+def _backward(plan: ContractionPlan, vals, grad_out, precision: int, leaf_needs=None):
+    """Leaf gradients (None where `leaf_needs` is false) from the result's.
+    The leaves' conjugated gradients are written into one flat buffer and
+    conjugated by one launch."""
+    if leaf_needs is None:
+        leaf_needs = [True] * plan.num_leaves
+    sizes = [int(np.prod(plan.shapes[i])) if len(plan.shapes[i]) else 1
+             for i in range(plan.num_leaves)]
+    at, total = {}, 0
+    for i in range(plan.num_leaves):
+        if leaf_needs[i]:
+            at[i] = total
+            total += sizes[i]
+    flat = torch.empty(max(total, 1), dtype=grad_out.dtype, device=grad_out.device)
+    slots = {i: flat[o: o + sizes[i]] for i, o in at.items()}
+    hs = _backward_conj(plan, vals, capi.conj(grad_out), precision, _needs(plan, leaf_needs),
+                        slots)
+    grads = capi.conj(flat)
+    return [None if h is None else grads[at[i]: at[i] + sizes[i]] for i, h in enumerate(hs)]
 
 
 class SlicedPlan:
@@ -246,22 +315,28 @@ def _sliced_forward(sp: SlicedPlan, leaves, precision: int):
     return total
 
 
-def _sliced_backward(sp: SlicedPlan, leaves, grad_out, precision: int):
-    grads = [None] * sp.full.num_leaves
+def _sliced_backward(sp: SlicedPlan, leaves, grad_out, precision: int, leaf_needs=None):
+    """Per slice the conjugated leaf gradients, summed over the slices (into
+    the full leaves' positions), then conjugated once."""
+    if leaf_needs is None:
+        leaf_needs = [True] * sp.full.num_leaves
+    need = _needs(sp.sub, leaf_needs)
+    h_out = capi.conj(grad_out)
+    hs = [None] * sp.full.num_leaves
     for v in range(sp.num_slices):
         vals = _forward(sp.sub, sp.gather(leaves, v), precision, keep=True)
-        g = _backward(sp.sub, vals, grad_out, precision)
-        for i, gi in enumerate(g):
-            if gi is None:
+        h = _backward_conj(sp.sub, vals, h_out, precision, need)
+        for i, hi in enumerate(h):
+            if hi is None:
                 continue
             if not sp.leaf_axes[i]:
-                grads[i] = gi if grads[i] is None else capi.add(grads[i], gi)
+                hs[i] = hi if hs[i] is None else capi.add(hs[i], hi)
                 continue
-            if grads[i] is None:
-                grads[i] = torch.zeros_like(leaves[i])
-            capi.slice_scatter_add(gi, sp.full.shapes[i], sp.leaf_axes[i], sp.leaf_strides[i], v,
-                                   grads[i])
-    return grads
+            if hs[i] is None:
+                hs[i] = torch.zeros_like(leaves[i])
+            capi.slice_scatter_add(hi, sp.full.shapes[i], sp.leaf_axes[i], sp.leaf_strides[i], v,
+                                   hs[i])
+    return [None if h is None else capi.conj(h) for h in hs]
 
 
 class _NetworkContraction(torch.autograd.Function):
@@ -284,11 +359,12 @@ class _NetworkContraction(torch.autograd.Function):
     def backward(ctx, grad_out):
         leaves = [l.contiguous().reshape(-1) for l in ctx.saved_tensors]
         g = grad_out.contiguous().reshape(-1).to(leaves[0].dtype)
+        needs = ctx.needs_input_grad[2:]
         if isinstance(ctx.plan, SlicedPlan):
-            grads = _sliced_backward(ctx.plan, leaves, g, ctx.precision)
+            grads = _sliced_backward(ctx.plan, leaves, g, ctx.precision, needs)
         else:
             vals = _forward(ctx.plan, leaves, ctx.precision, keep=True)
-            grads = _backward(ctx.plan, vals, g, ctx.precision)
+            grads = _backward(ctx.plan, vals, g, ctx.precision, needs)
         out = [None if gr is None else gr.reshape(s) for gr, s in zip(grads, ctx.leaf_shapes)]
         return (None, None, *out)
 
