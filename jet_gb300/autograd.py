@@ -175,39 +175,47 @@ def _needs(plan: ContractionPlan, leaf_needs) -> List[bool]:
 
 def _backward_conj(plan: ContractionPlan, vals, h_out, precision: int, need, slots=None):
     """The reverse sweep over conjugated gradients: H of every leaf (None
-    where no gradient is needed), from H of the result. `slots` (optional):
-    per leaf, the place to write its H (one contribution per leaf: the path
-    consumes each node once)."""
+    where no gradient is needed), from H of the result. A leaf's H comes in
+    the leaf's label order (into `slots[leaf]` when given: one contribution
+    per leaf, as the path consumes each node once); an intermediate's H stays
+    in the label order its contraction produced, since it is only read again
+    as an operand of contractions, which take any axis order."""
     slots = slots or {}
-    hs = [None] * len(vals)
-    hs[-1] = h_out
+    hs = [None] * len(vals)  # (tensor, labels, shape)
+    hs[-1] = (h_out, plan.labels[-1], plan.shapes[-1])
     for idx in range(len(plan.steps) - 1, -1, -1):
         st = plan.steps[idx]
         c_id = plan.num_leaves + idx
-        hc = hs[c_id]
-        if hc is None:
+        if hs[c_id] is None:
             continue
-        la, lb, lc = plan.labels[st.a], plan.labels[st.b], plan.labels[c_id]
-        sa, sb, sc = plan.shapes[st.a], plan.shapes[st.b], plan.shapes[c_id]
-        # H_A = contract(H_C, B) and H_B = contract(A, H_C), each in its
-        # operand's label order.
-        for i, x, lx, sx, y, ly, sy, target in (
-                (st.a, hc, lc, sc, vals[st.b], lb, sb, la),
-                (st.b, vals[st.a], la, sa, hc, lc, sc, lb)):
+        hc, lc, sc = hs[c_id]
+        la, lb = plan.labels[st.a], plan.labels[st.b]
+        sa, sb = plan.shapes[st.a], plan.shapes[st.b]
+        # H_A = contract(H_C, B) and H_B = contract(A, H_C).
+        for i, x, lx, sx, y, ly, sy in ((st.a, hc, lc, sc, vals[st.b], lb, sb),
+                                        (st.b, vals[st.a], la, sa, hc, lc, sc)):
             if not need[i]:
                 continue
             first = hs[i] is None
-            h = _operand_h(x, lx, sx, y, ly, sy, target, precision,
-                           slots.get(i) if first else None)
-            if first:
-                hs[i] = h
-            elif i in slots:
-                slots[i].copy_(capi.add(hs[i], h))
+            if i < plan.num_leaves:
+                target = plan.labels[i]
+                h = _operand_h(x, lx, sx, y, ly, sy, target, precision,
+                               slots.get(i) if first else None)
+                lh, sh = target, plan.shapes[i]
             else:
-                hs[i] = capi.add(hs[i], h)
+                h, lh, sh = _contract(x, lx, sx, y, ly, sy, precision)
+            if first:
+                hs[i] = (h, lh, sh)
+                continue
+            prev, lp, sp = hs[i]
+            h = capi.add(prev, _to_order(h, lh, sh, lp))
+            if i in slots:
+                slots[i].copy_(h)
+                h = slots[i]
+            hs[i] = (h, lp, sp)
         hs[c_id] = None
         vals[c_id] = None
-    return hs[: plan.num_leaves]
+    return [None if h is None else h[0] for h in hs[: plan.num_leaves]]
 
 
 def _backward(plan: ContractionPlan, vals, grad_out, precision: int, leaf_needs=None):
