@@ -48,7 +48,7 @@ from typing import List, Sequence, Tuple
 import numpy as np
 import torch
 
-from . import capi
+from . import capi, grouped
 
 
 @dataclasses.dataclass
@@ -77,6 +77,10 @@ class ContractionPlan:
             for x, d in zip(lab, sh):
                 self.dims[x] = int(d)
         self.steps: List[_Step] = []
+        # Grouped launches of tiny steps (jet_gb300.grouped), per (dtype,
+        # device): on by default; off runs every step as its own launch.
+        self.grouping = True
+        self._grouped = {}
         for a, b in path:
             la, lb = self.labels[a], self.labels[b]
             sb, sa = set(lb), set(la)
@@ -150,7 +154,33 @@ def _operand_h(x, x_labels, x_shape, y, y_labels, y_shape, target, precision, sl
     return _to_order(h, lh, sh, target, out=slot)
 
 
+def _grouped_for(plan: ContractionPlan, like, precision: int):
+    """The plan's grouped evaluation for tensors like `like`, or None (not
+    in the plain forms, grouping off, the plan unsuited, or first asked
+    inside a CUDA graph capture, where it cannot be built)."""
+    if (not plan.grouping or precision not in (capi.PREC_FP32, capi.PREC_AUTO)
+            or like.dtype not in (torch.complex64, torch.complex128)):
+        return None
+    key = (like.dtype, str(like.device))
+    if key in plan._grouped:
+        return plan._grouped[key]
+    if grouped.capturing(like.device):
+        return None
+    try:
+        g = grouped.Grouped(plan, like.dtype, like.device)
+    except grouped.NoGroup:
+        g = None
+    plan._grouped[key] = g
+    return g
+
+
 def _forward(plan: ContractionPlan, leaves, precision: int, keep: bool):
+    g = _grouped_for(plan, leaves[0], precision)
+    if g is not None:
+        vals = g.run_forward(leaves, precision)
+        if not keep:  # the arena is overwritten by the next evaluation
+            vals[-1] = vals[-1].clone()
+        return vals
     vals = list(leaves)
     for st in plan.steps:
         out = capi.contract(vals[st.a], plan.shapes[st.a], st.a_perm, vals[st.b],
@@ -224,6 +254,12 @@ def _backward(plan: ContractionPlan, vals, grad_out, precision: int, leaf_needs=
     conjugated by one launch."""
     if leaf_needs is None:
         leaf_needs = [True] * plan.num_leaves
+    g = _grouped_for(plan, grad_out, precision)
+    if g is not None:  # `vals` are then the values run_forward left in its arena
+        try:
+            return g.run_backward(grad_out, _needs(plan, leaf_needs), precision)
+        except grouped.NoGroup:
+            pass
     sizes = [int(np.prod(plan.shapes[i])) if len(plan.shapes[i]) else 1
              for i in range(plan.num_leaves)]
     at, total = {}, 0

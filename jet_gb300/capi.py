@@ -347,6 +347,13 @@ def contract_group(tasks, stream=None):
     return raw
 
 
+def contract_group_at(tasks_ptr: int, n_tasks: int, total_tiles: int, dtype_c: int,
+                      stream=None) -> None:
+    """jetgpu_contract_group on a task array already on the device (its
+    address, task count, summed jetgpu_group_tiles and dtype code)."""
+    check(lib.jetgpu_contract_group(tasks_ptr, n_tasks, total_tiles, dtype_c, _stream(stream)))
+
+
 def split_tf32(x, shape, perm, rows, cols, pitch, planes, scale_exp=0, n_planes=4,
                stream=None):
     """Permute + TF32 hi/lo split into 4 (or 6) planes of rows x pitch floats."""

@@ -46,6 +46,19 @@ class _Stand:
         self.calls["add"] += 1
         return _into(a + b, out)
 
+    def launch_group(self, group):
+        """jetgpu_contract_group: out[i, j] = sum_c x[a_row[i] + a_col[c]]
+        y[b_row[c] + b_col[j]] for every task, read through its tables."""
+        self.calls["group"] += 1
+        self.calls["grouped_tasks"] += len(group.tasks)
+        for t in group.tasks:
+            op = t["op"]
+            ar, ac, br, bc = (torch.as_tensor(x) for x in t["tables"])
+            x, y = group.view(op.x), group.view(op.y)
+            X = x[ar[:, None] + ac[None, :]]
+            Y = y[br[:, None] + bc[None, :]]
+            group.view(op.out)[: op.m * op.n] = (X @ Y).reshape(-1)
+
     @staticmethod
     def _index(shape, axes, strides, v):
         idx = [slice(None)] * len(shape)
@@ -67,11 +80,12 @@ class _Stand:
 
 @pytest.fixture
 def stand(monkeypatch):
-    from jet_gb300 import capi
+    from jet_gb300 import capi, grouped
 
     s = _Stand()
     for name in ("contract", "permute", "conj", "add", "slice_gather", "slice_scatter_add"):
         monkeypatch.setattr(capi, name, getattr(s, name))
+    monkeypatch.setattr(grouped, "launch_group", s.launch_group)
     return s
 
 
@@ -99,7 +113,7 @@ def _einsum_loss(leaves, labels, path):
     return vals[-1].real.reshape(())
 
 
-def _grads(spec, path, th, ph, via, **kw):
+def _grads(spec, path, th, ph, via, grouping=False, **kw):
     from jet_gb300 import autograd, expectation as ex
 
     t = torch.tensor(th, requires_grad=True)
@@ -107,6 +121,10 @@ def _grads(spec, path, th, ph, via, **kw):
     lv = ex.build_leaves(spec, t, p, dtype=torch.complex128)
     labels = [l.labels for l in spec]
     if via == "adjoint":
+        if "sliced" not in kw:
+            plan = autograd.ContractionPlan(labels, [l.shape for l in spec], path)
+            plan.grouping = grouping
+            kw["plan"] = plan
         loss = autograd.contract_network(lv, labels, path, precision=0, **kw).real
     else:
         loss = _einsum_loss(lv, labels, path)
@@ -164,3 +182,47 @@ def test_leaves_without_grad_get_none(stand):
     for x, r in zip(leaves, ref):
         if x.requires_grad:
             torch.testing.assert_close(x.grad, r.grad, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 3), (3, 3, 4)])
+def test_grouped_levels_match_einsum_autograd(stand, shape):
+    """The tiny steps of each dependency level in one grouped launch (tables
+    read through by the stand-in), forward and reverse sweep; the same plan
+    evaluated twice reuses its arenas and task tables."""
+    from jet_gb300 import autograd, expectation as ex
+
+    spec, path, th, ph = _network(*shape, seed=11)
+    labels = [l.labels for l in spec]
+    plan = autograd.ContractionPlan(labels, [l.shape for l in spec], path)
+    want, wt, wp = _grads(spec, path, th, ph, "einsum")
+    for rep in range(2):
+        stand.calls.clear()
+        t = torch.tensor(th, requires_grad=True)
+        p = torch.tensor(ph, requires_grad=True)
+        lv = ex.build_leaves(spec, t, p, dtype=torch.complex128)
+        loss = autograd.contract_network(lv, labels, path, precision=0, plan=plan).real
+        loss.backward()
+        assert abs(float(loss.detach()) - want) <= 1e-14
+        torch.testing.assert_close(t.grad, wt, rtol=0, atol=1e-13)
+        torch.testing.assert_close(p.grad, wp, rtol=0, atol=1e-13)
+        calls = dict(stand.calls)
+        steps = len(path)
+        # Forward, recomputation and the adjoint's contractions nearly all
+        # grouped: far fewer launches than steps.
+        assert calls["group"] > 0 and calls["grouped_tasks"] > steps
+        assert calls.get("contract", 0) + calls["group"] < steps
+        assert calls["conj"] == 2
+    g = plan._grouped[(torch.complex128, "cpu")]
+    assert g is not None and len(g.backward_schedules) == 1
+
+
+def test_grouping_off_runs_step_by_step(stand):
+    spec, path, th, ph = _network(2, 3, 3, seed=2)
+    _grads(spec, path, th, ph, "adjoint", grouping=False)
+    assert stand.calls["group"] == 0
+    want = _grads(spec, path, th, ph, "einsum")
+    stand.calls.clear()
+    got = _grads(spec, path, th, ph, "adjoint", grouping=True)
+    assert stand.calls["group"] > 0
+    assert abs(got[0] - want[0]) <= 1e-14
+    torch.testing.assert_close(got[1], want[1], rtol=0, atol=1e-13)
