@@ -1,8 +1,8 @@
 """Grouped launches for the differentiable contraction (jet_gb300.autograd).
 
-A light-cone network such as config 3's (679 steps, 668 of them tiny) has
-few dependency levels (23): the steps of one level read only values of lower
-levels. Launched one by one, each step costs a launch of a few microseconds
+A light-cone expectation network such as <Z_i Z_j> of a 6 x 6, 10-layer
+RX-RZ-CZ circuit (679 steps, 668 of them tiny) has few dependency levels
+(23): the steps of one level read only values of lower levels. Launched one by one, each step costs a launch of a few microseconds
 of device time, which is nearly all of its time. Here the tiny steps of a
 level (m n k below 131,072 and k <= 64, the bound by which the
 TaskBasedContractor's replay groups) share one jetgpu_contract_group launch,

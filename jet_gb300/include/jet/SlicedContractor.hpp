@@ -38,6 +38,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "GroupSchedule.hpp"
 #include "PathInfo.hpp"
 #include "Tensor.hpp"
 #include "TensorNetwork.hpp"
@@ -523,36 +524,31 @@ template <class T = std::complex<float>> class SlicedContractor {
             result_size_ *= fin.dims[j];
         }
         final_perm_needed_ = spos > 0 && spos < (int)fin.labels.size();
-        // What a chunk replays: consecutive independent tiny steps become one
-        // grouped launch; every other step is its own item.
+        // What a chunk replays: the tiny steps of a run, level by level, in
+        // grouped launches (group_schedule::Items); every other step is its
+        // own item. A level of one step keeps its own launch (split-k, tuned
+        // forms).
         items_.clear();
         {
-            std::vector<int> group;
-            std::vector<int> group_outs;
-            auto flush = [&] { // a lone step keeps its own launch (split-k, tuned forms)
-                if (group.size() == 1)
-                    items_.push_back(Item{group, false});
-                else if (!group.empty())
-                    items_.push_back(Item{group, true});
-                group.clear();
-                group_outs.clear();
-            };
-            for (size_t i = 0; i < steps_.size(); ++i) {
-                const Step &st = steps_[i];
-                if (!st.chunk)
-                    continue;
-                if (!Groupable(st)) {
-                    flush();
-                    items_.push_back(Item{{(int)i}, false});
-                    continue;
-                }
-                if (InVector(st.a, group_outs) || InVector(st.b, group_outs) ||
-                    group.size() >= 256)
-                    flush();
-                group.push_back((int)i);
-                group_outs.push_back(st.out);
+            std::vector<int> chunk_steps;
+            for (size_t i = 0; i < steps_.size(); ++i)
+                if (steps_[i].chunk)
+                    chunk_steps.push_back((int)i);
+            std::vector<char> groupable(chunk_steps.size());
+            std::vector<std::array<size_t, 2>> inputs(chunk_steps.size());
+            std::vector<size_t> outputs(chunk_steps.size());
+            for (size_t j = 0; j < chunk_steps.size(); ++j) {
+                const Step &st = steps_[chunk_steps[j]];
+                groupable[j] = Groupable(st);
+                inputs[j] = {(size_t)st.a, (size_t)st.b};
+                outputs[j] = (size_t)st.out;
             }
-            flush();
+            for (const auto &item : group_schedule::Items(groupable, inputs, outputs, 256)) {
+                std::vector<int> ids;
+                for (size_t j : item)
+                    ids.push_back(chunk_steps[j]);
+                items_.push_back(Item{ids, ids.size() > 1});
+            }
         }
         // Chunk arena: liveness-planned offsets (first fit, 256-byte aligned)
         // over the items: a group's outputs are all live while it runs.

@@ -36,6 +36,7 @@
 #include <unordered_set>
 #include <vector>
 
+#include "GroupSchedule.hpp"
 #include "PathInfo.hpp"
 #include "Tensor.hpp"
 #include "TensorNetwork.hpp"
@@ -52,45 +53,30 @@ struct StepShape {
     uint64_t m, n, k;
 };
 
-// Launch items in step order: one step, or (when `enabled`) a run of tiny
-// steps -- m n k below `max_work` and k <= 64 -- that read none of the run's
-// own outputs, at most 256 per run (a grouped launch's task limit).
+// Launch items: one step, or (when `enabled`) a level of a run of tiny steps
+// -- m n k below `max_work` and k <= 64 -- none of which reads another's
+// output, at most 256 per item (a grouped launch's task limit); see
+// group_schedule::Items for the order.
 inline std::vector<std::vector<size_t>> GroupTinySteps(const std::vector<StepShape> &steps,
                                                        bool enabled, double max_work)
 {
-    std::vector<std::vector<size_t>> items;
-    std::vector<size_t> group, group_outs;
-    auto flush = [&] {
-        if (!group.empty())
-            items.push_back(group);
-        group.clear();
-        group_outs.clear();
-    };
+    std::vector<char> groupable(steps.size());
+    std::vector<std::array<size_t, 2>> inputs(steps.size());
+    std::vector<size_t> outputs(steps.size());
     for (size_t i = 0; i < steps.size(); ++i) {
         const StepShape &st = steps[i];
-        const bool tiny = enabled && st.k <= 64 &&
-                          (double)st.m * (double)st.n * (double)st.k < max_work;
-        if (!tiny) {
-            flush();
-            items.push_back({i});
-            continue;
-        }
-        const bool reads_group =
-            std::find(group_outs.begin(), group_outs.end(), st.a) != group_outs.end() ||
-            std::find(group_outs.begin(), group_outs.end(), st.b) != group_outs.end();
-        if (reads_group || group.size() >= 256)
-            flush();
-        group.push_back(i);
-        group_outs.push_back(st.out);
+        groupable[i] = enabled && st.k <= 64 &&
+                       (double)st.m * (double)st.n * (double)st.k < max_work;
+        inputs[i] = {st.a, st.b};
+        outputs[i] = st.out;
     }
-    flush();
-    return items;
+    return group_schedule::Items(groupable, inputs, outputs, 256);
 }
 
 // First-fit arena offsets (256-byte aligned) of every step output, over its
-// lifetime: from its item to the item of its last consumer (never, for an
+// lifetime: from its item to the last item that reads it (never, for an
 // output no step reads). An item's outputs are all allocated before any input
-// it consumes for the last time is released: a grouped launch runs its steps
+// it reads for the last time is released: a grouped launch runs its steps
 // together. Leaves (leaf_of >= 0) live outside the arena. Returns the arena's
 // size; offset[b] is set for every step output b.
 inline size_t PlanArena(const std::vector<StepShape> &steps,
@@ -99,11 +85,12 @@ inline size_t PlanArena(const std::vector<StepShape> &steps,
                         std::vector<size_t> &offset)
 {
     const size_t nb = leaf_of.size();
-    std::vector<int> last(nb, -1);
-    for (size_t i = 0; i < steps.size(); ++i) {
-        last[steps[i].a] = (int)i;
-        last[steps[i].b] = (int)i;
-    }
+    std::vector<long> last(nb, -1); // the last item reading each buffer
+    for (size_t t = 0; t < items.size(); ++t)
+        for (size_t i : items[t]) {
+            last[steps[i].a] = std::max(last[steps[i].a], (long)t);
+            last[steps[i].b] = std::max(last[steps[i].b], (long)t);
+        }
     offset.assign(nb, 0);
     std::map<size_t, size_t> free_blocks;
     size_t top = 0;
@@ -136,13 +123,15 @@ inline size_t PlanArena(const std::vector<StepShape> &steps,
             }
         }
     };
-    for (const auto &item : items) {
-        for (size_t i : item)
+    for (size_t t = 0; t < items.size(); ++t) {
+        for (size_t i : items[t])
             offset[steps[i].out] = alloc(bytes[steps[i].out]);
-        for (size_t i : item)
+        for (size_t i : items[t])
             for (size_t in : {steps[i].a, steps[i].b})
-                if (leaf_of[in] < 0 && last[in] == (int)i)
+                if (leaf_of[in] < 0 && last[in] == (long)t) {
                     release(offset[in], bytes[in]);
+                    last[in] = -2; // released once
+                }
     }
     return top;
 }
