@@ -304,6 +304,7 @@ class SlicedPlan:
             labels.append([x for x in lab if x not in pos])
             shapes.append([d for x, d in zip(lab, sh) if x not in pos])
         self.sub = ContractionPlan(labels, shapes, path)
+        self.sub.grouping = plan.grouping
 
     def gather(self, leaves, v: int):
         """The leaves of slice value v (flat device tensors)."""
@@ -424,13 +425,18 @@ def contract_network(leaves: Sequence[torch.Tensor], labels: Sequence[Sequence[s
     and forward and backward run (and recompute) one slice at a time.
     memory_budget: device bytes for one slice's checkpointed backward; picks
     `sliced` (slices_for_budget) when `sliced` is not given. `plan` (a
-    ContractionPlan, or the SlicedPlan these build) skips the bookkeeping."""
+    ContractionPlan, or the SlicedPlan these build) skips the bookkeeping;
+    reused across calls in a plain form (FP32, AUTO), it also runs the tiny
+    steps of each dependency level as one grouped launch (jet_gb300.grouped)
+    over device arenas it owns, so its evaluations must not overlap in time.
+    A call without a plan runs every step as its own launch."""
     if plan is None:
         shapes = [list(l.shape) for l in leaves]
         if sliced is None and memory_budget is not None:
             sliced = slices_for_budget(labels, shapes, path, memory_budget,
                                        leaves[0].element_size())
         plan = ContractionPlan(labels, shapes, path)
+        plan.grouping = False  # made for this call: a grouped schedule would not be reused
         if sliced:
             plan = SlicedPlan(plan, path, sliced)
     return _NetworkContraction.apply(plan, precision, *leaves)

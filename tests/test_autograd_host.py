@@ -121,7 +121,7 @@ def _grads(spec, path, th, ph, via, grouping=False, **kw):
     lv = ex.build_leaves(spec, t, p, dtype=torch.complex128)
     labels = [l.labels for l in spec]
     if via == "adjoint":
-        if "sliced" not in kw:
+        if "plan" not in kw and "sliced" not in kw:
             plan = autograd.ContractionPlan(labels, [l.shape for l in spec], path)
             plan.grouping = grouping
             kw["plan"] = plan
@@ -151,15 +151,22 @@ def test_adjoint_matches_einsum_autograd(stand, shape):
     assert calls["contract"] >= 2 * steps + sum(1 for l in spec if l.kind != "const")
 
 
-def test_sliced_adjoint_matches_einsum_autograd(stand):
-    from jet_gb300 import circuits, expectation as ex
+@pytest.mark.parametrize("grouping", [True, False])
+def test_sliced_adjoint_matches_einsum_autograd(stand, grouping):
+    """Slice by slice, the sliced network's plan grouped (its forward and the
+    recomputation in grouped launches) or not."""
+    from jet_gb300 import autograd, circuits, expectation as ex
 
     spec, path, th, ph = _network(2, 3, 3, seed=4)
     net = ex.numeric_network(spec, th, ph)
     sliced = circuits.choose_slices(net, path, 2)
     assert sliced
-    loss, gt, gp = _grads(spec, path, th, ph, "adjoint", sliced=sliced)
+    plan = autograd.ContractionPlan([l.labels for l in spec], [l.shape for l in spec], path)
+    plan.grouping = grouping
+    sp = autograd.SlicedPlan(plan, path, sliced)
+    loss, gt, gp = _grads(spec, path, th, ph, "adjoint", sliced=sliced, plan=sp)
     assert stand.calls["slice_scatter_add"] > 0
+    assert (stand.calls["group"] > 0) == grouping
     want, wt, wp = _grads(spec, path, th, ph, "einsum")
     assert abs(loss - want) <= 1e-14
     torch.testing.assert_close(gt, wt, rtol=0, atol=1e-13)

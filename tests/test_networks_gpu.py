@@ -167,9 +167,13 @@ def config3():
         return json.load(f)
 
 
+@pytest.mark.parametrize("grouping", [True, False])
 @pytest.mark.parametrize("dtype,precision,tol_grad,tol_loss", [
     ("complex64", 2, 1e-4, 1e-6), ("complex128", 0, 1e-10, 1e-12)])
-def test_config3_gradient_matches_einsum(jet, config3, dtype, precision, tol_grad, tol_loss):
+def test_config3_gradient_matches_einsum(jet, config3, dtype, precision, tol_grad, tol_loss,
+                                         grouping):
+    """Through a plan, with the tiny steps of each dependency level in
+    grouped launches and step by step."""
     import torch
 
     from jet_gb300 import autograd, expectation as ex
@@ -183,8 +187,10 @@ def test_config3_gradient_matches_einsum(jet, config3, dtype, precision, tol_gra
     t = torch.tensor(g["thetas"], dtype=real, device=dev, requires_grad=True)
     p = torch.tensor(g["phis"], dtype=real, device=dev, requires_grad=True)
     lv = ex.build_leaves(spec, t, p, dtype=getattr(torch, dtype), device=dev)
-    loss = autograd.contract_network(lv, [lf.labels for lf in spec], path,
-                                     precision=precision).real
+    labels = [lf.labels for lf in spec]
+    plan = autograd.ContractionPlan(labels, [lf.shape for lf in spec], path)
+    plan.grouping = grouping
+    loss = autograd.contract_network(lv, labels, path, precision=precision, plan=plan).real
     loss.backward()
     assert abs(float(loss.item()) - g["loss"]) <= tol_loss
     gt = t.grad.double().cpu().numpy()
