@@ -23,6 +23,8 @@ namespace {
 constexpr int kGT = 32;       // output tile edge
 constexpr int kGK = 32;       // k slice
 constexpr int kMaxTasks = 256; // tasks per launch
+constexpr int kGThreads = 256; // threads per CTA: one per task in the tile prefix scan
+static_assert(kGThreads == kMaxTasks, "the prefix scan reads one task per thread");
 
 template <typename T> struct V2;
 template <> struct V2<float> {
@@ -33,7 +35,7 @@ template <> struct V2<double> {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kGThreads)
     group_contract_kernel(const jetgpu_group_task *__restrict__ tasks, int n_tasks,
                           uint64_t total_tiles)
 {
@@ -41,16 +43,27 @@ __global__ void __launch_bounds__(256)
     __shared__ uint64_t first_tile[kMaxTasks + 1];
     __shared__ V As[kGK][kGT + 1];
     __shared__ V Bs[kGK][kGT + 1];
-    if (threadIdx.x == 0) {
-        uint64_t acc = 0;
-        for (int t = 0; t < n_tasks; ++t) {
-            first_tile[t] = acc;
-            const jetgpu_group_task &q = tasks[t];
-            acc += q.batch * ((q.m + kGT - 1) / kGT) * ((q.n + kGT - 1) / kGT);
+    // First tile of every task: thread t reads task t's tile count, then a
+    // block-wide inclusive scan (kMaxTasks = blockDim.x = 256: 8 rounds).
+    // One thread walking the tasks took 0.13 us a task, 30 us for 184.
+    {
+        const int tid = threadIdx.x;
+        uint64_t mine = 0;
+        if (tid < n_tasks) {
+            const jetgpu_group_task &q = tasks[tid];
+            mine = q.batch * ((q.m + kGT - 1) / kGT) * ((q.n + kGT - 1) / kGT);
         }
-        first_tile[n_tasks] = acc;
+        first_tile[tid + 1] = mine;
+        if (tid == 0)
+            first_tile[0] = 0;
+        __syncthreads();
+        for (int off = 1; off < kMaxTasks; off <<= 1) {
+            const uint64_t add = tid >= off ? first_tile[tid + 1 - off] : 0;
+            __syncthreads();
+            first_tile[tid + 1] += add;
+            __syncthreads();
+        }
     }
-    __syncthreads();
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16; // 2 x 2 outputs each
     int t = 0; // this CTA's tiles come in increasing order: the task only advances
     for (uint64_t g = blockIdx.x; g < total_tiles; g += gridDim.x) {
@@ -139,9 +152,9 @@ int jetgpu_contract_group(const jetgpu_group_task *tasks, int n_tasks, uint64_t 
     const unsigned grid = GridFor(total_tiles, 8);
     cudaStream_t st = AsStream(stream);
     if (dtype == JETGPU_C64)
-        group_contract_kernel<float><<<grid, 256, 0, st>>>(tasks, n_tasks, total_tiles);
+        group_contract_kernel<float><<<grid, kGThreads, 0, st>>>(tasks, n_tasks, total_tiles);
     else
-        group_contract_kernel<double><<<grid, 256, 0, st>>>(tasks, n_tasks, total_tiles);
+        group_contract_kernel<double><<<grid, kGThreads, 0, st>>>(tasks, n_tasks, total_tiles);
     return CheckLaunch("group_contract_kernel");
 }
 
