@@ -211,8 +211,8 @@ template <class T = std::complex<float>> class Tensor {
     // The label -> dimension map is built from the labels and shape when it
     // is first read (GetIndexToDimension, RenameIndex, ==), by the same rule
     // as the reference's constructor: a contraction step creates a tensor
-    // whose map nothing reads, and building it was a third of the step's
-    // host time.
+    // whose map nothing reads (building it cost about 1 us of host time for
+    // a rank-27 result).
     void InitIndicesAndShape(const std::vector<std::string> &indices,
                              const std::vector<size_t> &shape) noexcept
     {
