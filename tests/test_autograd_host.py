@@ -233,3 +233,25 @@ def test_grouping_off_runs_step_by_step(stand):
     assert stand.calls["group"] > 0
     assert abs(got[0] - want[0]) <= 1e-14
     torch.testing.assert_close(got[1], want[1], rtol=0, atol=1e-13)
+
+
+def test_schedule_refuses_tables_outside_their_regions():
+    """A grouped task whose offset tables or output would leave its arena
+    region is refused on the host (NoGroup) before anything is uploaded."""
+    from jet_gb300 import grouped
+
+    arenas = {"val": torch.zeros(64, dtype=torch.complex128)}
+    # x: a 2 x 4 tensor, y: 4 x 3, out: 2 x 3 -> m 2, n 3, k 4 (tiny).
+    good = [grouped.Op(("val", 0, 8), ["i", "c"], [2, 4], ("val", 8, 12), ["c", "j"], [4, 3],
+                       ("val", 20, 6)),
+            grouped.Op(("val", 26, 8), ["i", "c"], [2, 4], ("val", 34, 12), ["c", "j"], [4, 3],
+                       ("val", 46, 6))]
+    s = grouped.Schedule([good], arenas, torch.complex128, torch.device("cpu"))
+    assert [k for k, _ in s.items] == ["group"] and len(s.groups[0].tasks) == 2
+    for bad_x, bad_out in ((("val", 0, 7), ("val", 20, 6)),   # x region one short
+                           (("val", 0, 8), ("val", 20, 5)),   # out region one short
+                           (("val", 0, 8), ("val", 60, 6))):  # out past the arena
+        ops = [grouped.Op(bad_x, ["i", "c"], [2, 4], ("val", 8, 12), ["c", "j"], [4, 3],
+                          bad_out), good[1]]
+        with pytest.raises(grouped.NoGroup):
+            grouped.Schedule([ops], arenas, torch.complex128, torch.device("cpu"))
