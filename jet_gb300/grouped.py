@@ -44,10 +44,14 @@ def tiny(m: int, n: int, k: int) -> bool:
 def layout(a_labels, a_shape, b_labels, b_shape):
     """ContractTensors' view of a pairwise contraction (Tensor.hpp:708-752):
     (a_perm, b_perm, m, n, k, left count, common count, C labels, C shape)."""
-    sb, sa = set(b_labels), set(a_labels)
-    left = [x for x in a_labels if x not in sb]
-    right = [x for x in b_labels if x not in sa]
-    common = [x for x in a_labels if x in sb]
+    pa, pb = {}, {}  # first position of each label
+    for i, x in enumerate(a_labels):
+        pa.setdefault(x, i)
+    for i, x in enumerate(b_labels):
+        pb.setdefault(x, i)
+    left = [x for x in a_labels if x not in pb]
+    right = [x for x in b_labels if x not in pa]
+    common = [x for x in a_labels if x in pb]
     dims = dict(zip(a_labels, a_shape))
     dims.update(zip(b_labels, b_shape))
     m = n = k = 1
@@ -57,9 +61,8 @@ def layout(a_labels, a_shape, b_labels, b_shape):
         n *= dims[x]
     for x in common:
         k *= dims[x]
-    return ([a_labels.index(x) for x in left + common],
-            [b_labels.index(x) for x in common + right], m, n, k, len(left), len(common),
-            left + right, [dims[x] for x in left + right])
+    return ([pa[x] for x in left + common], [pb[x] for x in common + right], m, n, k,
+            len(left), len(common), left + right, [dims[x] for x in left + right])
 
 
 class NoGroup(Exception):
